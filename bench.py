@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""Benchmark of the CRT-NTT big-integer multiply on one GB300.
+
+Workload (default): one multiply of two seeded uniform-random operands of
+2^28 32-bit limbs (1 GiB each), transform length N = 2^29 per prime over the
+three primes 2^64 - 2^b + 1 (b = 32, 34, 40), uint64 residues. A step is one
+full multiply (decomposition, 2 x 3 forward transforms, pointwise product,
+3 inverse transforms, Garner + carry). Inputs (2 x 1 GiB) and the 24 GiB of
+spectra are far larger than the 129 MB L2, so no L2 flush is needed between
+steps.
+
+Prints one JSON line. ``value`` is milliseconds per multiply with the
+operands already resident in HBM (CUDA events on the engine stream); ``e2e``
+is the same metric through the reference-facing C-ABI call ntt_bigint_mul on
+pinned host BigInts (2 GiB in, 2 GiB out per step, host wall clock).
+``--impl reference`` times the reference CPU path (the oracle restatement of
+the reference's scatter / NTT / Garner / gather, all host threads) on a
+bounded sample and scales it to the same metric.
+
+Under torchrun (--gpus N > 1) every rank runs an independent replica on its
+own GPU (the multiply does not shard across GPUs); ``value`` is then the
+max-over-ranks step time divided by the number of multiplies all ranks did.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms per 2^28-limb multiply (% HBM roofline)"
+UNIT = "ms"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--log-limbs", type=int, default=28, help="operand size 2^k limbs (28 = headline)")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-log-limbs", type=int, default=23, help="CPU baseline sample size 2^k limbs")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    """Barrier and max-reduction across ranks (gloo over torch.distributed)
+    for N > 1; no-ops for a single process."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = dist_env()
+        self.torch = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.torch, self.td = torch, td
+
+    def barrier(self):
+        if self.torch:
+            self.td.barrier()
+
+    def max(self, v):
+        if not self.torch:
+            return v
+        t = self.torch.tensor([float(v)], dtype=self.torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.torch:
+            self.td.destroy_process_group()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def bytes_model(log_limbs):
+    """Whole-multiply algorithmic bytes: 10 k N 8 + 8 (n_a + n_b), k = 3."""
+    n = 1 << log_limbs
+    N = 1 << (log_limbs + 1)
+    return 10 * 3 * N * 8 + 8 * (2 * n)
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.gpu = gpu_index
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9], float(parts[3])))
+            except ValueError:
+                continue
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[2][i].lower() == "active"})
+        sm = sorted(r[0] for r in rows)
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(r[3] for r in rows)}
+
+
+def host_info():
+    model = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part", "hardware")):
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    return {"nproc": os.cpu_count(), "arch": os.uname().machine, "cpu": model,
+            "omp_num_threads": os.environ.get("OMP_NUM_THREADS")}
+
+
+def cpu_baseline(log_limbs_sample, log_limbs_target, reps=1):
+    """Oracle CRT-NTT (restatement of the reference CPU path) on one bounded
+    sample, all host threads, scaled to the target size by N log N."""
+    import oracle
+    from cryptography_gb300 import synth
+    n = 1 << log_limbs_sample
+    a = synth.operand(n, 101)
+    b = synth.operand(n, 202)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        oracle.mul(a, b)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    Ns, Nt = 2 * n, 1 << (log_limbs_target + 1)
+    scale = (Nt * (log_limbs_target + 1)) / (Ns * (log_limbs_sample + 1))
+    out = {"value": t * 1e3 * scale, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+           "sample": "one 2^%d x 2^%d-limb multiply by the oracle CRT-NTT (scatter, radix-2 NTT per prime, "
+                     "Garner, gather; OpenMP) took %.2f s; scaled by N log N (x%.1f) to 2^%d limbs"
+                     % (log_limbs_sample, log_limbs_sample, t, scale, log_limbs_target),
+           "host": host_info()}
+    if oracle.gmp_available():
+        t0 = time.perf_counter()
+        oracle.gmp_mul(a, b)
+        tg = time.perf_counter() - t0
+        out["gmp_mpz_mul_1thread_sample_s"] = tg
+    return out
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return 0
+    times = []
+    res = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(args.cpu_log_limbs, args.log_limbs)
+        if i >= args.warmup:
+            times.append(r["value"])
+            res = r
+    v = float(np.median(times))
+    res["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded splitmix64 limbs)",
+            "config": {"workload": "2^%d x 2^%d 32-bit limbs, N=2^%d, 3 primes" % (args.log_limbs, args.log_limbs,
+                                                                                    args.log_limbs + 1),
+                       "sample_log_limbs": args.cpu_log_limbs},
+            "cpu_baseline": res, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, dist):
+    import cryptography_gb300 as g
+    from cryptography_gb300 import cudart, synth
+
+    cudart.set_device(dist.local)
+    lg = args.log_limbs
+    n = 1 << lg
+    g.init(lg + 1)
+    stream = g.lib().gbntt_stream()
+    a = synth.operand(n, 1 + 2 * dist.rank)
+    b = synth.operand(n, 2 + 2 * dist.rank)
+    da, db, dc = cudart.DeviceBuffer(4 * n), cudart.DeviceBuffer(4 * n), cudart.DeviceBuffer(8 * n)
+    da.upload(a)
+    db.upload(b)
+
+    def step():
+        g.mul_device(dc.ptr, da.ptr, n, db.ptr, n, None)
+
+    for _ in range(args.warmup):
+        step()
+    cudart.stream_sync(stream)
+    flags = g.device_errors()
+
+    clocks = ClockSampler(dist.local)
+    dist.barrier()
+    cudart.synchronize()
+    e0, e1 = cudart.Event(), cudart.Event()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    cudart.synchronize()
+    dist.barrier()
+    total_ms = e0.elapsed_ms(e1)
+    clk = clocks.stop()
+    flags |= g.device_errors()
+    total_ms = dist.max(total_ms)
+    ms = total_ms / (args.steps * dist.world)
+
+    # per-launch breakdown of one multiply (separate, instrumented run)
+    g.launch_log(True)
+    step()
+    recs = g.launch_records()
+    g.launch_log(False)
+    launches_per_step = len(recs)
+    by_kind = {}
+    for kind, log_l, nbytes, t in recs:
+        d = by_kind.setdefault(kind, {"launches": 0, "ms": 0.0, "bytes": 0.0})
+        d["launches"] += 1
+        d["ms"] += t
+        d["bytes"] += nbytes
+    tot = sum(d["ms"] for d in by_kind.values()) or 1.0
+    for d in by_kind.values():
+        d["share"] = d["ms"] / tot
+        d["GBps"] = d["bytes"] / (d["ms"] * 1e-3) / 1e9 if d["ms"] > 0 else None
+    pass_kinds = [k for k in by_kind if "pass" in k]
+    pass_ms = sum(by_kind[k]["ms"] for k in pass_kinds)
+    pass_bytes = sum(by_kind[k]["bytes"] for k in pass_kinds)
+    pass_launches = sum(by_kind[k]["launches"] for k in pass_kinds)
+    peak, peak_kind = peaks()
+    achieved = pass_bytes / (pass_ms * 1e-3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("ntt_pass_kernel_bytes_per_launch")
+        except (ValueError, OSError):
+            traffic = None
+    bm = bytes_model(lg)
+
+    # e2e through the reference-facing C ABI with pinned host BigInts
+    e2e = None
+    if args.e2e_steps > 0:
+        n64 = n // 2
+        pa, pb = cudart.PinnedBuffer(n64, np.uint64), cudart.PinnedBuffer(n64, np.uint64)
+        pc = cudart.PinnedBuffer(2 * n64 + 8, np.uint64)
+        pa.array[:] = a.view(np.uint64)
+        pb.array[:] = b.view(np.uint64)
+        u64p = ctypes.POINTER(ctypes.c_uint64)
+        A = g.BigInt(ctypes.cast(pa.ptr, u64p), n64, n64, 0)
+        B = g.BigInt(ctypes.cast(pb.ptr, u64p), n64, n64, 0)
+        C = g.BigInt(ctypes.cast(pc.ptr, u64p), 0, 2 * n64 + 8, 0)
+        L = g.lib()
+        L.ntt_bigint_mul(ctypes.byref(C), ctypes.byref(A), ctypes.byref(B))
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            L.ntt_bigint_mul(ctypes.byref(C), ctypes.byref(A), ctypes.byref(B))
+        t_e2e = (time.perf_counter() - t0) * 1e3
+        dist.barrier()
+        t_e2e = dist.max(t_e2e)
+        e2e = {"value": t_e2e / (args.e2e_steps * dist.world), "unit": UNIT, "h2d_bytes_per_step": 8 * n,
+               "d2h_bytes_per_step": 8 * n, "api": "ntt_bigint_mul (pinned host BigInts)",
+               "steps": args.e2e_steps}
+        if C.cap != 2 * n64 + 8 or C.n_limbs != 2 * n64:
+            e2e["warning"] = "unexpected output size"
+        for p_ in (pa, pb, pc):
+            p_.free()
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu:
+        try:
+            cpu = cpu_baseline(args.cpu_log_limbs, lg)
+        except Exception as ex:   # the baseline is reported, never required
+            cpu = {"error": str(ex)}
+
+    line = {
+        "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded splitmix64 limbs; inputs resident in HBM)",
+        "config": {"workload": "multiply 2^%d x 2^%d 32-bit limbs, NTT length 2^%d per prime, 3 primes "
+                               "(2^64-2^b+1, b=32,34,40), uint64 residues" % (lg, lg, lg + 1),
+                   "operand_limbs": n, "transform_log": lg + 1, "passes": g.plan(lg + 1),
+                   "l2_policy": "inputs and 24 GiB spectra >> 129 MB L2; no flush", "parallelism": "replicas"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "ntt_pass_kernel (%d launches per multiply)" % pass_launches,
+                     "algorithmic_bytes_per_launch": pass_bytes / max(1, pass_launches)},
+        "multiply_roofline": {"bytes_model": bm, "achieved_GBps": bm / (ms * 1e-3) / 1e9,
+                              "frac": bm / (ms * 1e-3) / 1e9 / peak,
+                              "model": "10*k*N*8 + 8*(n_a+n_b), k=3 (2-pass four-step with fused decomposition, "
+                                       "pointwise product and Garner+carry)"},
+        "launch_breakdown": by_kind,
+        "gpu_launches": launches_per_step * args.steps,
+        "device_error_flags": flags,
+        "clocks": clk,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    for buf in (da, db, dc):
+        buf.free()
+    g.teardown()
+    return 0 if flags == 0 else 3
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, dist)
+        return run_gpu(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

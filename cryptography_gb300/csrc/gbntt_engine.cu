@@ -1,0 +1,658 @@
+// gbntt_engine.cu — host side of the CRT-NTT multiply engine and its C ABI.
+//
+// Engine state is one process-wide object (as g_nms in the reference,
+// ntt/lib/arith/ntt_mul.hip:312-347) guarded by a mutex, so concurrent host
+// callers serialise here instead of relying on the caller's lock
+// (ntt/lib/arith/multiply.c:27). Unlike the reference, the transform length
+// is chosen per call (the smallest power of two >= n_a + n_b - 1, at least
+// 32) instead of always the init-time maximum (ntt_mul.hip:1001-1002), and
+// twiddle tables are two-level (2 x 2^15 entries per prime and direction,
+// L2-resident) instead of O(N) host-built tables (ntt_mul.hip:189-308).
+#include <cuda_runtime.h>
+#include <mutex>
+#include <vector>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdarg.h>
+#include <time.h>
+
+#include "gbntt_arith.cuh"
+#include "gbntt_internal.h"
+#include "gbntt.h"
+
+namespace gbntt {
+
+typedef unsigned __int128 u128;
+
+static uint64_t h_mul(uint64_t a, uint64_t b, uint64_t p) { return (uint64_t)((u128)a * b % p); }
+static uint64_t h_pow(uint64_t b, uint64_t e, uint64_t p)
+{
+    uint64_t r = 1;
+    b %= p;
+    while (e) {
+        if (e & 1) r = h_mul(r, b, p);
+        b = h_mul(b, b, p);
+        e >>= 1;
+    }
+    return r;
+}
+static uint64_t h_inv(uint64_t a, uint64_t p) { return h_pow(a % p, p - 2, p); }
+static uint64_t h_mont(uint64_t x, uint64_t p) { return (uint64_t)(((u128)(x % p) << 64) % p); }
+static const uint64_t kGen[3] = {7, 10, 19};   // reference PRIM_ROOT[0, 2, 3]
+
+struct Engine {
+    bool ready = false;
+    int max_log = 0;
+    size_t n_max = 0;
+    uint64_t *d_spec = nullptr;     // 6 x n_max: spectra of operand A (3) then B (3)
+    uint64_t *d_tw = nullptr;       // [prime][dir][hi|lo][2^15]
+    unsigned *d_ctl = nullptr;      // [0] ticket, [1] error, [2..] tile status
+    size_t n_status = 0;
+    uint32_t *d_io = nullptr;       // staging for host-pointer calls
+    size_t io_words = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t garner[4] = {0, 0, 0, 0};
+    unsigned long dispatch = 0;
+    // profiling (NTT_PROFILE=1): host wall clock per phase
+    int prof = 0;
+    double prof_ms[3] = {0, 0, 0};   // upload, compute, download
+    long prof_calls = 0;
+};
+
+static Engine g;
+static std::recursive_mutex g_mu;
+static char g_err[512] = "";
+
+static void set_err(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+
+#define CK(expr)                                                                              \
+    do {                                                                                      \
+        cudaError_t _e = (expr);                                                              \
+        if (_e != cudaSuccess) {                                                              \
+            set_err("CUDA error %d (%s) at %s:%d: %s", (int)_e, cudaGetErrorString(_e),        \
+                    __FILE__, __LINE__, #expr);                                               \
+            return GBNTT_ERR_CUDA;                                                            \
+        }                                                                                     \
+    } while (0)
+
+// Optional per-launch CUDA-event records (kind, pass size, algorithmic bytes)
+// for roofline reporting; off by default and never used in timed runs.
+struct LaunchRec {
+    int kind;       // 0 fwd first pass, 1 fwd pass, 2 inv first pass, 3 inv pass, 4 garner+carry
+    int log_l;
+    double bytes;   // algorithmic bytes moved by this launch
+    cudaEvent_t e0, e1;
+};
+static bool g_rec_on = false;
+static std::vector<LaunchRec> g_recs;
+
+static void rec_begin(cudaStream_t st, int kind, int log_l, double bytes)
+{
+    if (!g_rec_on) return;
+    LaunchRec r;
+    r.kind = kind;
+    r.log_l = log_l;
+    r.bytes = bytes;
+    cudaEventCreate(&r.e0);
+    cudaEventCreate(&r.e1);
+    cudaEventRecord(r.e0, st);
+    g_recs.push_back(r);
+}
+static void rec_end(cudaStream_t st)
+{
+    if (!g_rec_on || g_recs.empty()) return;
+    cudaEventRecord(g_recs.back().e1, st);
+}
+
+static double now_ms()
+{
+    timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return t.tv_sec * 1e3 + t.tv_nsec * 1e-6;
+}
+
+static uint64_t *tw_ptr(int pi, int dir, int hi)
+{
+    return g.d_tw + (((size_t)pi * 2 + dir) * 2 + hi) * kTwSize;
+}
+
+int plan_passes(int log_n, int *p)
+{
+    if (log_n <= kMaxPassLog) { p[0] = log_n; return 1; }
+    if (log_n <= 2 * kMaxPassLog) { p[0] = (log_n + 1) / 2; p[1] = log_n / 2; return 2; }
+    p[0] = (log_n + 2) / 3;
+    const int rest = log_n - p[0];
+    p[1] = (rest + 1) / 2;
+    p[2] = rest / 2;
+    return 3;
+}
+
+static int choose_log(size_t na, size_t nb)
+{
+    const size_t need = na + nb - 1;
+    int L = kMinLog;
+    while (((size_t)1 << L) < need) L++;
+    return L;
+}
+
+static size_t workspace_bytes(int max_log)
+{
+    const size_t n = (size_t)1 << max_log;
+    const size_t spec = 6 * n * sizeof(uint64_t);
+    const size_t tw = 3 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t);
+    const size_t ctl = (2 + carry_tiles((long long)n + 1) + 64) * sizeof(unsigned);
+    const size_t io = (3 * n + 64) * sizeof(uint32_t);
+    return spec + tw + ctl + io;
+}
+
+static void free_all()
+{
+    if (g.stream) cudaStreamSynchronize(g.stream);
+    cudaFree(g.d_spec);
+    cudaFree(g.d_tw);
+    cudaFree(g.d_ctl);
+    cudaFree(g.d_io);
+    if (g.stream) cudaStreamDestroy(g.stream);
+    g = Engine();
+}
+
+static int init_impl(int max_log)
+{
+    if (g.ready) return GBNTT_OK;
+    if (max_log < kMinLog || max_log > kMaxLog) {
+        set_err("gbntt_init: max_log32=%d outside [%d, %d]", max_log, kMinLog, kMaxLog);
+        return GBNTT_ERR_ARG;
+    }
+    const char *pe = getenv("NTT_PROFILE");
+    g.prof = pe ? atoi(pe) : 0;
+    g.max_log = max_log;
+    g.n_max = (size_t)1 << max_log;
+    CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+    if (cudaMalloc(&g.d_spec, 6 * g.n_max * sizeof(uint64_t)) != cudaSuccess ||
+        cudaMalloc(&g.d_tw, 3 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t)) != cudaSuccess) {
+        set_err("gbntt_init: device allocation of %zu bytes failed", workspace_bytes(max_log));
+        cudaGetLastError();
+        free_all();
+        return GBNTT_ERR_ALLOC;
+    }
+    g.n_status = (size_t)carry_tiles((long long)g.n_max + 1) + 64;
+    g.io_words = 3 * g.n_max + 64;
+    if (cudaMalloc(&g.d_ctl, (2 + g.n_status) * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&g.d_io, g.io_words * sizeof(uint32_t)) != cudaSuccess) {
+        set_err("gbntt_init: device allocation of %zu bytes failed", workspace_bytes(max_log));
+        cudaGetLastError();
+        free_all();
+        return GBNTT_ERR_ALLOC;
+    }
+    CK(cudaMemset(g.d_ctl, 0, (2 + g.n_status) * sizeof(unsigned)));
+
+    // Twiddle tables and the w_64 constants.
+    const size_t tw_words = 3 * 2 * 2 * (size_t)kTwSize;
+    uint64_t *h = (uint64_t *)malloc(tw_words * sizeof(uint64_t));
+    if (!h) { set_err("gbntt_init: host allocation failed"); free_all(); return GBNTT_ERR_ALLOC; }
+    static uint64_t w64[3][2][64];
+    for (int pi = 0; pi < 3; pi++) {
+        const uint64_t p = prime_value(pi);
+        const uint64_t w = h_pow(kGen[pi], (p - 1) >> kMaxLog, p);
+        for (int dir = 0; dir < 2; dir++) {
+            const uint64_t wd = dir ? h_inv(w, p) : w;
+            uint64_t *hi = h + (((size_t)pi * 2 + dir) * 2 + 0) * kTwSize;
+            uint64_t *lo = h + (((size_t)pi * 2 + dir) * 2 + 1) * kTwSize;
+            const uint64_t wbig = h_pow(wd, (uint64_t)kTwSize, p);
+            uint64_t x = 1, y = 1;
+            for (int i = 0; i < kTwSize; i++) {
+                lo[i] = h_mont(x, p);
+                hi[i] = h_mont(y, p);
+                x = h_mul(x, wd, p);
+                y = h_mul(y, wbig, p);
+            }
+            const uint64_t r64 = h_pow(wd, (uint64_t)1 << (kMaxLog - 6), p);
+            uint64_t z = 1;
+            for (int i = 0; i < 64; i++) { w64[pi][dir][i] = h_mont(z, p); z = h_mul(z, r64, p); }
+        }
+    }
+    cudaError_t e = cudaMemcpy(g.d_tw, h, tw_words * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    free(h);
+    if (e != cudaSuccess) { set_err("gbntt_init: twiddle upload failed: %s", cudaGetErrorString(e)); free_all(); return GBNTT_ERR_CUDA; }
+    e = upload_root_constants(w64);
+    if (e != cudaSuccess) { set_err("gbntt_init: constant upload failed: %s", cudaGetErrorString(e)); free_all(); return GBNTT_ERR_CUDA; }
+
+    // Garner constants (Montgomery forms):
+    //   [0] q0^-1 mod q1, [1] q0 mod q2, [2] (q0 q1)^-1 mod q2.
+    const uint64_t q0 = prime_value(0), q1 = prime_value(1), q2 = prime_value(2);
+    g.garner[0] = h_mont(h_inv(q0 % q1, q1), q1);
+    g.garner[1] = h_mont(q0 % q2, q2);
+    g.garner[2] = h_mont(h_inv(h_mul(q0 % q2, q1 % q2, q2), q2), q2);
+    g.garner[3] = 0;
+    g.ready = true;
+    return GBNTT_OK;
+}
+
+static TwTables tables(int dir)
+{
+    TwTables t;
+    for (int pi = 0; pi < 3; pi++) { t.hi[pi] = tw_ptr(pi, dir, 0); t.lo[pi] = tw_ptr(pi, dir, 1); }
+    return t;
+}
+
+// Forward transform of one operand: limbs -> 3 spectra at spec[pi * stride].
+static int forward(uint64_t *spec, size_t stride, const uint32_t *limbs, size_t n, int L, cudaStream_t st)
+{
+    int pl[3];
+    const int np = plan_passes(L, pl);
+    PassArgs a;
+    memset(&a, 0, sizeof a);
+    for (int pi = 0; pi < 3; pi++) a.data[pi] = spec + pi * stride;
+    a.limbs = limbs;
+    a.n_limbs = (long long)n;
+    a.tw = tables(0);
+    int log_m = L;
+    for (int i = 0; i < np; i++) {
+        a.log_m = log_m;
+        a.log_s = log_m - pl[i];
+        a.ncols = (long long)1 << (L - pl[i]);
+        a.twiddle = a.log_s > 0;
+        const double nb8 = 3.0 * 8.0 * (double)((size_t)1 << L);
+        rec_begin(st, i == 0 ? 0 : 1, pl[i], i == 0 ? 4.0 * (double)n + nb8 : 2.0 * nb8);
+        CK(launch_pass(pl[i], 0, i == 0 ? LD_U32 : LD_U64, a, 3, st));
+        rec_end(st);
+        log_m -= pl[i];
+    }
+    return GBNTT_OK;
+}
+
+// Pointwise product of the spectra and inverse transform, in place in specA.
+static int inverse(uint64_t *specA, const uint64_t *specB, size_t stride, int L, cudaStream_t st, bool square)
+{
+    int pl[3];
+    const int np = plan_passes(L, pl);
+    PassArgs a;
+    memset(&a, 0, sizeof a);
+    for (int pi = 0; pi < 3; pi++) {
+        a.data[pi] = specA + pi * stride;
+        a.other[pi] = specB + pi * stride;
+        // N^-1 * R^2: with the R^-1 left by the Montgomery pointwise product
+        // the inverse output is scaled by exactly N^-1.
+        const uint64_t p = prime_value(pi);
+        const uint64_t ninv = h_inv(((uint64_t)1 << L) % p, p);
+        a.scale[pi] = h_mont(h_mont(ninv, p), p);
+    }
+    a.tw = tables(1);
+    int log_ms[3];
+    int log_m = L;
+    for (int i = 0; i < np; i++) { log_ms[i] = log_m; log_m -= pl[i]; }
+    for (int i = np - 1; i >= 0; i--) {
+        a.log_m = log_ms[i];
+        a.log_s = log_ms[i] - pl[i];
+        a.ncols = (long long)1 << (L - pl[i]);
+        a.twiddle = a.log_s > 0;
+        a.use_scale = (i == 0);
+        const double nb8 = 3.0 * 8.0 * (double)((size_t)1 << L);
+        const bool first = (i == np - 1);
+        rec_begin(st, first ? 2 : 3, pl[i], first ? (square ? 2.0 : 3.0) * nb8 : 2.0 * nb8);
+        CK(launch_pass(pl[i], 1, first ? LD_PW : LD_U64, a, 3, st));
+        rec_end(st);
+    }
+    return GBNTT_OK;
+}
+
+static int carry(uint32_t *d_c, size_t n_out, const uint64_t *specA, size_t stride, int L, cudaStream_t st)
+{
+    CarryArgs c;
+    memset(&c, 0, sizeof c);
+    for (int pi = 0; pi < 3; pi++) c.res[pi] = specA + pi * stride;
+    c.out = d_c;
+    c.n_coef = (long long)1 << L;
+    c.n_out = (long long)n_out;
+    c.ticket = g.d_ctl;
+    c.error = g.d_ctl + 1;
+    c.status = g.d_ctl + 2;
+    for (int i = 0; i < 4; i++) c.garner[i] = g.garner[i];
+    const long long nt = carry_tiles((long long)n_out);
+    CK(cudaMemsetAsync(g.d_ctl, 0, sizeof(unsigned), st));
+    CK(cudaMemsetAsync(g.d_ctl + 2, 0, (size_t)nt * sizeof(unsigned), st));
+    rec_begin(st, 4, 0, 3.0 * 8.0 * (double)((size_t)1 << L) + 4.0 * (double)n_out);
+    CK(launch_garner_carry(c, st, nullptr));
+    rec_end(st);
+    return GBNTT_OK;
+}
+
+static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb, cudaStream_t st)
+{
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    if (!st) st = g.stream;
+    const size_t n_out = na + nb;
+    if (na == 0 || nb == 0) {
+        if (n_out) CK(cudaMemsetAsync(d_c, 0, n_out * sizeof(uint32_t), st));
+        return GBNTT_OK;
+    }
+    const int L = choose_log(na, nb);
+    if (L > g.max_log) {
+        set_err("product needs %zu coefficients but the engine was initialised for 2^%d", na + nb - 1, g.max_log);
+        return GBNTT_ERR_SIZE;
+    }
+    const bool square = (d_a == d_b && na == nb);
+    uint64_t *specA = g.d_spec;
+    uint64_t *specB = g.d_spec + 3 * g.n_max;
+    int rc = forward(specA, g.n_max, d_a, na, L, st);
+    if (rc) return rc;
+    if (!square) {
+        rc = forward(specB, g.n_max, d_b, nb, L, st);
+        if (rc) return rc;
+    }
+    rc = inverse(specA, square ? specA : specB, g.n_max, L, st, square);
+    if (rc) return rc;
+    return carry(d_c, n_out, specA, g.n_max, L, st);
+}
+
+static int read_errors(unsigned *flags)
+{
+    unsigned v = 0;
+    CK(cudaStreamSynchronize(g.stream));
+    CK(cudaMemcpy(&v, g.d_ctl + 1, sizeof v, cudaMemcpyDeviceToHost));
+    CK(cudaMemset(g.d_ctl + 1, 0, sizeof(unsigned)));
+    if (flags) *flags = v;
+    return GBNTT_OK;
+}
+
+// Host-pointer product through the staging buffer (a, b, c contiguous).
+static int mul_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b, size_t nb,
+                    const uint32_t *dev_a, const uint32_t *dev_b)
+{
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    const size_t n_out = na + nb;
+    if (na == 0 || nb == 0) { if (n_out) memset(c, 0, n_out * 4); return GBNTT_OK; }
+    if (choose_log(na, nb) > g.max_log) {
+        set_err("product needs %zu coefficients but the engine was initialised for 2^%d", na + nb - 1, g.max_log);
+        return GBNTT_ERR_SIZE;
+    }
+    const bool square = (a == b && na == nb);
+    uint32_t *da = g.d_io, *db = g.d_io + na, *dc = g.d_io + na + (square ? 0 : nb);
+    double t0 = g.prof ? now_ms() : 0;
+    const uint32_t *ua = dev_a, *ub = dev_b;
+    if (!ua) { CK(cudaMemcpyAsync(da, a, na * 4, cudaMemcpyHostToDevice, g.stream)); ua = da; }
+    if (square) ub = ua;
+    else if (!ub) { CK(cudaMemcpyAsync(db, b, nb * 4, cudaMemcpyHostToDevice, g.stream)); ub = db; }
+    if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[0] += t - t0; t0 = t; }
+    int rc = mul_dev(dc, ua, na, ub, nb, g.stream);
+    if (rc) return rc;
+    if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[1] += t - t0; t0 = t; }
+    CK(cudaMemcpyAsync(c, dc, n_out * 4, cudaMemcpyDeviceToHost, g.stream));
+    unsigned flags = 0;
+    rc = read_errors(&flags);
+    if (rc) return rc;
+    if (g.prof) { double t = now_ms(); g.prof_ms[2] += t - t0; g.prof_calls++; }
+    if (flags) {
+        set_err("device check failed (flags 0x%x): %s", flags,
+                (flags & ERR_GARNER_DIGIT) ? "CRT digit out of range" : "carry look-back wait gave up");
+        return GBNTT_ERR_DEVICE;
+    }
+    return GBNTT_OK;
+}
+
+// ---- reference BigInt path -------------------------------------------------
+static int g_ref_cap = 28;   // default cap of max_log_n for ntt_mul_init_impl
+static int g_ref_log = 0;    // max_log_n given to ntt_mul_init_impl
+
+static size_t limbs32(const gbntt_bigint *x)
+{
+    if (x->n_limbs <= 0) return 0;
+    size_t n = 2 * (size_t)x->n_limbs;
+    if ((x->limbs[x->n_limbs - 1] >> 32) == 0) n--;
+    return n;
+}
+
+static int bigint_mul_impl(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_bigint *b, bool *guard_fail,
+                           bool *managed_fail)
+{
+    *guard_fail = false;
+    *managed_fail = false;
+    if (!g.ready) { set_err("call ntt_mul_init first"); return GBNTT_ERR_NOT_INIT; }
+    g.dispatch++;
+    const long na64 = a->n_limbs, nb64 = b->n_limbs;
+    const long need = na64 + nb64 - 1;
+    const long nref = g_ref_log > 0 ? (1L << g_ref_log) : (1L << (g.max_log - 1));
+    if (need > nref) {
+        *guard_fail = true;
+        set_err("operands exceed the fixed NTT size — product needs %ld coeffs but N=%ld (log_n=%d). "
+                "Re-init ntt_mul with a larger max_log_n; the size-N cyclic convolution would otherwise "
+                "wrap silently and corrupt the result.", need, nref, g_ref_log);
+        return GBNTT_ERR_SIZE;
+    }
+    const size_t na = limbs32(a), nb = limbs32(b);
+    const bool square = (a == b) || (a->limbs == b->limbs && a->n_limbs == b->n_limbs);
+    const long n_coeffs = na64 + nb64;
+    const int newcap = (int)(n_coeffs + 4);
+    uint32_t *tmp = nullptr;
+    uint32_t *outp;
+    // The output lands in a host buffer that cannot alias the inputs.
+    const bool alias = (c == a) || (c == b) || c->limbs == a->limbs || c->limbs == b->limbs;
+    if (c->cap < newcap && c->managed) {
+        *managed_fail = true;
+        set_err("bigint_resize: managed BigInt cap=%d insufficient for new_cap=%d — pre-allocate larger", c->cap,
+                newcap);
+        return GBNTT_ERR_MANAGED_CAP;
+    }
+    const size_t n_out = na + nb;
+    if (alias || c->cap < newcap) {
+        tmp = (uint32_t *)malloc((n_out + 1) * sizeof(uint32_t));
+        if (!tmp) { set_err("host allocation failed"); return GBNTT_ERR_ALLOC; }
+        outp = tmp;
+    } else {
+        outp = (uint32_t *)c->limbs;
+    }
+    int rc = GBNTT_OK;
+    if (na == 0 || nb == 0) {
+        memset(outp, 0, n_out * 4);
+    } else {
+        const uint32_t *pa = (const uint32_t *)a->limbs, *pb = (const uint32_t *)b->limbs;
+        rc = mul_host(outp, pa, na, square ? pa : pb, square ? na : nb, a->managed ? pa : nullptr,
+                      (!square && b->managed) ? pb : nullptr);
+    }
+    if (rc) { free(tmp); return rc; }
+    if (c->cap < newcap) {
+        uint64_t *nl = (uint64_t *)realloc(c->limbs, (size_t)newcap * sizeof(uint64_t));
+        if (!nl) { free(tmp); set_err("bigint_resize: OOM"); return GBNTT_ERR_ALLOC; }
+        c->limbs = nl;
+        c->cap = newcap;
+    }
+    uint32_t *dst = (uint32_t *)c->limbs;
+    if (tmp) memcpy(dst, tmp, n_out * 4);
+    memset(dst + n_out, 0, ((size_t)c->cap * 2 - n_out) * 4);
+    free(tmp);
+    long n = (long)((n_out + 1) / 2);
+    while (n > 0 && c->limbs[n - 1] == 0) n--;
+    c->n_limbs = (int)n;
+    return GBNTT_OK;
+}
+
+}  // namespace gbntt
+
+using namespace gbntt;
+
+extern "C" {
+
+int gbntt_init(int max_log32)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    return init_impl(max_log32);
+}
+
+void gbntt_teardown(void)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!g.ready) return;
+    if (g.prof > 0 && g.prof_calls > 0) {
+        const double tot = g.prof_ms[0] + g.prof_ms[1] + g.prof_ms[2];
+        fprintf(stderr, "[ntt_prof] calls=%ld  upload=%.1fms  compute=%.1fms  download=%.1fms  total=%.1fms\n",
+                g.prof_calls, g.prof_ms[0], g.prof_ms[1], g.prof_ms[2], tot);
+    }
+    free_all();
+    g_ref_log = 0;
+}
+
+int gbntt_is_ready(void) { return g.ready ? 1 : 0; }
+int gbntt_max_log(void) { return g.max_log; }
+size_t gbntt_workspace_bytes(int max_log32) { return workspace_bytes(max_log32); }
+int gbntt_transform_log(size_t na, size_t nb) { return (na == 0 || nb == 0) ? 0 : choose_log(na, nb); }
+int gbntt_plan(int log_n, int *passes)
+{
+    if (log_n < kMinLog || log_n > kMaxLog || !passes) return 0;
+    return plan_passes(log_n, passes);
+}
+const char *gbntt_last_error(void) { return g_err; }
+
+int gbntt_launch_log(int enable)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    for (auto &r : g_recs) { cudaEventDestroy(r.e0); cudaEventDestroy(r.e1); }
+    g_recs.clear();
+    g_rec_on = enable != 0;
+    return GBNTT_OK;
+}
+
+int gbntt_launch_records(int *kind, int *log_l, double *bytes, float *ms, int max_records)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    cudaError_t e = cudaDeviceSynchronize();
+    int n = 0;
+    for (auto &r : g_recs) {
+        if (e != cudaSuccess || n >= max_records) break;
+        float t = 0.f;
+        e = cudaEventElapsedTime(&t, r.e0, r.e1);
+        kind[n] = r.kind;
+        log_l[n] = r.log_l;
+        bytes[n] = r.bytes;
+        ms[n] = t;
+        n++;
+    }
+    if (e != cudaSuccess) {
+        set_err("gbntt_launch_records: %s", cudaGetErrorString(e));
+        return -GBNTT_ERR_CUDA;
+    }
+    return n;
+}
+
+void *gbntt_stream(void) { return (void *)g.stream; }
+
+int gbntt_mul_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb, void *stream)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!d_c || (na && !d_a) || (nb && !d_b)) { set_err("null pointer"); return GBNTT_ERR_ARG; }
+    return mul_dev(d_c, d_a, na, d_b, nb, (cudaStream_t)stream);
+}
+
+int gbntt_sqr_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, void *stream)
+{
+    return gbntt_mul_u32(d_c, d_a, na, d_a, na, stream);
+}
+
+int gbntt_mul_u32_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b, size_t nb)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!c || (na && !a) || (nb && !b)) { set_err("null pointer"); return GBNTT_ERR_ARG; }
+    return mul_host(c, a, na, b, nb, nullptr, nullptr);
+}
+
+int gbntt_device_errors(unsigned int *flags)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    return read_errors(flags);
+}
+
+int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log_n, void *stream)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    if (log_n < kMinLog || log_n > g.max_log || n > ((size_t)1 << log_n)) { set_err("bad size"); return GBNTT_ERR_ARG; }
+    cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+    return forward(d_out, (size_t)1 << log_n, d_in, n, log_n, st);
+}
+
+// ---- reference-compatible entry points --------------------------------------
+void ntt_mul_init_impl(int max_log_n)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (g.ready) return;
+    int cap = g_ref_cap;
+    const char *e = getenv("NTT_MAX_LOGN");
+    if (e) { int v = atoi(e); if (v >= 3 && v <= kMaxLog - 1) cap = v; }
+    if (max_log_n < 3 || max_log_n > cap) {
+        fprintf(stderr, "ntt_mul_init: log_n=%d out of safe range [3,%d] (set NTT_MAX_LOGN to raise)\n", max_log_n,
+                cap);
+        exit(1);
+    }
+    // 64-bit coefficients of the reference = pairs of 32-bit coefficients.
+    int L = max_log_n + 1;
+    if (L < kMinLog) L = kMinLog;
+    int rc = init_impl(L);
+    if (rc) {
+        fprintf(stderr, "ntt_mul_init: %s\n", g_err);
+        exit(1);
+    }
+    g_ref_log = max_log_n;
+    g.dispatch = 0;
+}
+
+void ntt_mul_teardown_impl(void) { gbntt_teardown(); }
+
+unsigned long ntt_get_gpu_dispatch_count(void) { return g.dispatch; }
+
+void ntt_gpu_emergency_reset(void) { (void)cudaDeviceSynchronize(); }
+
+int ntt_bigint_mul_checked(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_bigint *b)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!c || !a || !b) { set_err("null BigInt"); return GBNTT_ERR_ARG; }
+    bool gf, mf;
+    return bigint_mul_impl(c, a, b, &gf, &mf);
+}
+
+void ntt_bigint_mul(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_bigint *b)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!g.ready) {
+        fprintf(stderr, "ntt_bigint_mul: call ntt_mul_init first\n");
+        exit(1);
+    }
+    bool gf = false, mf = false;
+    int rc = bigint_mul_impl(c, a, b, &gf, &mf);
+    if (rc == GBNTT_OK) return;
+    if (mf) {
+        fprintf(stderr, "%s\n", g_err);
+        abort();
+    }
+    fprintf(stderr, "ntt_bigint_mul: %s\n", g_err);
+    fflush(stderr);
+    exit(1);
+}
+
+void ntt_bigint_sqr(gbntt_bigint *c, const gbntt_bigint *a) { ntt_bigint_mul(c, a, a); }
+
+gbntt_bigint bigint_alloc_managed(int cap)
+{
+    gbntt_bigint r;
+    memset(&r, 0, sizeof r);
+    void *p = nullptr;
+    if (cap <= 0 || cudaMallocManaged(&p, (size_t)cap * sizeof(uint64_t)) != cudaSuccess) {
+        fprintf(stderr, "bigint_alloc_managed: cudaMallocManaged(%d limbs) failed\n", cap);
+        exit(1);
+    }
+    memset(p, 0, (size_t)cap * sizeof(uint64_t));
+    r.limbs = (uint64_t *)p;
+    r.cap = cap;
+    r.managed = 1;
+    return r;
+}
+
+void hip_free_limbs(uint64_t *p) { cudaFree(p); }
+
+}  // extern "C"

@@ -1,0 +1,63 @@
+// gbntt_internal.h — declarations shared by the kernel and engine
+// translation units (not part of the public C ABI).
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace gbntt {
+
+constexpr int kMaxLog = 30;        // largest transform: 2^30 coefficients
+constexpr int kTwBits = 15;        // two-level twiddle split: e = hi*2^15 + lo
+constexpr int kTwSize = 1 << kTwBits;
+constexpr int kMinLog = 5;         // smallest transform length used (32)
+constexpr int kMaxPassLog = 10;    // largest sub-DFT staged in one CTA
+
+enum LoadKind { LD_U64 = 0, LD_U32 = 1, LD_PW = 2 };
+
+// Twiddle tables of one direction for the three primes: Montgomery forms of
+// w^e, w the primitive 2^30-th root g^((p-1)/2^30) (or its inverse), with
+// hi[i] = w^(i*2^15) and lo[i] = w^i for i < 2^15.
+struct TwTables {
+    const uint64_t *hi[3];
+    const uint64_t *lo[3];
+};
+
+struct PassArgs {
+    uint64_t *data[3];          // residues per prime, transformed in place
+    const uint64_t *other[3];   // second spectrum for the fused pointwise product
+    const uint32_t *limbs;      // 32-bit limbs for the fused decomposition
+    long long n_limbs;          // limbs beyond this index read as zero
+    TwTables tw;
+    uint64_t scale[3];          // Montgomery constant folded into inverse twiddles
+    long long ncols;            // N / L columns per prime
+    int log_m;                  // log2 of the sub-problem length M
+    int log_s;                  // log2 of the column stride S = M / L
+    int twiddle;                // apply the pass twiddle w_M^(j k)
+    int use_scale;              // fold scale[] into the inverse input twiddles
+    int prime_base;             // prime index of blockIdx.y == 0
+};
+
+struct CarryArgs {
+    const uint64_t *res[3];     // inverse-transform output, natural order
+    uint32_t *out;              // product limbs
+    long long n_coef;           // length of res[] (the transform length N)
+    long long n_out;            // limbs to write
+    unsigned int *ticket;       // dynamic tile counter (zeroed per launch)
+    unsigned int *status;       // per-tile look-back words (zeroed per launch)
+    unsigned int *error;        // sticky error bits
+    uint64_t garner[4];         // Montgomery Garner constants (see engine)
+};
+
+enum ErrorBits : unsigned int {
+    ERR_GARNER_DIGIT = 1u,      // third mixed-radix digit nonzero: corrupted residues
+    ERR_LOOKBACK_TIMEOUT = 2u,  // carry look-back wait gave up
+};
+
+// Launchers (gbntt_kernels.cu).
+cudaError_t upload_root_constants(const uint64_t w64[3][2][64]);
+cudaError_t launch_pass(int log_l, int dir, int load_kind, const PassArgs &args, int nprimes,
+                        cudaStream_t stream);
+cudaError_t launch_garner_carry(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out);
+long long carry_tiles(long long n_out);
+
+}  // namespace gbntt

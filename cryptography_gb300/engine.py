@@ -1,0 +1,235 @@
+"""ctypes bindings of ``libgbntt.so`` (see ``include/gbntt.h``)."""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+
+GBNTT_OK = 0
+GBNTT_ERR_NOT_INIT = 1
+GBNTT_ERR_SIZE = 2
+GBNTT_ERR_CUDA = 3
+GBNTT_ERR_DEVICE = 4
+GBNTT_ERR_ARG = 5
+GBNTT_ERR_MANAGED_CAP = 6
+GBNTT_ERR_ALLOC = 7
+
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_vp = ctypes.c_void_p
+_sz = ctypes.c_size_t
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("gbntt error %d: %s" % (code, msg))
+        self.code = code
+
+
+class BigInt(ctypes.Structure):
+    """The reference BigInt at LIMB_BITS == 64 (ntt/lib/arith/bigint.h:69-74)."""
+    _fields_ = [("limbs", _u64p), ("n_limbs", ctypes.c_int), ("cap", ctypes.c_int), ("managed", ctypes.c_int)]
+
+
+# Every symbol declared in include/gbntt.h.
+EXPORTS = (
+    "ntt_mul_init_impl", "ntt_mul_teardown_impl", "ntt_bigint_mul", "ntt_get_gpu_dispatch_count",
+    "ntt_gpu_emergency_reset", "bigint_alloc_managed", "hip_free_limbs", "ntt_bigint_sqr",
+    "ntt_bigint_mul_checked", "gbntt_init", "gbntt_teardown", "gbntt_is_ready", "gbntt_max_log",
+    "gbntt_workspace_bytes", "gbntt_transform_log", "gbntt_plan", "gbntt_mul_u32", "gbntt_sqr_u32",
+    "gbntt_mul_u32_host", "gbntt_device_errors", "gbntt_debug_forward", "gbntt_last_error", "gbntt_stream",
+    "gbntt_launch_log", "gbntt_launch_records",
+)
+
+_lib = None
+
+
+def lib_path():
+    return os.path.join(_HERE, "libgbntt.so")
+
+
+def lib():
+    """Load the CUDA library. Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        raise ImportError("libgbntt.so not built: run `python -c \"import __graft_entry__ as g; g.build()\"` "
+                          "(no CPU fallback exists)")
+    L = ctypes.CDLL(path)
+    L.ntt_mul_init_impl.argtypes = [ctypes.c_int]
+    L.ntt_mul_init_impl.restype = None
+    L.ntt_mul_teardown_impl.restype = None
+    L.ntt_bigint_mul.argtypes = [ctypes.POINTER(BigInt)] * 3
+    L.ntt_bigint_mul.restype = None
+    L.ntt_bigint_sqr.argtypes = [ctypes.POINTER(BigInt)] * 2
+    L.ntt_bigint_sqr.restype = None
+    L.ntt_bigint_mul_checked.argtypes = [ctypes.POINTER(BigInt)] * 3
+    L.ntt_bigint_mul_checked.restype = ctypes.c_int
+    L.ntt_get_gpu_dispatch_count.restype = ctypes.c_ulong
+    L.ntt_gpu_emergency_reset.restype = None
+    L.bigint_alloc_managed.argtypes = [ctypes.c_int]
+    L.bigint_alloc_managed.restype = BigInt
+    L.hip_free_limbs.argtypes = [_u64p]
+    L.hip_free_limbs.restype = None
+    L.gbntt_init.argtypes = [ctypes.c_int]
+    L.gbntt_init.restype = ctypes.c_int
+    L.gbntt_teardown.restype = None
+    L.gbntt_is_ready.restype = ctypes.c_int
+    L.gbntt_max_log.restype = ctypes.c_int
+    L.gbntt_workspace_bytes.argtypes = [ctypes.c_int]
+    L.gbntt_workspace_bytes.restype = _sz
+    L.gbntt_transform_log.argtypes = [_sz, _sz]
+    L.gbntt_transform_log.restype = ctypes.c_int
+    L.gbntt_plan.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.gbntt_plan.restype = ctypes.c_int
+    L.gbntt_mul_u32.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp]
+    L.gbntt_mul_u32.restype = ctypes.c_int
+    L.gbntt_sqr_u32.argtypes = [_vp, _vp, _sz, _vp]
+    L.gbntt_sqr_u32.restype = ctypes.c_int
+    L.gbntt_mul_u32_host.argtypes = [_u32p, _u32p, _sz, _u32p, _sz]
+    L.gbntt_mul_u32_host.restype = ctypes.c_int
+    L.gbntt_device_errors.argtypes = [ctypes.POINTER(ctypes.c_uint)]
+    L.gbntt_device_errors.restype = ctypes.c_int
+    L.gbntt_debug_forward.argtypes = [_vp, _vp, _sz, ctypes.c_int, _vp]
+    L.gbntt_debug_forward.restype = ctypes.c_int
+    L.gbntt_launch_log.argtypes = [ctypes.c_int]
+    L.gbntt_launch_log.restype = ctypes.c_int
+    L.gbntt_launch_records.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+    L.gbntt_launch_records.restype = ctypes.c_int
+    L.gbntt_last_error.restype = ctypes.c_char_p
+    L.gbntt_stream.restype = _vp
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != GBNTT_OK:
+        raise EngineError(rc, lib().gbntt_last_error().decode(errors="replace"))
+
+
+def init(max_log32):
+    _check(lib().gbntt_init(int(max_log32)))
+
+
+def teardown():
+    lib().gbntt_teardown()
+
+
+def is_ready():
+    return bool(lib().gbntt_is_ready())
+
+
+def workspace_bytes(max_log32):
+    return int(lib().gbntt_workspace_bytes(int(max_log32)))
+
+
+def transform_log(na, nb):
+    return int(lib().gbntt_transform_log(na, nb))
+
+
+def plan(log_n):
+    p = (ctypes.c_int * 3)()
+    n = lib().gbntt_plan(int(log_n), p)
+    return [p[i] for i in range(n)]
+
+
+LAUNCH_KINDS = ("fwd_pass_first", "fwd_pass", "inv_pass_first", "inv_pass", "garner_carry")
+
+
+def launch_log(enable):
+    lib().gbntt_launch_log(1 if enable else 0)
+
+
+def launch_records(max_records=4096):
+    """[(kind name, pass log2, algorithmic bytes, ms)] of the logged launches."""
+    k = (ctypes.c_int * max_records)()
+    l_ = (ctypes.c_int * max_records)()
+    b = (ctypes.c_double * max_records)()
+    m = (ctypes.c_float * max_records)()
+    n = lib().gbntt_launch_records(k, l_, b, m, max_records)
+    if n < 0:
+        _check(-n)
+    return [(LAUNCH_KINDS[k[i]], l_[i], b[i], m[i]) for i in range(n)]
+
+
+def device_errors():
+    f = ctypes.c_uint(0)
+    _check(lib().gbntt_device_errors(ctypes.byref(f)))
+    return int(f.value)
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def mul(a, b):
+    """Host-pointer product of two uint32 limb vectors; returns na+nb limbs."""
+    a = _u32(a)
+    b = a if b is a else _u32(b)
+    c = np.zeros(len(a) + len(b), dtype=np.uint32)
+    _check(lib().gbntt_mul_u32_host(c.ctypes.data_as(_u32p), a.ctypes.data_as(_u32p), len(a),
+                                    b.ctypes.data_as(_u32p), len(b)))
+    return c
+
+
+def sqr(a):
+    a = _u32(a)
+    return mul(a, a)
+
+
+def mul_device(c_ptr, a_ptr, na, b_ptr, nb, stream=None):
+    """Device-pointer product (raw addresses), stream-ordered."""
+    _check(lib().gbntt_mul_u32(c_ptr, a_ptr, na, b_ptr, nb, stream))
+
+
+_libc = ctypes.CDLL(None)
+_libc.calloc.restype = ctypes.c_void_p
+_libc.calloc.argtypes = [_sz, _sz]
+_libc.free.restype = None
+_libc.free.argtypes = [ctypes.c_void_p]
+
+
+def bigint_alloc(cap):
+    """A BigInt whose limbs come from libc calloc, as bigint_alloc does
+    (ntt/lib/arith/bigint.c:19-29), so the engine may realloc it."""
+    p = _libc.calloc(max(1, int(cap)), 8)
+    if not p:
+        raise MemoryError("calloc failed")
+    return BigInt(ctypes.cast(p, _u64p), 0, max(1, int(cap)), 0)
+
+
+def bigint_free(b):
+    if b.managed:
+        lib().hip_free_limbs(b.limbs)
+    else:
+        _libc.free(ctypes.cast(b.limbs, ctypes.c_void_p))
+    b.limbs = ctypes.cast(None, _u64p)
+    b.n_limbs = b.cap = b.managed = 0
+
+
+def bigint_set_int(b, v):
+    """Store v in b (must fit b.cap); sets the trimmed n_limbs."""
+    n = max(0, (v.bit_length() + 63) // 64)
+    if n > b.cap:
+        raise ValueError("value needs %d limbs, cap is %d" % (n, b.cap))
+    ctypes.memset(b.limbs, 0, 8 * b.cap)
+    if n:
+        ctypes.memmove(b.limbs, v.to_bytes(8 * n, "little"), 8 * n)
+    b.n_limbs = n
+    return b
+
+
+def bigint_from_int(v, cap=None):
+    n = max(1, (v.bit_length() + 63) // 64)
+    return bigint_set_int(bigint_alloc(max(cap or 0, n)), v)
+
+
+def bigint_to_int(b):
+    if b.n_limbs <= 0:
+        return 0
+    buf = ctypes.string_at(b.limbs, 8 * b.n_limbs)
+    return int.from_bytes(buf, "little")

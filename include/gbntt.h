@@ -1,0 +1,157 @@
+/*
+ * gbntt.h — C ABI of the GB300 CRT-NTT big-integer multiply engine.
+ *
+ * Two layers:
+ *
+ * 1. Drop-in entry points with the names, argument meaning and error
+ *    behaviour of the reference engine (cecoppola/cryptography, ntt/).
+ *    They work on the reference's BigInt layout at LIMB_BITS = 64
+ *    (ntt/lib/arith/bigint.h:69-74) and, like the reference, print a
+ *    message and exit(1) on misuse or failure.
+ *
+ * 2. A native API on 32-bit little-endian limbs (a uint64 limb array is the
+ *    same bytes as a uint32 array of twice the length) that returns error
+ *    codes instead of exiting, with device-pointer, host-pointer and batched
+ *    forms.
+ *
+ * No CUDA or torch types appear in the signatures: streams are passed as
+ * `void *` holding a cudaStream_t (NULL = the engine's own stream).
+ */
+#ifndef GBNTT_H
+#define GBNTT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Layout-identical to the reference BigInt with LIMB_BITS == 64
+ * (ntt/lib/arith/bigint.h:69-74): value = sum limbs[i] * 2^(64 i). */
+typedef struct {
+    uint64_t *limbs;   /* little-endian limbs                      */
+    int       n_limbs; /* significant limbs (trimmed)              */
+    int       cap;     /* allocated limbs                          */
+    int       managed; /* 1: limbs from bigint_alloc_managed       */
+} gbntt_bigint;
+
+/* ---- status codes of the native API --------------------------------- */
+#define GBNTT_OK              0
+#define GBNTT_ERR_NOT_INIT    1  /* engine not initialised                  */
+#define GBNTT_ERR_SIZE        2  /* product does not fit the initialised N  */
+#define GBNTT_ERR_CUDA        3  /* a CUDA runtime call failed              */
+#define GBNTT_ERR_DEVICE      4  /* device-side check failed (Garner digit
+                                    or a carry look-back wait gave up)      */
+#define GBNTT_ERR_ARG         5  /* invalid argument                        */
+#define GBNTT_ERR_MANAGED_CAP 6  /* managed output BigInt too small         */
+#define GBNTT_ERR_ALLOC       7  /* device or host allocation failed        */
+
+/* =====================================================================
+ * 1. Reference-compatible entry points
+ * ===================================================================== */
+
+/* Replaces ntt_mul_init_impl (ntt/lib/arith/ntt_mul.hip:379), reached from
+ * ntt_mul_init (ntt/lib/arith/multiply.c:97). Sizes the engine for products
+ * of up to 2^max_log_n 64-bit coefficients, i.e. operands with
+ * n_a + n_b - 1 <= 2^max_log_n 64-bit limbs. Valid range [3, cap]; cap is
+ * 28 unless NTT_MAX_LOGN (<= 29) raises it. Out of range: message + exit(1).
+ * A second call while initialised is a no-op, as in the reference. */
+void ntt_mul_init_impl(int max_log_n);
+
+/* Replaces ntt_mul_teardown_impl (ntt/lib/arith/ntt_mul.hip:533). Frees all
+ * device state; NTT_PROFILE=1 prints the per-phase summary first. */
+void ntt_mul_teardown_impl(void);
+
+/* Replaces ntt_bigint_mul (ntt/lib/arith/ntt_mul.hip:995; prototype
+ * ntt/lib/arith/multiply.h:46). c = a * b exactly. c is grown with realloc
+ * to n_a + n_b + 4 limbs when needed (a managed c that is too small aborts,
+ * as bigint_resize does in ntt/lib/arith/bigint.c:46-60); c->n_limbs is
+ * trimmed and limbs above it are zero. c may alias a or b; a == b takes the
+ * squaring path (one forward transform). Exits with a message when not
+ * initialised or when n_a + n_b - 1 > 2^max_log_n (the reference's cyclic
+ * wrap guard, ntt_mul.hip:1013-1022). */
+void ntt_bigint_mul(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_bigint *b);
+
+/* Replaces ntt_get_gpu_dispatch_count (ntt/lib/arith/ntt_mul.hip:595). */
+unsigned long ntt_get_gpu_dispatch_count(void);
+
+/* Replaces ntt_gpu_emergency_reset (ntt/lib/arith/ntt_mul.hip:1248): drains
+ * in-flight work with cudaDeviceSynchronize; never resets the device. */
+void ntt_gpu_emergency_reset(void);
+
+/* Strong overrides of the reference's weak allocators
+ * (ntt/lib/arith/bigint.c:31-69, ntt/lib/arith/bigint_hip_alloc.hip):
+ * cudaMallocManaged limbs, zeroed, managed = 1. */
+gbntt_bigint bigint_alloc_managed(int cap);
+void hip_free_limbs(uint64_t *p);
+
+/* Additive (no reference equivalent): c = a * a. */
+void ntt_bigint_sqr(gbntt_bigint *c, const gbntt_bigint *a);
+
+/* Additive: ntt_bigint_mul returning a GBNTT_* code instead of exiting. */
+int ntt_bigint_mul_checked(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_bigint *b);
+
+/* =====================================================================
+ * 2. Native API (32-bit limbs)
+ * ===================================================================== */
+
+/* Initialise for transforms up to 2^max_log32 32-bit coefficients
+ * (5 <= max_log32 <= 30): products with n_a + n_b - 1 <= 2^max_log32. */
+int gbntt_init(int max_log32);
+void gbntt_teardown(void);
+int gbntt_is_ready(void);
+int gbntt_max_log(void);
+
+/* Device memory the engine allocates at gbntt_init(max_log32). */
+size_t gbntt_workspace_bytes(int max_log32);
+
+/* Transform length log2 chosen for an n_a x n_b product. */
+int gbntt_transform_log(size_t na, size_t nb);
+
+/* Pass plan for a transform of 2^log_n points: writes the pass sizes
+ * (log2, outermost first) to passes[0..2] and returns the pass count. */
+int gbntt_plan(int log_n, int *passes);
+
+/* d_c[0 .. na+nb) = d_a * d_b on the device, stream-ordered (returns after
+ * enqueueing). d_b == d_a with nb == na squares. d_c must not overlap the
+ * inputs. Device-side check failures are recorded and reported by
+ * gbntt_device_errors(). */
+int gbntt_mul_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb,
+                  void *stream);
+int gbntt_sqr_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, void *stream);
+
+/* Host-pointer form: copies in, multiplies, copies out, synchronises and
+ * checks the device error flags. c must hold na + nb limbs. */
+int gbntt_mul_u32_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b, size_t nb);
+
+/* Synchronise the engine stream, return and clear the device error bits
+ * (1 = Garner digit check, 2 = look-back wait gave up). */
+int gbntt_device_errors(unsigned int *flags);
+
+/* Forward spectra of a limb vector for each prime (3 x 2^log_n uint64, in
+ * the engine's digit-reversed order; see gbntt_plan). For known-answer
+ * tests. d_out needs 3 * 2^log_n entries. */
+int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log_n, void *stream);
+
+/* Per-launch timing for roofline reports. gbntt_launch_log(1) makes every
+ * following kernel launch record CUDA events (kind: 0 first forward pass,
+ * 1 forward pass, 2 first inverse pass with the pointwise product,
+ * 3 inverse pass, 4 Garner + carry), its pass size log2 and its algorithmic
+ * bytes; gbntt_launch_log(0) stops and clears. gbntt_launch_records
+ * synchronises and copies up to max_records entries; returns the count or
+ * a negative GBNTT_* code. */
+int gbntt_launch_log(int enable);
+int gbntt_launch_records(int *kind, int *log_l, double *bytes, float *ms, int max_records);
+
+/* Last error message of this library. */
+const char *gbntt_last_error(void);
+
+/* Engine stream (cudaStream_t) used when NULL is passed. */
+void *gbntt_stream(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBNTT_H */

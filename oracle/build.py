@@ -1,0 +1,67 @@
+"""Build recipe for the CPU oracle (test infrastructure only).
+
+* ``build_oracle()`` compiles ``crt_ntt_oracle.c`` (the CPU restatement of the
+  reference CRT-NTT multiply) into ``oracle/liboracle.so``.
+* ``build_ref()`` compiles the reference's own host sources, by path from the
+  reference checkout, together with ``ref_shim.cpp`` into
+  ``oracle/_ref/libref.so``. Nothing from the reference is copied; when the
+  checkout is absent (the GPU machine) it is skipped and the tests that need it
+  skip too.
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_SO = os.path.join(REF_DIR, "libref.so")
+REFERENCE_ROOT = os.environ.get("GBNTT_REFERENCE_ROOT", "/root/reference")
+
+
+def _stale(target, sources):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def build_oracle(force=False):
+    src = os.path.join(HERE, "crt_ntt_oracle.c")
+    if force or _stale(ORACLE_SO, [src, __file__]):
+        tmp = ORACLE_SO + ".tmp"
+        subprocess.check_call(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=gnu11",
+                               "-Wall", src, "-o", tmp, "-ldl"])
+        os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+def reference_available():
+    return os.path.isfile(os.path.join(REFERENCE_ROOT, "ntt", "lib", "garner.hip"))
+
+
+def build_ref(force=False):
+    """Compile the reference host code (bigint.c, garner.hip host part,
+    primes.h, shoup.h) by path. Returns the .so path or None if the
+    reference checkout is not present."""
+    if not reference_available():
+        return None
+    lib = os.path.join(REFERENCE_ROOT, "ntt", "lib")
+    arith = os.path.join(lib, "arith")
+    shim = os.path.join(HERE, "ref_shim.cpp")
+    bigint_c = os.path.join(arith, "bigint.c")
+    if not (force or _stale(REF_SO, [shim, bigint_c, os.path.join(lib, "garner.hip"), __file__])):
+        return REF_SO
+    os.makedirs(REF_DIR, exist_ok=True)
+    obj = os.path.join(REF_DIR, "bigint.o")
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-c", "-I", lib, "-I", arith,
+                           bigint_c, "-o", obj])
+    tmp = REF_SO + ".tmp"
+    subprocess.check_call(["g++", "-O2", "-fopenmp", "-fPIC", "-shared",
+                           "-I", lib, "-I", arith, shim, obj, "-o", tmp])
+    os.replace(tmp, REF_SO)
+    return REF_SO
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    print(build_ref(force=True))
