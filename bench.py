@@ -47,8 +47,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--log-limbs", type=int, default=28, help="operand size 2^k limbs (28 = headline)")
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-log-limbs", type=int, default=23, help="CPU baseline sample size 2^k limbs")
+    ap.add_argument("--cpu-log-limbs", type=int, default=22, help="CPU baseline sample size 2^k limbs")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--plan", default="", help="comma-separated pass sizes overriding the default plan")
     return ap.parse_args()
 
 
@@ -156,7 +157,7 @@ def host_info():
             "omp_num_threads": os.environ.get("OMP_NUM_THREADS")}
 
 
-def cpu_baseline(log_limbs_sample, log_limbs_target, reps=1):
+def cpu_baseline(log_limbs_sample, log_limbs_target, reps=1, with_gmp=True):
     """Oracle CRT-NTT (restatement of the reference CPU path) on one bounded
     sample, all host threads, scaled to the target size by N log N."""
     import oracle
@@ -177,7 +178,7 @@ def cpu_baseline(log_limbs_sample, log_limbs_target, reps=1):
                      "Garner, gather; OpenMP) took %.2f s; scaled by N log N (x%.1f) to 2^%d limbs"
                      % (log_limbs_sample, log_limbs_sample, t, scale, log_limbs_target),
            "host": host_info()}
-    if oracle.gmp_available():
+    if with_gmp and oracle.gmp_available():
         t0 = time.perf_counter()
         oracle.gmp_mul(a, b)
         tg = time.perf_counter() - t0
@@ -191,7 +192,7 @@ def run_reference(args, dist):
     times = []
     res = None
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline(args.cpu_log_limbs, args.log_limbs)
+        r = cpu_baseline(args.cpu_log_limbs, args.log_limbs, with_gmp=(i == args.warmup + args.steps - 1))
         if i >= args.warmup:
             times.append(r["value"])
             res = r
@@ -216,6 +217,8 @@ def run_gpu(args, dist):
     lg = args.log_limbs
     n = 1 << lg
     g.init(lg + 1)
+    if args.plan:
+        g.set_plan(lg + 1, [int(x) for x in args.plan.split(",")])
     stream = g.lib().gbntt_stream()
     a = synth.operand(n, 1 + 2 * dist.rank)
     b = synth.operand(n, 2 + 2 * dist.rank)

@@ -34,6 +34,7 @@ from .engine import (  # noqa: F401
     mul,
     mul_device,
     plan,
+    set_plan,
     sqr,
     teardown,
     transform_log,

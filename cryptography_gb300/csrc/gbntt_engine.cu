@@ -123,8 +123,17 @@ static uint64_t *tw_ptr(int pi, int dir, int hi)
     return g.d_tw + (((size_t)pi * 2 + dir) * 2 + hi) * kTwSize;
 }
 
+// Per-length plan overrides (set by gbntt_set_plan, e.g. from an autotuner):
+// [log_n][0] = pass count (0: default plan), [1..3] = pass sizes.
+static int g_plan_override[kMaxLog + 1][4];
+
 int plan_passes(int log_n, int *p)
 {
+    if (log_n >= 0 && log_n <= kMaxLog && g_plan_override[log_n][0] > 0) {
+        const int np = g_plan_override[log_n][0];
+        for (int i = 0; i < np; i++) p[i] = g_plan_override[log_n][1 + i];
+        return np;
+    }
     if (log_n <= kMaxPassLog) { p[0] = log_n; return 1; }
     if (log_n <= 2 * kMaxPassLog) { p[0] = (log_n + 1) / 2; p[1] = log_n / 2; return 2; }
     p[0] = (log_n + 2) / 3;
@@ -508,6 +517,26 @@ int gbntt_plan(int log_n, int *passes)
     return plan_passes(log_n, passes);
 }
 const char *gbntt_last_error(void) { return g_err; }
+
+int gbntt_set_plan(int log_n, int npasses, const int *passes)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (log_n < kMinLog || log_n > kMaxLog) { set_err("gbntt_set_plan: log_n %d out of range", log_n); return GBNTT_ERR_ARG; }
+    if (npasses == 0) { g_plan_override[log_n][0] = 0; return GBNTT_OK; }
+    if (npasses < 1 || npasses > 3 || !passes) { set_err("gbntt_set_plan: 1 to 3 passes"); return GBNTT_ERR_ARG; }
+    int sum = 0;
+    for (int i = 0; i < npasses; i++) {
+        if (passes[i] < kMinLog || passes[i] > kMaxPassLog) {
+            set_err("gbntt_set_plan: pass size 2^%d outside [2^%d, 2^%d]", passes[i], kMinLog, kMaxPassLog);
+            return GBNTT_ERR_ARG;
+        }
+        sum += passes[i];
+    }
+    if (sum != log_n) { set_err("gbntt_set_plan: pass sizes sum to %d, not %d", sum, log_n); return GBNTT_ERR_ARG; }
+    g_plan_override[log_n][0] = npasses;
+    for (int i = 0; i < npasses; i++) g_plan_override[log_n][1 + i] = passes[i];
+    return GBNTT_OK;
+}
 
 int gbntt_launch_log(int enable)
 {

@@ -113,6 +113,11 @@ int gbntt_transform_log(size_t na, size_t nb);
  * (log2, outermost first) to passes[0..2] and returns the pass count. */
 int gbntt_plan(int log_n, int *passes);
 
+/* Override the pass plan of transforms of 2^log_n points (1 to 3 passes,
+ * each of 2^5 .. 2^10 points, sizes summing to log_n, outermost first);
+ * npasses = 0 restores the default plan. Used by the autotuner. */
+int gbntt_set_plan(int log_n, int npasses, const int *passes);
+
 /* d_c[0 .. na+nb) = d_a * d_b on the device, stream-ordered (returns after
  * enqueueing). d_b == d_a with nb == na squares. d_c must not overlap the
  * inputs. Device-side check failures are recorded and reported by

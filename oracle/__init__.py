@@ -49,6 +49,8 @@ def lib():
             f.argtypes = [_u32p, ctypes.c_long, _u32p, ctypes.c_long, _u32p]
         L.oracle_mod_u32.restype = ctypes.c_uint64
         L.oracle_mod_u32.argtypes = [_u32p, ctypes.c_long, ctypes.c_uint64]
+        L.oracle_mod_u32_par.restype = ctypes.c_uint64
+        L.oracle_mod_u32_par.argtypes = [_u32p, ctypes.c_long, ctypes.c_uint64]
         L.oracle_gmp_available.restype = ctypes.c_int
         L.oracle_num_threads.restype = ctypes.c_int
         _lib = L
@@ -158,8 +160,9 @@ def gather_u32(coeff_words, out_cap):
 
 
 def mod_u32(a, q):
+    """Value of the limb vector modulo q (q < 2^63), OpenMP-parallel."""
     a = _as_u32(a)
-    return int(lib().oracle_mod_u32(_p32(a), len(a), q))
+    return int(lib().oracle_mod_u32_par(_p32(a), len(a), q))
 
 
 def to_int(limbs):

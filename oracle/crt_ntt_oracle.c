@@ -291,6 +291,27 @@ uint64_t oracle_mod_u32(const uint32_t *a, long n, uint64_t q)
     return (uint64_t)r;
 }
 
+/* Same value with OpenMP: chunk values mod q combined with 2^(32 len) mod q. */
+uint64_t oracle_mod_u32_par(const uint32_t *a, long n, uint64_t q)
+{
+    const long chunk = 1L << 20;
+    long nch = (n + chunk - 1) / chunk;
+    if (nch <= 1) return oracle_mod_u32(a, n, q);
+    uint64_t *val = (uint64_t *)malloc((size_t)nch * sizeof(uint64_t));
+    #pragma omp parallel for schedule(dynamic)
+    for (long c = 0; c < nch; c++) {
+        long s = c * chunk, m = (s + chunk <= n) ? chunk : n - s;
+        val[c] = oracle_mod_u32(a + s, m, q);
+    }
+    /* shift = 2^(32 chunk) mod q */
+    u128 sh = 1, b = ((u128)1 << 32) % q;
+    for (long e = chunk; e; e >>= 1) { if (e & 1) sh = sh * b % q; b = b * b % q; }
+    u128 r = 0;
+    for (long c = nch - 1; c >= 0; c--) r = (r * sh + val[c]) % q;
+    free(val);
+    return (uint64_t)r;
+}
+
 /* ---- GMP ground truth through the public mpz ABI (dlopen) -------------- */
 typedef struct { int alloc, size; void *d; } orc_mpz;
 static void (*g_init)(orc_mpz *);

@@ -158,7 +158,8 @@ def test_device_pointer_api(engine):
     rng = np.random.default_rng(8)
     na, nb = 5000, 3001
     a, b = _rand(rng, na), _rand(rng, nb)
-    da, db, dc = cudart.DeviceBuffer(4 * na), cudart.DeviceBuffer(4 * nb), cudart.DeviceBuffer(4 * (na + nb))
+    da, db = cudart.DeviceBuffer(4 * na), cudart.DeviceBuffer(4 * nb)
+    dc = cudart.DeviceBuffer(4 * max(na + nb, 2 * na))
     da.upload(a)
     db.upload(b)
     engine.mul_device(dc.ptr, da.ptr, na, db.ptr, nb, None)
