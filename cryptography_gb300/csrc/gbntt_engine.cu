@@ -538,6 +538,15 @@ int gbntt_set_plan(int log_n, int npasses, const int *passes)
     return GBNTT_OK;
 }
 
+int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t n,
+                       void *stream)
+{
+    if (prime < 0 || prime > 2 || op < 0 || op > 5) { set_err("gbntt_debug_modops: bad prime/op"); return GBNTT_ERR_ARG; }
+    cudaStream_t st = stream ? (cudaStream_t)stream : (g.ready ? g.stream : (cudaStream_t)0);
+    CK(launch_modops(prime, op, d_a, d_b, d_out, (long long)n, st));
+    return GBNTT_OK;
+}
+
 int gbntt_launch_log(int enable)
 {
     std::lock_guard<std::recursive_mutex> lk(g_mu);

@@ -59,5 +59,7 @@ cudaError_t launch_pass(int log_l, int dir, int load_kind, const PassArgs &args,
                         cudaStream_t stream);
 cudaError_t launch_garner_carry(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out);
 long long carry_tiles(long long n_out);
+cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *b, uint64_t *out, long long n,
+                          cudaStream_t stream);
 
 }  // namespace gbntt

@@ -73,6 +73,41 @@ __device__ __forceinline__ void dft_reg(uint64_t (&x)[1 << LOG_R])
     }
 }
 
+// ---------------------------------------------------------------------------
+// Element-wise modular operations over device arrays (self-test of the
+// arithmetic, as the reference's test_modops.hip pins primes.h / shoup.h).
+// op: 0 add_mod, 1 sub_mod, 2 mont_mul, 3..5 the plain C++ forms.
+// ---------------------------------------------------------------------------
+template <int PI>
+__device__ __forceinline__ uint64_t modop(int op, uint64_t a, uint64_t b)
+{
+    switch (op) {
+    case 0: return add_mod<PI>(a, b);
+    case 1: return sub_mod<PI>(a, b);
+    case 2: return mont_mul<PI>(a, b);
+    case 3: return add_mod_ref<PI>(a, b);
+    case 4: return sub_mod_ref<PI>(a, b);
+    default: return mont_mul_ref<PI>(a, b);
+    }
+}
+
+__global__ void modops_kernel(int prime, int op, const uint64_t *a, const uint64_t *b, uint64_t *out, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t x = a[i], y = b[i];
+    out[i] = prime == 0 ? modop<0>(op, x, y) : (prime == 1 ? modop<1>(op, x, y) : modop<2>(op, x, y));
+}
+
+cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *b, uint64_t *out, long long n,
+                          cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    const long long grid = (n + 255) / 256;
+    modops_kernel<<<(unsigned)grid, 256, 0, stream>>>(prime, op, a, b, out, n);
+    return cudaGetLastError();
+}
+
 constexpr int kPassThreads = 256;
 
 template <int PI, int LOG_L, int DIR, int LD>

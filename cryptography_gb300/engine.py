@@ -39,7 +39,7 @@ EXPORTS = (
     "ntt_bigint_mul_checked", "gbntt_init", "gbntt_teardown", "gbntt_is_ready", "gbntt_max_log",
     "gbntt_workspace_bytes", "gbntt_transform_log", "gbntt_plan", "gbntt_mul_u32", "gbntt_sqr_u32",
     "gbntt_mul_u32_host", "gbntt_device_errors", "gbntt_debug_forward", "gbntt_last_error", "gbntt_stream",
-    "gbntt_launch_log", "gbntt_launch_records", "gbntt_set_plan",
+    "gbntt_launch_log", "gbntt_launch_records", "gbntt_set_plan", "gbntt_debug_modops",
 )
 
 _lib = None
@@ -95,6 +95,8 @@ def lib():
     L.gbntt_device_errors.restype = ctypes.c_int
     L.gbntt_debug_forward.argtypes = [_vp, _vp, _sz, ctypes.c_int, _vp]
     L.gbntt_debug_forward.restype = ctypes.c_int
+    L.gbntt_debug_modops.argtypes = [ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _sz, _vp]
+    L.gbntt_debug_modops.restype = ctypes.c_int
     L.gbntt_set_plan.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.gbntt_set_plan.restype = ctypes.c_int
     L.gbntt_launch_log.argtypes = [ctypes.c_int]

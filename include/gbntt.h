@@ -139,6 +139,14 @@ int gbntt_device_errors(unsigned int *flags);
  * tests. d_out needs 3 * 2^log_n entries. */
 int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log_n, void *stream);
 
+/* Element-wise modular arithmetic on device arrays for self-tests: for
+ * prime index 0..2 (2^64 - 2^b + 1, b = 32, 34, 40) and op 0 = (a+b) mod p,
+ * 1 = (a-b) mod p, 2 = a*b*2^-64 mod p (Montgomery), 3..5 = the same with
+ * the plain C++ forms. a, b canonical (a may be any 64-bit value for op
+ * 2 and 5). Stream-ordered. */
+int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t n,
+                       void *stream);
+
 /* Per-launch timing for roofline reports. gbntt_launch_log(1) makes every
  * following kernel launch record CUDA events (kind: 0 first forward pass,
  * 1 forward pass, 2 first inverse pass with the pointwise product,

@@ -237,3 +237,38 @@ def test_size_guard_native(engine):
     with pytest.raises(engine.EngineError) as ei:
         engine.mul(np.ones((1 << big) // 2 + 2, dtype=np.uint32), np.ones((1 << big) // 2 + 2, dtype=np.uint32))
     assert ei.value.code == engine.GBNTT_ERR_SIZE
+
+
+@pytest.mark.parametrize("prime", [0, 1, 2])
+def test_device_modops(engine, prime):
+    # the device modular arithmetic (PTX carry-chain forms and the plain C++
+    # forms) against Python integers on random and corner operands, as the
+    # reference's lib/test_modops.hip pins add/sub/mul for every prime
+    p = oracle.PRIMES[prime]
+    rng = np.random.default_rng(40 + prime)
+    corners = [0, 1, 2, p - 1, p - 2, (1 << 32) - 1, 1 << 32, p >> 1, 1 << 63, p - (1 << 32)]
+    n = 1 << 16
+    a = np.array([int(x) % p for x in rng.integers(0, 1 << 64, n, dtype=np.uint64)], dtype=np.uint64)
+    b = np.array([int(x) % p for x in rng.integers(0, 1 << 64, n, dtype=np.uint64)], dtype=np.uint64)
+    k = len(corners)
+    a[:k * k] = np.repeat(np.array(corners, dtype=np.uint64), k)
+    b[:k * k] = np.tile(np.array(corners, dtype=np.uint64), k)
+    wide = a.copy()
+    wide[k * k:k * k + 100] = rng.integers(0, 1 << 64, 100, dtype=np.uint64) | np.uint64(1 << 63)
+    wide[-4:] = [(1 << 64) - 1, (1 << 64) - 2, p, p + 1]
+    da, db, dw, dout = (cudart.DeviceBuffer(8 * n) for _ in range(4))
+    da.upload(a)
+    db.upload(b)
+    dw.upload(wide)
+    rinv = pow(1 << 64, -1, p)
+    want = {0: [(int(x) + int(y)) % p for x, y in zip(a, b)],
+            1: [(int(x) - int(y)) % p for x, y in zip(a, b)],
+            2: [int(x) * int(y) * rinv % p for x, y in zip(wide, b)]}
+    for op in range(6):
+        src = dw if op % 3 == 2 else da
+        assert engine.lib().gbntt_debug_modops(prime, op, src.ptr, db.ptr, dout.ptr, n, None) == 0
+        cudart.stream_sync(engine.lib().gbntt_stream())
+        got = [int(v) for v in dout.download(np.uint64, n)]
+        assert got == want[op % 3], (prime, op)
+    for buf in (da, db, dw, dout):
+        buf.free()
