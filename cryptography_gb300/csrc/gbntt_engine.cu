@@ -61,6 +61,18 @@ struct Engine {
 };
 
 static Engine g;
+// Montgomery forms of w_64^i per prime and direction (kernel arguments).
+static uint64_t g_w64[3][2][64];
+
+static cudaError_t launch_pass_any(int pi, int log_l, int dir, int ld, PassArgs &a, cudaStream_t st)
+{
+    memcpy(a.w64, g_w64[pi][dir], sizeof a.w64);
+    switch (pi) {
+    case 0: return launch_pass_prime<0>(log_l, dir, ld, a, st);
+    case 1: return launch_pass_prime<1>(log_l, dir, ld, a, st);
+    default: return launch_pass_prime<2>(log_l, dir, ld, a, st);
+    }
+}
 static std::recursive_mutex g_mu;
 static char g_err[512] = "";
 
@@ -206,7 +218,7 @@ static int init_impl(int max_log)
     const size_t tw_words = 3 * 2 * 2 * (size_t)kTwSize;
     uint64_t *h = (uint64_t *)malloc(tw_words * sizeof(uint64_t));
     if (!h) { set_err("gbntt_init: host allocation failed"); free_all(); return GBNTT_ERR_ALLOC; }
-    static uint64_t w64[3][2][64];
+    uint64_t (&w64)[3][2][64] = g_w64;
     for (int pi = 0; pi < 3; pi++) {
         const uint64_t p = prime_value(pi);
         const uint64_t w = h_pow(kGen[pi], (p - 1) >> kMaxLog, p);
@@ -230,8 +242,6 @@ static int init_impl(int max_log)
     cudaError_t e = cudaMemcpy(g.d_tw, h, tw_words * sizeof(uint64_t), cudaMemcpyHostToDevice);
     free(h);
     if (e != cudaSuccess) { set_err("gbntt_init: twiddle upload failed: %s", cudaGetErrorString(e)); free_all(); return GBNTT_ERR_CUDA; }
-    e = upload_root_constants(w64);
-    if (e != cudaSuccess) { set_err("gbntt_init: constant upload failed: %s", cudaGetErrorString(e)); free_all(); return GBNTT_ERR_CUDA; }
 
     // Garner constants (Montgomery forms):
     //   [0] q0^-1 mod q1, [1] q0 mod q2, [2] (q0 q1)^-1 mod q2.
@@ -268,10 +278,12 @@ static int forward(uint64_t *spec, size_t stride, const uint32_t *limbs, size_t 
         a.log_s = log_m - pl[i];
         a.ncols = (long long)1 << (L - pl[i]);
         a.twiddle = a.log_s > 0;
-        const double nb8 = 3.0 * 8.0 * (double)((size_t)1 << L);
-        rec_begin(st, i == 0 ? 0 : 1, pl[i], i == 0 ? 4.0 * (double)n + nb8 : 2.0 * nb8);
-        CK(launch_pass(pl[i], 0, i == 0 ? LD_U32 : LD_U64, a, 3, st));
-        rec_end(st);
+        const double nb8 = 8.0 * (double)((size_t)1 << L);
+        for (int pi = 0; pi < 3; pi++) {
+            rec_begin(st, i == 0 ? 0 : 1, pl[i], i == 0 ? 4.0 * (double)n + nb8 : 2.0 * nb8);
+            CK(launch_pass_any(pi, pl[i], 0, i == 0 ? LD_U32 : LD_U64, a, st));
+            rec_end(st);
+        }
         log_m -= pl[i];
     }
     return GBNTT_OK;
@@ -303,11 +315,13 @@ static int inverse(uint64_t *specA, const uint64_t *specB, size_t stride, int L,
         a.ncols = (long long)1 << (L - pl[i]);
         a.twiddle = a.log_s > 0;
         a.use_scale = (i == 0);
-        const double nb8 = 3.0 * 8.0 * (double)((size_t)1 << L);
+        const double nb8 = 8.0 * (double)((size_t)1 << L);
         const bool first = (i == np - 1);
-        rec_begin(st, first ? 2 : 3, pl[i], first ? (square ? 2.0 : 3.0) * nb8 : 2.0 * nb8);
-        CK(launch_pass(pl[i], 1, first ? LD_PW : LD_U64, a, 3, st));
-        rec_end(st);
+        for (int pi = 0; pi < 3; pi++) {
+            rec_begin(st, first ? 2 : 3, pl[i], first ? (square ? 2.0 : 3.0) * nb8 : 2.0 * nb8);
+            CK(launch_pass_any(pi, pl[i], 1, first ? LD_PW : LD_U64, a, st));
+            rec_end(st);
+        }
     }
     return GBNTT_OK;
 }

@@ -34,7 +34,8 @@ struct PassArgs {
     int log_s;                  // log2 of the column stride S = M / L
     int twiddle;                // apply the pass twiddle w_M^(j k)
     int use_scale;              // fold scale[] into the inverse input twiddles
-    int prime_base;             // prime index of blockIdx.y == 0
+    int prime_base;             // unused (one launch per prime)
+    uint64_t w64[64];           // Montgomery w_64^i of this launch's prime and direction
 };
 
 struct CarryArgs {
@@ -54,9 +55,8 @@ enum ErrorBits : unsigned int {
 };
 
 // Launchers (gbntt_kernels.cu).
-cudaError_t upload_root_constants(const uint64_t w64[3][2][64]);
-cudaError_t launch_pass(int log_l, int dir, int load_kind, const PassArgs &args, int nprimes,
-                        cudaStream_t stream);
+template <int PI>
+cudaError_t launch_pass_prime(int log_l, int dir, int ld, const PassArgs &a, cudaStream_t st);
 cudaError_t launch_garner_carry(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out);
 long long carry_tiles(long long n_out);
 cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *b, uint64_t *out, long long n,

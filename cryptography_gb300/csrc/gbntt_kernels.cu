@@ -1,20 +1,11 @@
 // gbntt_kernels.cu — sm_103a kernels of the CRT-NTT multiply.
 //
-// 1. ntt_pass_kernel: one radix-2^l pass (l = 5..10) of an in-place NTT over
-//    all three primes. A CTA owns G adjacent columns of one pass; it stages
-//    G x 2^l residues in shared memory with 64-bit coalesced loads, computes
-//    each 2^l-point DFT as A x B (A = 2^ceil(l/2), B = 2^floor(l/2)) with
-//    fully unrolled register butterflies, and writes back in place.
-//    Forward passes are decimation in frequency (natural order in, digit-
-//    reversed order out, pass twiddle applied after the sub-DFT); inverse
-//    passes are the exact transpose (twiddle before the sub-DFT, natural
-//    order out). Fused into the passes: limb -> residue decomposition (first
-//    forward pass reads 32-bit limbs), the pointwise product (first inverse
-//    pass reads both spectra), and the N^-1 scale (last inverse pass).
-//    Reference counterparts: stockham_kernel* and the Bailey 4-step
-//    launchers in ntt/lib/ntt_kernel.hip:625-833, :1172-1375, the scatter
-//    kernel ntt/lib/arith/ntt_mul.hip:117-160 and hadamard_kernel
-//    ntt/lib/ntt_kernel.hip:386-399.
+// 1. The NTT pass kernels live in gbntt_pass.cuh (one translation unit per
+//    prime). Fused into the passes: limb -> residue decomposition (first
+//    forward pass reads 32-bit limbs; reference scatter kernel
+//    ntt/lib/arith/ntt_mul.hip:117-160), the pointwise product (first
+//    inverse pass; reference hadamard_kernel ntt/lib/ntt_kernel.hip:386-399
+//    and stockham_kernel_had :739-780) and the N^-1 scale (last inverse pass).
 // 2. garner_carry_kernel: CRT reconstruction of every coefficient from its
 //    three residues, the limb sums w0(c_j) + w1(c_{j-1}) + w2(c_{j-2}), and
 //    the carry propagation over all product limbs as one decoupled look-back
@@ -27,51 +18,6 @@
 #include "gbntt_internal.h"
 
 namespace gbntt {
-
-// Montgomery forms of w_64^i (primitive 64th root, consistent with the
-// 2^30-th root of the twiddle tables), per prime and direction.
-__constant__ uint64_t c_w64[3][2][64];
-
-cudaError_t upload_root_constants(const uint64_t w64[3][2][64])
-{
-    return cudaMemcpyToSymbol(c_w64, w64, sizeof(uint64_t) * 3 * 2 * 64);
-}
-
-__host__ __device__ constexpr int bitrev(int x, int bits)
-{
-    int r = 0;
-    for (int i = 0; i < bits; i++) r = (r << 1) | ((x >> i) & 1);
-    return r;
-}
-
-// w^E from the two-level tables (Montgomery form), E < 2^30.
-template <int PI>
-__device__ __forceinline__ uint64_t tw_exp(const uint64_t *hi, const uint64_t *lo, uint32_t e)
-{
-    return mont_mul<PI>(__ldg(hi + (e >> kTwBits)), __ldg(lo + (e & (kTwSize - 1))));
-}
-
-// In-register radix-2 DIF DFT of 2^LOG_R points: natural order in,
-// bit-reversed order out (X[k] ends in x[bitrev(k)]).
-template <int PI, int DIR, int LOG_R>
-__device__ __forceinline__ void dft_reg(uint64_t (&x)[1 << LOG_R])
-{
-    constexpr int R = 1 << LOG_R;
-#pragma unroll
-    for (int s = R / 2; s >= 1; s >>= 1) {
-#pragma unroll
-        for (int blk = 0; blk < R; blk += 2 * s) {
-#pragma unroll
-            for (int i = 0; i < s; i++) {
-                uint64_t u = x[blk + i], v = x[blk + i + s];
-                x[blk + i] = add_mod<PI>(u, v);
-                uint64_t d = sub_mod<PI>(u, v);
-                // w_{2s}^i = w_64^(i * 32 / s)
-                x[blk + i + s] = (i == 0) ? d : mont_mul<PI>(d, c_w64[PI][DIR][i * (32 / s)]);
-            }
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------
 // Element-wise modular operations over device arrays (self-test of the
@@ -106,177 +52,6 @@ cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *
     const long long grid = (n + 255) / 256;
     modops_kernel<<<(unsigned)grid, 256, 0, stream>>>(prime, op, a, b, out, n);
     return cudaGetLastError();
-}
-
-constexpr int kPassThreads = 256;
-
-template <int PI, int LOG_L, int DIR, int LD>
-__device__ __forceinline__ void pass_body(const PassArgs &a, uint64_t *sm)
-{
-    constexpr int L = 1 << LOG_L;
-    constexpr int LOG_A = (LOG_L + 1) / 2, LOG_B = LOG_L / 2;
-    constexpr int A = 1 << LOG_A, B = 1 << LOG_B;
-    constexpr int T = kPassThreads;
-    constexpr int G = T / A;                 // columns per CTA
-    constexpr int LOG_G = 8 - LOG_A;
-    constexpr int RS = L + A + 1;            // odd row stride (in 8-byte words)
-    const int tid = threadIdx.x;
-    const long long col0 = (long long)blockIdx.x * G;
-    const int log_s = a.log_s, log_m = a.log_m;
-    const long long smask = (1LL << log_s) - 1;
-    const int log_gs = LOG_G < log_s ? LOG_G : log_s;
-    const long long left = a.ncols - col0;
-    const int gvalid = left < G ? (int)left : G;
-    uint64_t *data = a.data[PI];
-    const uint64_t *twhi = a.tw.hi[PI];
-    const uint64_t *twlo = a.tw.lo[PI];
-    const int sh = kMaxLog - log_m;
-
-    // ---- cooperative coalesced load: element (g, m) -> sm[g*RS + m + m/B]
-#pragma unroll 4
-    for (int e = tid; e < G * L; e += T) {
-        const int gp = e & ((1 << log_gs) - 1);
-        const int rest = e >> log_gs;
-        const int m = rest & (L - 1);
-        const int g = ((rest >> LOG_L) << log_gs) + gp;
-        uint64_t v = 0;
-        if (g < gvalid) {
-            const long long col = col0 + g;
-            const long long addr = ((col >> log_s) << log_m) + (col & smask) + ((long long)m << log_s);
-            if (LD == LD_U32) {
-                v = addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
-            } else if (LD == LD_PW) {
-                v = mont_mul<PI>(data[addr], a.other[PI][addr]);
-            } else {
-                v = data[addr];
-            }
-        }
-        sm[g * RS + m + (m >> LOG_B)] = v;
-    }
-    __syncthreads();
-
-    // ---- step 1: A-point DFTs over the high digit, one per (g, b)
-    if (tid < G * B) {
-        const int g = tid >> LOG_B, b = tid & (B - 1);
-        uint64_t x[A];
-#pragma unroll
-        for (int i = 0; i < A; i++) x[i] = sm[g * RS + i * (B + 1) + b];
-        if (DIR == 1 && (a.twiddle || a.use_scale)) {
-            // inverse pass: input twiddle w_M^-((iB + b) j), times the scale
-            const uint64_t j = (uint64_t)((col0 + g) & smask);
-            uint64_t base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)b * j) << sh));
-            const uint64_t step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * j) << sh));
-            if (a.use_scale) base = mont_mul<PI>(base, a.scale[PI]);
-#pragma unroll
-            for (int i = 0; i < A; i++) {
-                x[i] = mont_mul<PI>(x[i], base);
-                if (i + 1 < A) base = mont_mul<PI>(base, step);
-            }
-        }
-        dft_reg<PI, DIR, LOG_A>(x);
-#pragma unroll
-        for (int ka = 0; ka < A; ka++) {
-            uint64_t v = x[bitrev(ka, LOG_A)];
-            if (ka > 0 && b > 0)   // in-CTA twiddle w_L^(b ka)
-                v = mont_mul<PI>(v, __ldg(twhi + ((b * ka) << (kTwBits - LOG_L))));
-            sm[g * RS + ka * (B + 1) + b] = v;
-        }
-    }
-    __syncthreads();
-
-    // ---- step 2: B-point DFTs over the low digit, one per (g, ka)
-    const int g2 = tid >> LOG_A, ka = tid & (A - 1);
-    uint64_t y[B];
-#pragma unroll
-    for (int i = 0; i < B; i++) y[i] = sm[g2 * RS + ka * (B + 1) + i];
-    dft_reg<PI, DIR, LOG_B>(y);
-    if (DIR == 0 && a.twiddle) {
-        // forward pass: output twiddle w_M^((ka + A kb) j)
-        const uint64_t j = (uint64_t)((col0 + g2) & smask);
-        uint64_t base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)ka * j) << sh));
-        const uint64_t step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)A * j) << sh));
-#pragma unroll
-        for (int kb = 0; kb < B; kb++) {
-            const int idx = bitrev(kb, LOG_B);
-            y[idx] = mont_mul<PI>(y[idx], base);
-            if (kb + 1 < B) base = mont_mul<PI>(base, step);
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kb = 0; kb < B; kb++) {
-        const int k = ka + A * kb;
-        sm[g2 * RS + k + (k >> LOG_B)] = y[bitrev(kb, LOG_B)];
-    }
-    __syncthreads();
-
-    // ---- cooperative coalesced store
-#pragma unroll 4
-    for (int e = tid; e < G * L; e += T) {
-        const int gp = e & ((1 << log_gs) - 1);
-        const int rest = e >> log_gs;
-        const int m = rest & (L - 1);
-        const int g = ((rest >> LOG_L) << log_gs) + gp;
-        if (g < gvalid) {
-            const long long col = col0 + g;
-            const long long addr = ((col >> log_s) << log_m) + (col & smask) + ((long long)m << log_s);
-            data[addr] = sm[g * RS + m + (m >> LOG_B)];
-        }
-    }
-}
-
-template <int LOG_L, int DIR, int LD>
-__global__ void __launch_bounds__(kPassThreads, 2) ntt_pass_kernel(PassArgs a)
-{
-    extern __shared__ uint64_t sm[];
-    switch (blockIdx.y + a.prime_base) {
-    case 0: pass_body<0, LOG_L, DIR, LD>(a, sm); break;
-    case 1: pass_body<1, LOG_L, DIR, LD>(a, sm); break;
-    default: pass_body<2, LOG_L, DIR, LD>(a, sm); break;
-    }
-}
-
-template <int LOG_L>
-constexpr size_t pass_smem_bytes()
-{
-    return (size_t)(kPassThreads >> ((LOG_L + 1) / 2)) * ((1 << LOG_L) + (1 << ((LOG_L + 1) / 2)) + 1) * 8;
-}
-
-typedef void (*PassFn)(PassArgs);
-
-template <int LOG_L>
-static cudaError_t launch_pass_l(int dir, int load_kind, const PassArgs &args, int nprimes, cudaStream_t stream)
-{
-    PassFn fn;
-    if (dir == 0)
-        fn = load_kind == LD_U32 ? ntt_pass_kernel<LOG_L, 0, LD_U32> : ntt_pass_kernel<LOG_L, 0, LD_U64>;
-    else
-        fn = load_kind == LD_PW ? ntt_pass_kernel<LOG_L, 1, LD_PW> : ntt_pass_kernel<LOG_L, 1, LD_U64>;
-    const size_t smem = pass_smem_bytes<LOG_L>();
-    static bool attr_done[2][3] = {{false, false, false}, {false, false, false}};
-    if (!attr_done[dir][load_kind]) {
-        cudaError_t e = cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_done[dir][load_kind] = true;
-    }
-    constexpr int G = kPassThreads >> ((LOG_L + 1) / 2);
-    const long long gx = (args.ncols + G - 1) / G;
-    dim3 grid((unsigned)gx, (unsigned)nprimes);
-    fn<<<grid, kPassThreads, smem, stream>>>(args);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_pass(int log_l, int dir, int load_kind, const PassArgs &args, int nprimes, cudaStream_t stream)
-{
-    switch (log_l) {
-    case 5: return launch_pass_l<5>(dir, load_kind, args, nprimes, stream);
-    case 6: return launch_pass_l<6>(dir, load_kind, args, nprimes, stream);
-    case 7: return launch_pass_l<7>(dir, load_kind, args, nprimes, stream);
-    case 8: return launch_pass_l<8>(dir, load_kind, args, nprimes, stream);
-    case 9: return launch_pass_l<9>(dir, load_kind, args, nprimes, stream);
-    case 10: return launch_pass_l<10>(dir, load_kind, args, nprimes, stream);
-    default: return cudaErrorInvalidValue;
-    }
 }
 
 // ---------------------------------------------------------------------------

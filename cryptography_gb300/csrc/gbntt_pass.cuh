@@ -1,0 +1,275 @@
+// gbntt_pass.cuh — one NTT pass of 2^l points (l = 5..10) for one prime.
+//
+// The transform of N = 2^L points is a chain of 1-3 passes (outermost
+// first). Pass i owns sub-problems of M_i points; inside each, element
+// (j, m) sits at j + S_i m (column j < S_i, row m < 2^l, S_i = M_i / 2^l).
+// A forward (decimation-in-frequency) pass computes, for every column, the
+// 2^l-point DFT over m, multiplies output k by w_M^(j k) and stores it at
+// j + S_i k; the next pass then works on the contiguous blocks of S_i points.
+// The inverse pass is the exact transpose: input k of column j is first
+// multiplied by w_M^-(j k), then the inverse 2^l-point DFT is stored back in
+// natural order. Spectra therefore come out digit-reversed by pass and go
+// back to natural order, with no transposes. The reference reaches the same
+// structure with explicit transposes (Bailey four-step,
+// ntt/lib/ntt_kernel.hip:835-925, :1172-1375).
+//
+// Inside a CTA (128 threads, G columns): the 2^l-point DFT is A x B with
+// A = 2^ceil(l/2), B = 2^floor(l/2): step 1 runs one A-point register DFT
+// per (column, b), multiplies by w_L^(b k_a), step 2 runs A/B B-point
+// register DFTs per thread. Shared memory holds the G x 2^l tile with an odd
+// row stride and one pad word per B words, so both steps are free of bank
+// conflicts. Two address layouts:
+//   STRIDED (S >= G): the CTA's G columns are adjacent in every row, so each
+//     thread walks one column with a constant pointer increment;
+//   CONTIG (S == 1): the CTA's columns are G consecutive rows of 2^l words.
+#pragma once
+#include "gbntt_arith.cuh"
+#include "gbntt_internal.h"
+
+namespace gbntt {
+
+enum PassLayout { LAYOUT_STRIDED = 0, LAYOUT_CONTIG = 1 };
+
+constexpr int kPassThreads = 128;
+constexpr int kLogPassThreads = 7;
+
+template <int LOG_L>
+struct PassShape {
+    static constexpr int L = 1 << LOG_L;
+    static constexpr int LOG_A = (LOG_L + 1) / 2, LOG_B = LOG_L / 2;
+    static constexpr int A = 1 << LOG_A, B = 1 << LOG_B;
+    static constexpr int T = kPassThreads;
+    static constexpr int LOG_G = kLogPassThreads - LOG_B;
+    static constexpr int G = 1 << LOG_G;          // columns per CTA
+    static constexpr int RS = L + A + 1;          // odd row stride in 8-byte words
+    static constexpr size_t SMEM = (size_t)G * RS * 8;
+};
+
+__host__ __device__ constexpr int bitrev(int x, int bits)
+{
+    int r = 0;
+    for (int i = 0; i < bits; i++) r = (r << 1) | ((x >> i) & 1);
+    return r;
+}
+
+// w^E from the two-level tables (Montgomery form), E < 2^30.
+template <int PI>
+__device__ __forceinline__ uint64_t tw_exp(const uint64_t *hi, const uint64_t *lo, uint32_t e)
+{
+    return mont_mul<PI>(__ldg(hi + (e >> kTwBits)), __ldg(lo + (e & (kTwSize - 1))));
+}
+
+// In-register radix-2 DIF DFT of 2^LOG_R points: natural order in,
+// bit-reversed order out (X[k] ends in x[bitrev(k)]). w64 = Montgomery forms
+// of the primitive 64th root's powers.
+template <int PI, int LOG_R>
+__device__ __forceinline__ void dft_reg(uint64_t (&x)[1 << LOG_R], const uint64_t *w64)
+{
+    constexpr int R = 1 << LOG_R;
+#pragma unroll
+    for (int s = R / 2; s >= 1; s >>= 1) {
+#pragma unroll
+        for (int blk = 0; blk < R; blk += 2 * s) {
+#pragma unroll
+            for (int i = 0; i < s; i++) {
+                const uint64_t u = x[blk + i], v = x[blk + i + s];
+                x[blk + i] = add_mod<PI>(u, v);
+                const uint64_t d = sub_mod<PI>(u, v);
+                // w_{2s}^i = w_64^(i * 32 / s)
+                x[blk + i + s] = (i == 0) ? d : mont_mul<PI>(d, w64[i * (32 / s)]);
+            }
+        }
+    }
+}
+
+template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
+__device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const uint64_t *w64)
+{
+    using S_ = PassShape<LOG_L>;
+    constexpr int L = S_::L, A = S_::A, B = S_::B, LOG_B = S_::LOG_B, G = S_::G, LOG_G = S_::LOG_G;
+    constexpr int T = S_::T, RS = S_::RS;
+    const int t = threadIdx.x;
+    const long long col0 = (long long)blockIdx.x * G;
+    const int log_s = a.log_s, log_m = a.log_m;
+    uint64_t *data = a.data[PI];
+    const uint64_t *twhi = a.tw.hi[PI];
+    const uint64_t *twlo = a.tw.lo[PI];
+    const int sh = kMaxLog - log_m;
+    // column index within the sub-problem of the first column of this CTA
+    const uint64_t j0 = LAYOUT == LAYOUT_STRIDED ? (uint64_t)(col0 & ((1LL << log_s) - 1)) : 0ull;
+
+    // ---- load: tile element (g, m) -> sm[g*RS + m + m/B]
+    if (LAYOUT == LAYOUT_STRIDED) {
+        const int g = t & (G - 1), m0 = t >> LOG_G;            // m = m0 + it*B
+        const long long S = 1LL << log_s;
+        const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
+        const long long stepg = (long long)B * S;
+        uint64_t *dst = sm + g * RS + m0;
+#pragma unroll 8
+        for (int it = 0; it < A; it++) {
+            const long long addr = base + it * stepg;
+            uint64_t v;
+            if (LD == LD_U32) v = addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
+            else if (LD == LD_PW) v = mont_mul<PI>(data[addr], a.other[PI][addr]);
+            else v = data[addr];
+            dst[it * (B + 1)] = v;
+        }
+    } else {
+        const long long rows_left = a.ncols - col0;
+        const long long base = col0 << LOG_L;
+#pragma unroll 8
+        for (int it = 0; it < A; it++) {
+            const int e = t + it * T;
+            const int g = e >> LOG_L, m = e & (L - 1);
+            uint64_t v = 0;
+            if (g < rows_left) {
+                const long long addr = base + e;
+                if (LD == LD_U32) v = addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
+                else if (LD == LD_PW) v = mont_mul<PI>(data[addr], a.other[PI][addr]);
+                else v = data[addr];
+            }
+            sm[g * RS + m + (m >> LOG_B)] = v;
+        }
+    }
+    __syncthreads();
+
+    // ---- step 1: one A-point DFT per (g, b) over the high digit
+    {
+        const int g = t >> LOG_B, b = t & (B - 1);
+        uint64_t x[A];
+#pragma unroll
+        for (int i = 0; i < A; i++) x[i] = sm[g * RS + i * (B + 1) + b];
+        if (DIR == 1 && (a.twiddle || a.use_scale)) {
+            // inverse pass: input twiddle w_M^-((iB + b) j), times the scale
+            const uint64_t j = j0 + (uint64_t)(LAYOUT == LAYOUT_STRIDED ? g : 0);
+            uint64_t base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)b * j) << sh));
+            const uint64_t step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * j) << sh));
+            if (a.use_scale) base = mont_mul<PI>(base, a.scale[PI]);
+#pragma unroll
+            for (int i = 0; i < A; i++) {
+                x[i] = mont_mul<PI>(x[i], base);
+                if (i + 1 < A) base = mont_mul<PI>(base, step);
+            }
+        }
+        dft_reg<PI, S_::LOG_A>(x, w64);
+#pragma unroll
+        for (int ka = 0; ka < A; ka++) {
+            uint64_t v = x[bitrev(ka, S_::LOG_A)];
+            if (ka > 0 && b > 0)   // w_L^(b ka)
+                v = mont_mul<PI>(v, __ldg(twhi + ((b * ka) << (kTwBits - LOG_L))));
+            sm[g * RS + ka * (B + 1) + b] = v;
+        }
+    }
+    __syncthreads();
+
+    // ---- step 2: A/B B-point DFTs per thread over the low digit
+    {
+        constexpr int R = A / B;
+        const int g = t >> LOG_B, q = t & (B - 1);
+        uint64_t y[R][B];
+        uint64_t step = 0;
+        if (DIR == 0 && LAYOUT == LAYOUT_STRIDED && a.twiddle) {
+            const uint64_t j = j0 + (uint64_t)g;
+            step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)A * j) << sh));
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int ka = q + r * B;
+#pragma unroll
+            for (int i = 0; i < B; i++) y[r][i] = sm[g * RS + ka * (B + 1) + i];
+            dft_reg<PI, LOG_B>(y[r], w64);
+            if (DIR == 0 && LAYOUT == LAYOUT_STRIDED && a.twiddle) {
+                // forward pass: output twiddle w_M^((ka + A kb) j)
+                const uint64_t j = j0 + (uint64_t)g;
+                uint64_t base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)ka * j) << sh));
+#pragma unroll
+                for (int kb = 0; kb < B; kb++) {
+                    const int idx = bitrev(kb, LOG_B);
+                    y[r][idx] = mont_mul<PI>(y[r][idx], base);
+                    if (kb + 1 < B) base = mont_mul<PI>(base, step);
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int ka = q + r * B;
+#pragma unroll
+            for (int kb = 0; kb < B; kb++) {
+                const int k = ka + A * kb;
+                sm[g * RS + k + (k >> LOG_B)] = y[r][bitrev(kb, LOG_B)];
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- store: same addressing as the load
+    if (LAYOUT == LAYOUT_STRIDED) {
+        const int g = t & (G - 1), m0 = t >> LOG_G;
+        const long long S = 1LL << log_s;
+        const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
+        const long long stepg = (long long)B * S;
+        const uint64_t *src = sm + g * RS + m0;
+#pragma unroll 8
+        for (int it = 0; it < A; it++) data[base + it * stepg] = src[it * (B + 1)];
+    } else {
+        const long long rows_left = a.ncols - col0;
+        const long long base = col0 << LOG_L;
+#pragma unroll 8
+        for (int it = 0; it < A; it++) {
+            const int e = t + it * T;
+            const int g = e >> LOG_L, m = e & (L - 1);
+            if (g < rows_left) data[base + e] = sm[g * RS + m + (m >> LOG_B)];
+        }
+    }
+}
+
+template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
+__global__ void __launch_bounds__(kPassThreads, 4) ntt_pass_kernel(PassArgs a)
+{
+    extern __shared__ uint64_t sm[];
+    pass_tile<PI, LOG_L, DIR, LD, LAYOUT>(a, sm, a.w64);
+}
+
+// Launcher for one prime (explicitly instantiated, one translation unit per
+// prime so the three are compiled in parallel).
+template <int PI, int LOG_L>
+static cudaError_t launch_pass_l(int dir, int ld, const PassArgs &a, cudaStream_t st)
+{
+    using S_ = PassShape<LOG_L>;
+    const int layout = a.log_s == 0 ? LAYOUT_CONTIG : LAYOUT_STRIDED;
+    void (*fn)(PassArgs) = nullptr;
+    if (dir == 0) {
+        if (ld == LD_U32)
+            fn = layout == LAYOUT_STRIDED ? ntt_pass_kernel<PI, LOG_L, 0, LD_U32, LAYOUT_STRIDED>
+                                          : ntt_pass_kernel<PI, LOG_L, 0, LD_U32, LAYOUT_CONTIG>;
+        else
+            fn = layout == LAYOUT_STRIDED ? ntt_pass_kernel<PI, LOG_L, 0, LD_U64, LAYOUT_STRIDED>
+                                          : ntt_pass_kernel<PI, LOG_L, 0, LD_U64, LAYOUT_CONTIG>;
+    } else {
+        // the pointwise pass is always the innermost (contiguous) one and the
+        // other inverse passes are strided
+        if (ld == LD_PW && layout == LAYOUT_CONTIG) fn = ntt_pass_kernel<PI, LOG_L, 1, LD_PW, LAYOUT_CONTIG>;
+        else if (ld == LD_U64 && layout == LAYOUT_STRIDED) fn = ntt_pass_kernel<PI, LOG_L, 1, LD_U64, LAYOUT_STRIDED>;
+    }
+    if (!fn) return cudaErrorInvalidValue;
+    const long long gx = (a.ncols + S_::G - 1) / S_::G;
+    fn<<<(unsigned)gx, kPassThreads, S_::SMEM, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int PI>
+cudaError_t launch_pass_prime(int log_l, int dir, int ld, const PassArgs &a, cudaStream_t st)
+{
+    switch (log_l) {
+    case 5: return launch_pass_l<PI, 5>(dir, ld, a, st);
+    case 6: return launch_pass_l<PI, 6>(dir, ld, a, st);
+    case 7: return launch_pass_l<PI, 7>(dir, ld, a, st);
+    case 8: return launch_pass_l<PI, 8>(dir, ld, a, st);
+    case 9: return launch_pass_l<PI, 9>(dir, ld, a, st);
+    case 10: return launch_pass_l<PI, 10>(dir, ld, a, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace gbntt

@@ -1,0 +1,6 @@
+// gbntt_pass_p0.cu — pass kernels of prime index 0 (see gbntt_pass.cuh).
+#include "gbntt_pass.cuh"
+
+namespace gbntt {
+template cudaError_t launch_pass_prime<0>(int log_l, int dir, int ld, const PassArgs &a, cudaStream_t st);
+}  // namespace gbntt
