@@ -28,8 +28,11 @@ def _cuda_lib_dir():
 
 
 def _flags():
+    extra = []
+    if os.environ.get("GBNTT_PASS_MIN_BLOCKS"):   # tuning knob: resident CTAs per SM of the pass kernels
+        extra.append("-DGBNTT_PASS_MIN_BLOCKS=%d" % int(os.environ["GBNTT_PASS_MIN_BLOCKS"]))
     return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
-                   "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr"]
+                   "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr"] + extra
 
 
 def _deps():
@@ -37,7 +40,7 @@ def _deps():
 
 
 def stale():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or os.environ.get("GBNTT_FORCE_BUILD"):
         return True
     t = os.path.getmtime(LIB)
     return any(os.path.getmtime(d) > t for d in _deps())
