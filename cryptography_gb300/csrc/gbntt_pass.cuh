@@ -30,9 +30,6 @@ namespace gbntt {
 
 enum PassLayout { LAYOUT_STRIDED = 0, LAYOUT_CONTIG = 1 };
 
-#ifndef GBNTT_PASS_MIN_BLOCKS
-#define GBNTT_PASS_MIN_BLOCKS 5   // resident CTAs per SM the register budget targets
-#endif
 constexpr int kPassThreads = 128;
 constexpr int kLogPassThreads = 7;
 
@@ -85,128 +82,63 @@ __device__ __forceinline__ void dft_reg(uint64_t (&x)[1 << LOG_R], const uint64_
     }
 }
 
-// cp.async helpers (8-byte / 4-byte copies, zero-filled when src_bytes == 0).
-__device__ __forceinline__ void cp_async8(void *dst, const void *src, int src_bytes)
-{
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes));
-}
-__device__ __forceinline__ void cp_async4(void *dst, const void *src, int src_bytes)
-{
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
-// Shared-memory plan of one CTA (in 8-byte words):
-//   [0, L)              in-CTA twiddles twm[ka*B + b] = w_L^(b ka)
-//   then, by load kind:
-//   LD_U64: two tile buffers (double buffering)
-//   LD_U32: one 8-byte work tile + two 4-byte input tiles
-//   LD_PW : two 8-byte tiles (both spectra, single buffered)
-template <int LOG_L, int LD>
-struct PassSmem {
-    using S_ = PassShape<LOG_L>;
-    static constexpr int TILE = S_::G * S_::RS;     // words of one 8-byte tile
-    static constexpr int TW = S_::L;
-    static constexpr size_t BYTES = 8 * (size_t)(TW + (LD == LD_U32 ? TILE + TILE : 2 * TILE));
-};
-
-// Element (g, m) of tile `tile` -> global index, for both layouts.
-template <int LOG_L, int LAYOUT>
-struct TileAddr {
-    using S_ = PassShape<LOG_L>;
-    long long base;    // address of (g_thread, m_thread(it = 0))
-    long long step;    // address increment per iteration
-    __device__ __forceinline__ TileAddr(long long col0, int log_s, int log_m, int t)
-    {
-        if (LAYOUT == LAYOUT_STRIDED) {
-            const int g = t & (S_::G - 1), m0 = t >> S_::LOG_G;
-            const long long S = 1LL << log_s;
-            base = ((col0 >> log_s) << log_m) + (col0 & (S - 1)) + g + (long long)m0 * S;
-            step = (long long)S_::B * S;
-        } else {
-            base = (col0 << LOG_L) + t;
-            step = S_::T;
-        }
-    }
-};
-
-// Shared-memory word of iteration `it` of thread t (same mapping as TileAddr).
-template <int LOG_L, int LAYOUT>
-__device__ __forceinline__ int tile_slot(int t, int it)
-{
-    using S_ = PassShape<LOG_L>;
-    if (LAYOUT == LAYOUT_STRIDED) {
-        const int g = t & (S_::G - 1), m0 = t >> S_::LOG_G;
-        return g * S_::RS + m0 + it * (S_::B + 1);
-    } else {
-        const int e = t + it * S_::T;
-        const int g = e >> LOG_L, m = e & (S_::L - 1);
-        return g * S_::RS + m + (m >> S_::LOG_B);
-    }
-}
-
-// Row (column group member) of iteration `it` of thread t, for bounds checks
-// of the contiguous layout.
-template <int LOG_L, int LAYOUT>
-__device__ __forceinline__ int tile_row(int t, int it)
-{
-    using S_ = PassShape<LOG_L>;
-    return LAYOUT == LAYOUT_STRIDED ? (t & (S_::G - 1)) : ((t + it * S_::T) >> LOG_L);
-}
-
-// Issue the asynchronous loads of one tile (A copies per thread).
-template <int LOG_L, int LD, int LAYOUT>
-__device__ __forceinline__ void tile_load_async(const PassArgs &a, const uint64_t *src64, long long col0, void *dst,
-                                                int t)
-{
-    using S_ = PassShape<LOG_L>;
-    const TileAddr<LOG_L, LAYOUT> ad(col0, a.log_s, a.log_m, t);
-    const long long rows_left = a.ncols - col0;
-#pragma unroll 8
-    for (int it = 0; it < S_::A; it++) {
-        const long long addr = ad.base + it * ad.step;
-        const int slot = tile_slot<LOG_L, LAYOUT>(t, it);
-        const bool row_ok = LAYOUT == LAYOUT_STRIDED || tile_row<LOG_L, LAYOUT>(t, it) < rows_left;
-        if (LD == LD_U32) {
-            const bool ok = row_ok && addr < a.n_limbs;
-            cp_async4((uint32_t *)dst + slot, ok ? (const void *)(a.limbs + addr) : (const void *)a.limbs, ok ? 4 : 0);
-        } else {
-            cp_async8((uint64_t *)dst + slot, row_ok ? (const void *)(src64 + addr) : (const void *)src64,
-                      row_ok ? 8 : 0);
-        }
-    }
-}
-
-// Steps 1 and 2 of one tile, in place in `w` (8-byte words); `in32` is the
-// 4-byte input tile of the first forward pass, `inB` the second spectrum of
-// the pointwise pass.
 template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
-__device__ __forceinline__ void tile_compute(const PassArgs &a, uint64_t *w, const uint32_t *in32,
-                                             const uint64_t *inB, const uint64_t *twm, const uint64_t *w64,
-                                             long long col0, int t)
+__device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const uint64_t *w64)
 {
     using S_ = PassShape<LOG_L>;
-    constexpr int A = S_::A, B = S_::B, LOG_B = S_::LOG_B, RS = S_::RS;
+    constexpr int L = S_::L, A = S_::A, B = S_::B, LOG_B = S_::LOG_B, G = S_::G, LOG_G = S_::LOG_G;
+    constexpr int T = S_::T, RS = S_::RS;
+    const int t = threadIdx.x;
+    const long long col0 = (long long)blockIdx.x * G;
+    const int log_s = a.log_s, log_m = a.log_m;
+    uint64_t *data = a.data[PI];
     const uint64_t *twhi = a.tw.hi[PI];
     const uint64_t *twlo = a.tw.lo[PI];
-    const int sh = kMaxLog - a.log_m;
-    const uint64_t j0 = LAYOUT == LAYOUT_STRIDED ? (uint64_t)(col0 & ((1LL << a.log_s) - 1)) : 0ull;
+    const int sh = kMaxLog - log_m;
+    // column index within the sub-problem of the first column of this CTA
+    const uint64_t j0 = LAYOUT == LAYOUT_STRIDED ? (uint64_t)(col0 & ((1LL << log_s) - 1)) : 0ull;
+
+    // ---- load: tile element (g, m) -> sm[g*RS + m + m/B]
+    if (LAYOUT == LAYOUT_STRIDED) {
+        const int g = t & (G - 1), m0 = t >> LOG_G;            // m = m0 + it*B
+        const long long S = 1LL << log_s;
+        const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
+        const long long stepg = (long long)B * S;
+        uint64_t *dst = sm + g * RS + m0;
+#pragma unroll 8
+        for (int it = 0; it < A; it++) {
+            const long long addr = base + it * stepg;
+            uint64_t v;
+            if (LD == LD_U32) v = addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
+            else if (LD == LD_PW) v = mont_mul<PI>(data[addr], a.other[PI][addr]);
+            else v = data[addr];
+            dst[it * (B + 1)] = v;
+        }
+    } else {
+        const long long rows_left = a.ncols - col0;
+        const long long base = col0 << LOG_L;
+#pragma unroll 8
+        for (int it = 0; it < A; it++) {
+            const int e = t + it * T;
+            const int g = e >> LOG_L, m = e & (L - 1);
+            uint64_t v = 0;
+            if (g < rows_left) {
+                const long long addr = base + e;
+                if (LD == LD_U32) v = addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
+                else if (LD == LD_PW) v = mont_mul<PI>(data[addr], a.other[PI][addr]);
+                else v = data[addr];
+            }
+            sm[g * RS + m + (m >> LOG_B)] = v;
+        }
+    }
+    __syncthreads();
 
     // ---- step 1: one A-point DFT per (g, b) over the high digit
     {
         const int g = t >> LOG_B, b = t & (B - 1);
         uint64_t x[A];
 #pragma unroll
-        for (int i = 0; i < A; i++) {
-            const int idx = g * RS + i * (B + 1) + b;
-            if (LD == LD_U32) x[i] = in32[idx];
-            else if (LD == LD_PW) x[i] = mont_mul<PI>(w[idx], inB[idx]);
-            else x[i] = w[idx];
-        }
+        for (int i = 0; i < A; i++) x[i] = sm[g * RS + i * (B + 1) + b];
         if (DIR == 1 && (a.twiddle || a.use_scale)) {
             // inverse pass: input twiddle w_M^-((iB + b) j), times the scale
             const uint64_t j = j0 + (uint64_t)(LAYOUT == LAYOUT_STRIDED ? g : 0);
@@ -223,8 +155,9 @@ __device__ __forceinline__ void tile_compute(const PassArgs &a, uint64_t *w, con
 #pragma unroll
         for (int ka = 0; ka < A; ka++) {
             uint64_t v = x[bitrev(ka, S_::LOG_A)];
-            if (ka > 0 && b > 0) v = mont_mul<PI>(v, twm[ka * B + b]);   // w_L^(b ka)
-            w[g * RS + ka * (B + 1) + b] = v;
+            if (ka > 0 && b > 0)   // w_L^(b ka)
+                v = mont_mul<PI>(v, __ldg(twhi + ((b * ka) << (kTwBits - LOG_L))));
+            sm[g * RS + ka * (B + 1) + b] = v;
         }
     }
     __syncthreads();
@@ -243,7 +176,7 @@ __device__ __forceinline__ void tile_compute(const PassArgs &a, uint64_t *w, con
         for (int r = 0; r < R; r++) {
             const int ka = q + r * B;
 #pragma unroll
-            for (int i = 0; i < B; i++) y[r][i] = w[g * RS + ka * (B + 1) + i];
+            for (int i = 0; i < B; i++) y[r][i] = sm[g * RS + ka * (B + 1) + i];
             dft_reg<PI, LOG_B>(y[r], w64);
             if (DIR == 0 && LAYOUT == LAYOUT_STRIDED && a.twiddle) {
                 // forward pass: output twiddle w_M^((ka + A kb) j)
@@ -264,111 +197,38 @@ __device__ __forceinline__ void tile_compute(const PassArgs &a, uint64_t *w, con
 #pragma unroll
             for (int kb = 0; kb < B; kb++) {
                 const int k = ka + A * kb;
-                w[g * RS + k + (k >> LOG_B)] = y[r][bitrev(kb, LOG_B)];
+                sm[g * RS + k + (k >> LOG_B)] = y[r][bitrev(kb, LOG_B)];
             }
         }
     }
     __syncthreads();
-}
 
-// Global stores of one finished tile from `w`.
-template <int LOG_L, int LAYOUT>
-__device__ __forceinline__ void tile_store(const PassArgs &a, uint64_t *dst64, long long col0, const uint64_t *w, int t)
-{
-    using S_ = PassShape<LOG_L>;
-    const TileAddr<LOG_L, LAYOUT> ad(col0, a.log_s, a.log_m, t);
-    const long long rows_left = a.ncols - col0;
+    // ---- store: same addressing as the load
+    if (LAYOUT == LAYOUT_STRIDED) {
+        const int g = t & (G - 1), m0 = t >> LOG_G;
+        const long long S = 1LL << log_s;
+        const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
+        const long long stepg = (long long)B * S;
+        const uint64_t *src = sm + g * RS + m0;
 #pragma unroll 8
-    for (int it = 0; it < S_::A; it++) {
-        if (LAYOUT == LAYOUT_STRIDED || tile_row<LOG_L, LAYOUT>(t, it) < rows_left)
-            dst64[ad.base + it * ad.step] = w[tile_slot<LOG_L, LAYOUT>(t, it)];
+        for (int it = 0; it < A; it++) data[base + it * stepg] = src[it * (B + 1)];
+    } else {
+        const long long rows_left = a.ncols - col0;
+        const long long base = col0 << LOG_L;
+#pragma unroll 8
+        for (int it = 0; it < A; it++) {
+            const int e = t + it * T;
+            const int g = e >> LOG_L, m = e & (L - 1);
+            if (g < rows_left) data[base + e] = sm[g * RS + m + (m >> LOG_B)];
+        }
     }
 }
 
-// Persistent pass kernel: each CTA walks tiles blockIdx.x, +gridDim.x, ...;
-// the next tile's loads (cp.async) are in flight while the current one is
-// computed (not for the pointwise pass, which stages two spectra).
 template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
-__device__ __forceinline__ void pass_persistent(const PassArgs &a, uint64_t *sm, const uint64_t *w64)
-{
-    using S_ = PassShape<LOG_L>;
-    using P_ = PassSmem<LOG_L, LD>;
-    const int t = threadIdx.x;
-    const long long ntiles = (a.ncols + S_::G - 1) / S_::G;
-    uint64_t *twm = sm;
-    uint64_t *data = a.data[PI];
-    const uint64_t *twhi = a.tw.hi[PI];
-
-    // in-CTA twiddles, once per CTA: twm[ka*B + b] = w_L^(b ka)
-    for (int idx = t; idx < S_::L; idx += S_::T) {
-        const int ka = idx >> S_::LOG_B, b = idx & (S_::B - 1);
-        twm[idx] = __ldg(twhi + ((b * ka) << (kTwBits - LOG_L)));
-    }
-
-    long long tile = blockIdx.x;
-    if (LD == LD_PW) {
-        uint64_t *wA = sm + P_::TW, *wB = wA + P_::TILE;
-        for (; tile < ntiles; tile += gridDim.x) {
-            const long long col0 = tile * S_::G;
-            tile_load_async<LOG_L, LD_U64, LAYOUT>(a, data, col0, wA, t);
-            tile_load_async<LOG_L, LD_U64, LAYOUT>(a, a.other[PI], col0, wB, t);
-            cp_async_commit();
-            cp_async_wait<0>();
-            __syncthreads();
-            tile_compute<PI, LOG_L, DIR, LD, LAYOUT>(a, wA, nullptr, wB, twm, w64, col0, t);
-            tile_store<LOG_L, LAYOUT>(a, data, col0, wA, t);
-            __syncthreads();
-        }
-        return;
-    }
-
-    if (LD == LD_U32) {
-        uint64_t *work = sm + P_::TW;
-        uint32_t *in0 = (uint32_t *)(work + P_::TILE), *in1 = in0 + P_::TILE;
-        int cur = 0;
-        if (tile < ntiles) tile_load_async<LOG_L, LD_U32, LAYOUT>(a, nullptr, tile * S_::G, in0, t);
-        cp_async_commit();
-        for (; tile < ntiles; tile += gridDim.x) {
-            const long long col0 = tile * S_::G;
-            const long long next = tile + gridDim.x;
-            if (next < ntiles) tile_load_async<LOG_L, LD_U32, LAYOUT>(a, nullptr, next * S_::G, cur ? in0 : in1, t);
-            cp_async_commit();
-            cp_async_wait<1>();
-            __syncthreads();
-            tile_compute<PI, LOG_L, DIR, LD_U32, LAYOUT>(a, work, cur ? in1 : in0, nullptr, twm, w64, col0, t);
-            tile_store<LOG_L, LAYOUT>(a, data, col0, work, t);
-            __syncthreads();
-            cur ^= 1;
-        }
-        cp_async_wait<0>();
-        return;
-    }
-
-    uint64_t *buf0 = sm + P_::TW, *buf1 = buf0 + P_::TILE;
-    int cur = 0;
-    if (tile < ntiles) tile_load_async<LOG_L, LD_U64, LAYOUT>(a, data, tile * S_::G, buf0, t);
-    cp_async_commit();
-    for (; tile < ntiles; tile += gridDim.x) {
-        const long long col0 = tile * S_::G;
-        const long long next = tile + gridDim.x;
-        if (next < ntiles) tile_load_async<LOG_L, LD_U64, LAYOUT>(a, data, next * S_::G, cur ? buf0 : buf1, t);
-        cp_async_commit();
-        cp_async_wait<1>();
-        __syncthreads();
-        uint64_t *w = cur ? buf1 : buf0;
-        tile_compute<PI, LOG_L, DIR, LD_U64, LAYOUT>(a, w, nullptr, nullptr, twm, w64, col0, t);
-        tile_store<LOG_L, LAYOUT>(a, data, col0, w, t);
-        __syncthreads();
-        cur ^= 1;
-    }
-    cp_async_wait<0>();
-}
-
-template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
-__global__ void __launch_bounds__(kPassThreads, GBNTT_PASS_MIN_BLOCKS) ntt_pass_kernel(PassArgs a)
+__global__ void __launch_bounds__(kPassThreads, 4) ntt_pass_kernel(PassArgs a)
 {
     extern __shared__ uint64_t sm[];
-    pass_persistent<PI, LOG_L, DIR, LD, LAYOUT>(a, sm, a.w64);
+    pass_tile<PI, LOG_L, DIR, LD, LAYOUT>(a, sm, a.w64);
 }
 
 // Launcher for one prime (explicitly instantiated, one translation unit per
@@ -393,34 +253,8 @@ static cudaError_t launch_pass_l(int dir, int ld, const PassArgs &a, cudaStream_
         else if (ld == LD_U64 && layout == LAYOUT_STRIDED) fn = ntt_pass_kernel<PI, LOG_L, 1, LD_U64, LAYOUT_STRIDED>;
     }
     if (!fn) return cudaErrorInvalidValue;
-    size_t smem = 0;
-    if (ld == LD_U32) smem = PassSmem<LOG_L, LD_U32>::BYTES;
-    else if (ld == LD_PW) smem = PassSmem<LOG_L, LD_PW>::BYTES;
-    else smem = PassSmem<LOG_L, LD_U64>::BYTES;
-    // per-kernel one-time setup: shared-memory limit and resident CTAs per SM
-    struct Slot { void (*fn)(PassArgs); int per_sm; };
-    static Slot cache[8] = {};
-    int per_sm = 0;
-    for (auto &c : cache) {
-        if (c.fn == fn) { per_sm = c.per_sm; break; }
-    }
-    if (per_sm == 0) {
-        cudaError_t e = cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPassThreads, smem);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) return cudaErrorInvalidConfiguration;
-        for (auto &c : cache) {
-            if (!c.fn) { c.fn = fn; c.per_sm = per_sm; break; }
-        }
-    }
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long ntiles = (a.ncols + S_::G - 1) / S_::G;
-    const long long cap = (long long)sms * per_sm;
-    const long long gx = ntiles < cap ? ntiles : cap;
-    fn<<<(unsigned)gx, kPassThreads, smem, st>>>(a);
+    const long long gx = (a.ncols + S_::G - 1) / S_::G;
+    fn<<<(unsigned)gx, kPassThreads, S_::SMEM, st>>>(a);
     return cudaGetLastError();
 }
 
