@@ -30,6 +30,9 @@ namespace gbntt {
 
 enum PassLayout { LAYOUT_STRIDED = 0, LAYOUT_CONTIG = 1 };
 
+#ifndef GBNTT_PASS_MIN_BLOCKS
+#define GBNTT_PASS_MIN_BLOCKS 5   // resident CTAs per SM the register budget targets (measured best of 3..6)
+#endif
 constexpr int kPassThreads = 128;
 constexpr int kLogPassThreads = 7;
 
@@ -225,7 +228,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
 }
 
 template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
-__global__ void __launch_bounds__(kPassThreads, 4) ntt_pass_kernel(PassArgs a)
+__global__ void __launch_bounds__(kPassThreads, GBNTT_PASS_MIN_BLOCKS) ntt_pass_kernel(PassArgs a)
 {
     extern __shared__ uint64_t sm[];
     pass_tile<PI, LOG_L, DIR, LD, LAYOUT>(a, sm, a.w64);
