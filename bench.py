@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--cpu-log-limbs", type=int, default=22, help="CPU baseline sample size 2^k limbs")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plan", default="", help="comma-separated pass sizes overriding the default plan")
+    ap.add_argument("--no-packed", action="store_true", help="skip the packed (64-bit coefficient) measurement")
     return ap.parse_args()
 
 
@@ -251,6 +252,30 @@ def run_gpu(args, dist):
     total_ms = dist.max(total_ms)
     ms = total_ms / (args.steps * dist.world)
 
+    # packed mode (one 64-bit limb per coefficient, transform length 2^lg)
+    packed = None
+    if not args.no_packed:
+        def step64():
+            g.lib().gbntt_mul_u64(dc.ptr, da.ptr, n // 2, db.ptr, n // 2, None)
+        for _ in range(args.warmup):
+            step64()
+        cudart.stream_sync(stream)
+        p0, p1 = cudart.Event(), cudart.Event()
+        dist.barrier()
+        p0.record(stream)
+        for _ in range(args.steps):
+            step64()
+        p1.record(stream)
+        p1.synchronize()
+        dist.barrier()
+        pms = dist.max(p0.elapsed_ms(p1)) / (args.steps * dist.world)
+        flags |= g.device_errors()
+        bmp = 10 * 3 * (1 << lg) * 8 + 8 * (2 * n)
+        packed = {"ms": pms, "transform_log": lg, "bytes_model": bmp,
+                  "multiply_roofline_frac": bmp / (pms * 1e-3) / 1e9 / peaks()[0],
+                  "note": "same integers as 2^%d 64-bit limbs, one coefficient per limb (reference granularity); "
+                          "not the headline configuration" % (lg - 1)}
+
     # per-launch breakdown of one multiply (separate, instrumented run)
     g.launch_log(True)
     step()
@@ -335,6 +360,7 @@ def run_gpu(args, dist):
                               "frac": bm / (ms * 1e-3) / 1e9 / peak,
                               "model": "10*k*N*8 + 8*(n_a+n_b), k=3 (2-pass four-step with fused decomposition, "
                                        "pointwise product and Garner+carry)"},
+        "packed_64bit_coefficients": packed,
         "launch_breakdown": by_kind,
         "gpu_launches": launches_per_step * args.steps,
         "device_error_flags": flags,

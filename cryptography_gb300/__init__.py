@@ -33,6 +33,8 @@ from .engine import (  # noqa: F401
     lib_path,
     mul,
     mul_device,
+    mul64,
+    set_coeff_bits,
     plan,
     set_plan,
     sqr,

@@ -53,6 +53,8 @@ struct Engine {
     size_t io_words = 0;
     cudaStream_t stream = nullptr;
     uint64_t garner[4] = {0, 0, 0, 0};
+    uint64_t q01_lo = 0, q01_hi = 0;   // q0 * q1
+    int bigint_coeff_bits = 32;        // coefficient width used by the BigInt entry points
     unsigned long dispatch = 0;
     // profiling (NTT_PROFILE=1): host wall clock per phase
     int prof = 0;
@@ -168,8 +170,8 @@ static size_t workspace_bytes(int max_log)
     const size_t n = (size_t)1 << max_log;
     const size_t spec = 6 * n * sizeof(uint64_t);
     const size_t tw = 3 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t);
-    const size_t ctl = (2 + carry_tiles((long long)n + 1) + 64) * sizeof(unsigned);
-    const size_t io = (3 * n + 64) * sizeof(uint32_t);
+    const size_t ctl = (2 + carry_tiles64((long long)n + 1) + 64) * sizeof(unsigned);
+    const size_t io = (4 * n + 64) * sizeof(uint32_t);
     return spec + tw + ctl + io;
 }
 
@@ -203,8 +205,8 @@ static int init_impl(int max_log)
         free_all();
         return GBNTT_ERR_ALLOC;
     }
-    g.n_status = (size_t)carry_tiles((long long)g.n_max + 1) + 64;
-    g.io_words = 3 * g.n_max + 64;
+    g.n_status = (size_t)carry_tiles64((long long)g.n_max + 1) + 64;
+    g.io_words = 4 * g.n_max + 64;
     if (cudaMalloc(&g.d_ctl, (2 + g.n_status) * sizeof(unsigned)) != cudaSuccess ||
         cudaMalloc(&g.d_io, g.io_words * sizeof(uint32_t)) != cudaSuccess) {
         set_err("gbntt_init: device allocation of %zu bytes failed", workspace_bytes(max_log));
@@ -250,6 +252,15 @@ static int init_impl(int max_log)
     g.garner[1] = h_mont(q0 % q2, q2);
     g.garner[2] = h_mont(h_inv(h_mul(q0 % q2, q1 % q2, q2), q2), q2);
     g.garner[3] = 0;
+    {
+        const u128 q01 = (u128)q0 * q1;
+        g.q01_lo = (uint64_t)q01;
+        g.q01_hi = (uint64_t)(q01 >> 64);
+    }
+    {
+        const char *cb = getenv("GBNTT_COEFF_BITS");
+        g.bigint_coeff_bits = (cb && atoi(cb) == 64) ? 64 : 32;
+    }
     g.ready = true;
     return GBNTT_OK;
 }
@@ -262,14 +273,16 @@ static TwTables tables(int dir)
 }
 
 // Forward transform of one operand: limbs -> 3 spectra at spec[pi * stride].
-static int forward(uint64_t *spec, size_t stride, const uint32_t *limbs, size_t n, int L, cudaStream_t st)
+static int forward(uint64_t *spec, size_t stride, const void *limbs, size_t n, int L, cudaStream_t st,
+                   bool packed = false)
 {
     int pl[3];
     const int np = plan_passes(L, pl);
     PassArgs a;
     memset(&a, 0, sizeof a);
     for (int pi = 0; pi < 3; pi++) a.data[pi] = spec + pi * stride;
-    a.limbs = limbs;
+    a.limbs = packed ? nullptr : (const uint32_t *)limbs;
+    a.limbs64 = packed ? (const uint64_t *)limbs : nullptr;
     a.n_limbs = (long long)n;
     a.tw = tables(0);
     int log_m = L;
@@ -280,8 +293,8 @@ static int forward(uint64_t *spec, size_t stride, const uint32_t *limbs, size_t 
         a.twiddle = a.log_s > 0;
         const double nb8 = 8.0 * (double)((size_t)1 << L);
         for (int pi = 0; pi < 3; pi++) {
-            rec_begin(st, i == 0 ? 0 : 1, pl[i], i == 0 ? 4.0 * (double)n + nb8 : 2.0 * nb8);
-            CK(launch_pass_any(pi, pl[i], 0, i == 0 ? LD_U32 : LD_U64, a, st));
+            rec_begin(st, i == 0 ? 0 : 1, pl[i], i == 0 ? (packed ? 8.0 : 4.0) * (double)n + nb8 : 2.0 * nb8);
+            CK(launch_pass_any(pi, pl[i], 0, i == 0 ? (packed ? LD_U64LIMB : LD_U32) : LD_U64, a, st));
             rec_end(st);
         }
         log_m -= pl[i];
@@ -375,6 +388,59 @@ static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t
     return carry(d_c, n_out, specA, g.n_max, L, st);
 }
 
+static int carry64(uint64_t *d_c, size_t n_out, const uint64_t *specA, size_t stride, int L, cudaStream_t st)
+{
+    CarryArgs c;
+    memset(&c, 0, sizeof c);
+    for (int pi = 0; pi < 3; pi++) c.res[pi] = specA + pi * stride;
+    c.out64 = d_c;
+    c.n_coef = (long long)1 << L;
+    c.n_out = (long long)n_out;
+    c.ticket = g.d_ctl;
+    c.error = g.d_ctl + 1;
+    c.status = g.d_ctl + 2;
+    for (int i = 0; i < 4; i++) c.garner[i] = g.garner[i];
+    c.q01_lo = g.q01_lo;
+    c.q01_hi = g.q01_hi;
+    const long long nt = carry_tiles64((long long)n_out);
+    CK(cudaMemsetAsync(g.d_ctl, 0, sizeof(unsigned), st));
+    CK(cudaMemsetAsync(g.d_ctl + 2, 0, (size_t)nt * sizeof(unsigned), st));
+    rec_begin(st, 4, 0, 3.0 * 8.0 * (double)((size_t)1 << L) + 8.0 * (double)n_out);
+    CK(launch_garner_carry64(c, st, nullptr));
+    rec_end(st);
+    return GBNTT_OK;
+}
+
+// Packed mode: one 64-bit limb per coefficient (the reference's own
+// granularity), transform length >= n_a + n_b - 1 in 64-bit limbs.
+static int mul_dev64(uint64_t *d_c, const uint64_t *d_a, size_t na, const uint64_t *d_b, size_t nb, cudaStream_t st)
+{
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    if (!st) st = g.stream;
+    const size_t n_out = na + nb;
+    if (na == 0 || nb == 0) {
+        if (n_out) CK(cudaMemsetAsync(d_c, 0, n_out * sizeof(uint64_t), st));
+        return GBNTT_OK;
+    }
+    const int L = choose_log(na, nb);
+    if (L > g.max_log) {
+        set_err("product needs %zu coefficients but the engine was initialised for 2^%d", na + nb - 1, g.max_log);
+        return GBNTT_ERR_SIZE;
+    }
+    const bool square = (d_a == d_b && na == nb);
+    uint64_t *specA = g.d_spec;
+    uint64_t *specB = g.d_spec + 3 * g.n_max;
+    int rc = forward(specA, g.n_max, d_a, na, L, st, true);
+    if (rc) return rc;
+    if (!square) {
+        rc = forward(specB, g.n_max, d_b, nb, L, st, true);
+        if (rc) return rc;
+    }
+    rc = inverse(specA, square ? specA : specB, g.n_max, L, st, square);
+    if (rc) return rc;
+    return carry64(d_c, n_out, specA, g.n_max, L, st);
+}
+
 static int read_errors(unsigned *flags)
 {
     unsigned v = 0;
@@ -408,6 +474,42 @@ static int mul_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b
     if (rc) return rc;
     if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[1] += t - t0; t0 = t; }
     CK(cudaMemcpyAsync(c, dc, n_out * 4, cudaMemcpyDeviceToHost, g.stream));
+    unsigned flags = 0;
+    rc = read_errors(&flags);
+    if (rc) return rc;
+    if (g.prof) { double t = now_ms(); g.prof_ms[2] += t - t0; g.prof_calls++; }
+    if (flags) {
+        set_err("device check failed (flags 0x%x): %s", flags,
+                (flags & ERR_GARNER_DIGIT) ? "CRT digit out of range" : "carry look-back wait gave up");
+        return GBNTT_ERR_DEVICE;
+    }
+    return GBNTT_OK;
+}
+
+// Host-pointer packed product through the staging buffer.
+static int mul_host64(uint64_t *c, const uint64_t *a, size_t na, const uint64_t *b, size_t nb, const uint64_t *dev_a,
+                      const uint64_t *dev_b)
+{
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    const size_t n_out = na + nb;
+    if (na == 0 || nb == 0) { if (n_out) memset(c, 0, n_out * 8); return GBNTT_OK; }
+    if (choose_log(na, nb) > g.max_log) {
+        set_err("product needs %zu coefficients but the engine was initialised for 2^%d", na + nb - 1, g.max_log);
+        return GBNTT_ERR_SIZE;
+    }
+    const bool square = (a == b && na == nb);
+    uint64_t *io = (uint64_t *)g.d_io;
+    uint64_t *da = io, *db = io + na, *dc = io + na + (square ? 0 : nb);
+    double t0 = g.prof ? now_ms() : 0;
+    const uint64_t *ua = dev_a, *ub = dev_b;
+    if (!ua) { CK(cudaMemcpyAsync(da, a, na * 8, cudaMemcpyHostToDevice, g.stream)); ua = da; }
+    if (square) ub = ua;
+    else if (!ub) { CK(cudaMemcpyAsync(db, b, nb * 8, cudaMemcpyHostToDevice, g.stream)); ub = db; }
+    if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[0] += t - t0; t0 = t; }
+    int rc = mul_dev64(dc, ua, na, ub, nb, g.stream);
+    if (rc) return rc;
+    if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[1] += t - t0; t0 = t; }
+    CK(cudaMemcpyAsync(c, dc, n_out * 8, cudaMemcpyDeviceToHost, g.stream));
     unsigned flags = 0;
     rc = read_errors(&flags);
     if (rc) return rc;
@@ -463,9 +565,11 @@ static int bigint_mul_impl(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_b
                 newcap);
         return GBNTT_ERR_MANAGED_CAP;
     }
-    const size_t n_out = na + nb;
+    const bool packed = g.bigint_coeff_bits == 64;
+    // 32-bit words written: the packed path writes whole 64-bit limbs
+    const size_t n_out = packed ? 2 * (size_t)(na64 + nb64) : na + nb;
     if (alias || c->cap < newcap) {
-        tmp = (uint32_t *)malloc((n_out + 1) * sizeof(uint32_t));
+        tmp = (uint32_t *)malloc((n_out + 2) * sizeof(uint32_t));
         if (!tmp) { set_err("host allocation failed"); return GBNTT_ERR_ALLOC; }
         outp = tmp;
     } else {
@@ -474,6 +578,11 @@ static int bigint_mul_impl(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_b
     int rc = GBNTT_OK;
     if (na == 0 || nb == 0) {
         memset(outp, 0, n_out * 4);
+    } else if (packed) {
+        // one 64-bit limb per coefficient
+        const uint64_t *pa = a->limbs, *pb = b->limbs;
+        rc = mul_host64((uint64_t *)outp, pa, (size_t)na64, square ? pa : pb, square ? (size_t)na64 : (size_t)nb64,
+                        a->managed ? pa : nullptr, (!square && b->managed) ? pb : nullptr);
     } else {
         const uint32_t *pa = (const uint32_t *)a->limbs, *pb = (const uint32_t *)b->limbs;
         rc = mul_host(outp, pa, na, square ? pa : pb, square ? na : nb, a->managed ? pa : nullptr,
@@ -600,6 +709,36 @@ int gbntt_mul_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t 
     if (!d_c || (na && !d_a) || (nb && !d_b)) { set_err("null pointer"); return GBNTT_ERR_ARG; }
     return mul_dev(d_c, d_a, na, d_b, nb, (cudaStream_t)stream);
 }
+
+int gbntt_mul_u64(uint64_t *d_c, const uint64_t *d_a, size_t na, const uint64_t *d_b, size_t nb, void *stream)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!d_c || (na && !d_a) || (nb && !d_b)) { set_err("null pointer"); return GBNTT_ERR_ARG; }
+    return mul_dev64(d_c, d_a, na, d_b, nb, (cudaStream_t)stream);
+}
+
+int gbntt_sqr_u64(uint64_t *d_c, const uint64_t *d_a, size_t na, void *stream)
+{
+    return gbntt_mul_u64(d_c, d_a, na, d_a, na, stream);
+}
+
+int gbntt_mul_u64_host(uint64_t *c, const uint64_t *a, size_t na, const uint64_t *b, size_t nb)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!c || (na && !a) || (nb && !b)) { set_err("null pointer"); return GBNTT_ERR_ARG; }
+    return mul_host64(c, a, na, b, nb, nullptr, nullptr);
+}
+
+int gbntt_set_coeff_bits(int bits)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (bits != 32 && bits != 64) { set_err("gbntt_set_coeff_bits: 32 or 64"); return GBNTT_ERR_ARG; }
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    g.bigint_coeff_bits = bits;
+    return GBNTT_OK;
+}
+
+int gbntt_coeff_bits(void) { return g.bigint_coeff_bits; }
 
 int gbntt_sqr_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, void *stream)
 {

@@ -12,7 +12,7 @@ constexpr int kTwSize = 1 << kTwBits;
 constexpr int kMinLog = 5;         // smallest transform length used (32)
 constexpr int kMaxPassLog = 10;    // largest sub-DFT staged in one CTA
 
-enum LoadKind { LD_U64 = 0, LD_U32 = 1, LD_PW = 2 };
+enum LoadKind { LD_U64 = 0, LD_U32 = 1, LD_PW = 2, LD_U64LIMB = 3 };
 
 // Twiddle tables of one direction for the three primes: Montgomery forms of
 // w^e, w the primitive 2^30-th root g^((p-1)/2^30) (or its inverse), with
@@ -26,6 +26,7 @@ struct PassArgs {
     uint64_t *data[3];          // residues per prime, transformed in place
     const uint64_t *other[3];   // second spectrum for the fused pointwise product
     const uint32_t *limbs;      // 32-bit limbs for the fused decomposition
+    const uint64_t *limbs64;    // 64-bit limbs (one per coefficient) for the packed mode
     long long n_limbs;          // limbs beyond this index read as zero
     TwTables tw;
     uint64_t scale[3];          // Montgomery constant folded into inverse twiddles
@@ -40,13 +41,15 @@ struct PassArgs {
 
 struct CarryArgs {
     const uint64_t *res[3];     // inverse-transform output, natural order
-    uint32_t *out;              // product limbs
+    uint32_t *out;              // product limbs (32-bit coefficient mode)
+    uint64_t *out64;            // product limbs (64-bit coefficient mode)
     long long n_coef;           // length of res[] (the transform length N)
     long long n_out;            // limbs to write
     unsigned int *ticket;       // dynamic tile counter (zeroed per launch)
     unsigned int *status;       // per-tile look-back words (zeroed per launch)
     unsigned int *error;        // sticky error bits
     uint64_t garner[4];         // Montgomery Garner constants (see engine)
+    uint64_t q01_lo, q01_hi;    // q0 * q1 as 128 bits (64-bit coefficient mode)
 };
 
 enum ErrorBits : unsigned int {
@@ -58,7 +61,9 @@ enum ErrorBits : unsigned int {
 template <int PI>
 cudaError_t launch_pass_prime(int log_l, int dir, int ld, const PassArgs &a, cudaStream_t st);
 cudaError_t launch_garner_carry(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out);
+cudaError_t launch_garner_carry64(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out);
 long long carry_tiles(long long n_out);
+long long carry_tiles64(long long n_out);
 cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *b, uint64_t *out, long long n,
                           cudaStream_t stream);
 

@@ -74,6 +74,42 @@ constexpr unsigned kFnIdentity = 0u | (1u << 2) | (2u << 4);
 
 __device__ __forceinline__ int spad(int q) { return q + (q >> 5); }
 
+// Decoupled look-back (one thread per tile): publishes this tile's carry
+// transfer function, walks predecessors until an inclusive carry (or a
+// constant composed function) is known, publishes its own inclusive carry
+// and returns the carry into the tile. Status word: bits 8-9 flag (1 =
+// aggregate function, 2 = inclusive carry), bits 0-5 value. Every wait is
+// bounded; on timeout the error bit is set and carry 0 is assumed.
+__device__ unsigned lookback_carry(unsigned *status, long long tile, unsigned block_agg, unsigned &err)
+{
+    unsigned cin = 0;
+    if (tile == 0) {
+        atomicExch(&status[0], (2u << 8) | fn_apply(block_agg, 0));
+        return 0;
+    }
+    atomicExch(&status[tile], (1u << 8) | block_agg);
+    unsigned acc = kFnIdentity;
+    long long j = tile - 1;
+    for (;;) {
+        unsigned w = 0;
+        int spins = 0;
+        for (;;) {
+            w = atomicAdd(&status[j], 0u);
+            if (w >> 8) break;
+            if (++spins > kLookbackSpinLimit) { err |= ERR_LOOKBACK_TIMEOUT; w = 2u << 8; break; }
+            __nanosleep(32);
+        }
+        const unsigned flag = w >> 8, val = w & 63u;
+        if (flag == 2) { cin = fn_apply(acc, val); break; }
+        acc = fn_compose(acc, val);
+        const unsigned c0 = fn_apply(acc, 0);
+        if (c0 == fn_apply(acc, 1) && c0 == fn_apply(acc, 2)) { cin = c0; break; }
+        --j;
+    }
+    atomicExch(&status[tile], (2u << 8) | fn_apply(block_agg, cin));
+    return cin;
+}
+
 // c_j from its residues (mixed radix, Garner): returns the three 32-bit words
 // of c_j < 2^96 and flags a nonzero third digit (c_j >= q0*q1 means the
 // residues are corrupted: a true coefficient is below 2^93).
@@ -176,34 +212,7 @@ __global__ void __launch_bounds__(kCarryThreads) garner_carry_kernel(CarryArgs a
     const unsigned thread_prefix = fn_compose(lane_excl, warp_prefix);
 
     // phase 4: decoupled look-back for this tile's carry-in (bounded waits)
-    if (tid == 0) {
-        unsigned cin = 0;
-        if (tile == 0) {
-            atomicExch(&a.status[0], (2u << 8) | fn_apply(block_agg, 0));
-        } else {
-            atomicExch(&a.status[tile], (1u << 8) | block_agg);
-            unsigned acc = kFnIdentity;
-            long long j = tile - 1;
-            for (;;) {
-                unsigned w = 0;
-                int spins = 0;
-                for (;;) {
-                    w = atomicAdd(&a.status[j], 0u);
-                    if (w >> 8) break;
-                    if (++spins > kLookbackSpinLimit) { err |= ERR_LOOKBACK_TIMEOUT; w = 2u << 8; break; }
-                    __nanosleep(32);
-                }
-                const unsigned flag = w >> 8, val = w & 63u;
-                if (flag == 2) { cin = fn_apply(acc, val); break; }
-                acc = fn_compose(acc, val);
-                const unsigned c0 = fn_apply(acc, 0);
-                if (c0 == fn_apply(acc, 1) && c0 == fn_apply(acc, 2)) { cin = c0; break; }
-                --j;
-            }
-            atomicExch(&a.status[tile], (2u << 8) | fn_apply(block_agg, cin));
-        }
-        s_cin = cin;
-    }
+    if (tid == 0) s_cin = lookback_carry(a.status, tile, block_agg, err);
     __syncthreads();
 
     // phase 5: final limbs with this thread's carry-in, coalesced store
@@ -223,6 +232,150 @@ __global__ void __launch_bounds__(kCarryThreads) garner_carry_kernel(CarryArgs a
         if (pos < a.n_out) a.out[pos] = out_s[spad(q)];
     }
     if (err) atomicOr(a.error, err);
+}
+
+// ---------------------------------------------------------------------------
+// Garner + carry for 64-bit coefficients (packed mode): one 64-bit limb per
+// coefficient, as the reference engine does (ntt/lib/arith/bigint.h:30-43).
+// A coefficient is below n * 2^128 < 2^158 and needs all three mixed-radix
+// digits: c = a0 + a1 q0 + a2 q0 q1 < 2^192, three 64-bit words w0..w2.
+// Product limb j = w0(c_j) + w1(c_{j-1}) + w2(c_{j-2}) + carry; the carry
+// into a limb is again 0, 1 or 2, so the scan monoid is the one above.
+// ---------------------------------------------------------------------------
+constexpr int kCarry64Threads = 256;
+constexpr int kCarry64PerThread = 4;
+constexpr int kCarry64Tile = kCarry64Threads * kCarry64PerThread;
+
+long long carry_tiles64(long long n_out) { return (n_out + kCarry64Tile - 1) / kCarry64Tile; }
+
+typedef unsigned __int128 u128;
+
+__device__ __forceinline__ void garner_coef64(const CarryArgs &a, long long j, uint64_t &w0, uint64_t &w1,
+                                              uint64_t &w2, unsigned &err)
+{
+    if (j < 0 || j >= a.n_coef) { w0 = w1 = w2 = 0; return; }
+    constexpr uint64_t q0 = Prime<0>::P, q1 = Prime<1>::P, q2 = Prime<2>::P;
+    const uint64_t r0 = a.res[0][j], r1 = a.res[1][j], r2 = a.res[2][j];
+    const uint64_t a0 = r0;
+    const uint64_t a0_1 = a0 >= q1 ? a0 - q1 : a0;
+    const uint64_t a1 = mont_mul<1>(sub_mod<1>(r1, a0_1), a.garner[0]);
+    const uint64_t a0_2 = a0 >= q2 ? a0 - q2 : a0;
+    uint64_t t = sub_mod<2>(r2, a0_2);
+    t = sub_mod<2>(t, mont_mul<2>(a1, a.garner[1]));
+    const uint64_t a2 = mont_mul<2>(t, a.garner[2]);
+    // c = a0 + a1 q0 + a2 (q0 q1)
+    u128 lo = (u128)a1 * q0 + a0;                     // < 2^128
+    const u128 x = (u128)a2 * a.q01_lo;
+    const u128 y = (u128)a2 * a.q01_hi;
+    u128 s0 = (u128)(uint64_t)lo + (uint64_t)x;
+    w0 = (uint64_t)s0;
+    u128 s1 = (s0 >> 64) + (uint64_t)(lo >> 64) + (uint64_t)(x >> 64) + (uint64_t)y;
+    w1 = (uint64_t)s1;
+    w2 = (uint64_t)(s1 >> 64) + (uint64_t)(y >> 64);
+    // a true coefficient is below 2^158: a larger top word means corrupted residues
+    if ((w2 >> 31) != 0) err |= ERR_GARNER_DIGIT;
+}
+
+__global__ void __launch_bounds__(kCarry64Threads) garner_carry64_kernel(CarryArgs a)
+{
+    constexpr int T = kCarry64Threads, K = kCarry64PerThread, TILE = kCarry64Tile;
+    constexpr int SW = TILE + 2 + (TILE + 2) / 32 + 1;
+    __shared__ uint64_t W0[SW], W1[SW], W2[SW];
+    __shared__ unsigned s_warp[T / 32];
+    __shared__ unsigned s_tile, s_cin;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(a.ticket, 1u);
+    __syncthreads();
+    const long long tile = s_tile;
+    const long long base = tile * TILE;
+    unsigned err = 0;
+
+#pragma unroll
+    for (int r = 0; r < K; r++) {
+        const int q = r * T + tid;
+        uint64_t w0, w1, w2;
+        garner_coef64(a, base + q, w0, w1, w2, err);
+        W0[spad(q + 2)] = w0; W1[spad(q + 2)] = w1; W2[spad(q + 2)] = w2;
+    }
+    if (tid < 2) {
+        uint64_t w0, w1, w2;
+        garner_coef64(a, base - 2 + tid, w0, w1, w2, err);
+        W0[spad(tid)] = w0; W1[spad(tid)] = w1; W2[spad(tid)] = w2;
+    }
+    __syncthreads();
+
+    const int q0 = tid * K;
+    u128 s[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int q = q0 + k;
+        s[k] = (u128)W0[spad(q + 2)] + W1[spad(q + 1)] + W2[spad(q)];
+    }
+    unsigned fn;
+    {
+        u128 c = 0;
+        bool all_max = true, rest_max = true, low_ge = false;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const u128 v = s[k] + c;
+            const uint64_t limb = (uint64_t)v;
+            c = v >> 64;
+            if (limb != ~0ull) all_max = false;
+            if (k == 0) low_ge = limb >= ~0ull - 1;
+            else if (limb != ~0ull) rest_max = false;
+        }
+        const unsigned f0 = (unsigned)c;
+        const unsigned f1 = f0 + (all_max ? 1u : 0u);
+        const unsigned f2 = f0 + ((rest_max && low_ge) ? 1u : 0u);
+        fn = f0 | (f1 << 2) | (f2 << 4);
+    }
+
+    unsigned inc = fn;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned o = __shfl_up_sync(0xFFFFFFFFu, inc, d);
+        if (lane >= d) inc = fn_compose(inc, o);
+    }
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    unsigned warp_prefix = kFnIdentity, block_agg = kFnIdentity;
+#pragma unroll
+    for (int w = 0; w < T / 32; w++) {
+        if (w == warp) warp_prefix = block_agg;
+        block_agg = fn_compose(s_warp[w], block_agg);
+    }
+    unsigned lane_excl = __shfl_up_sync(0xFFFFFFFFu, inc, 1);
+    if (lane == 0) lane_excl = kFnIdentity;
+    const unsigned thread_prefix = fn_compose(lane_excl, warp_prefix);
+
+    if (tid == 0) s_cin = lookback_carry(a.status, tile, block_agg, err);
+    __syncthreads();
+
+    u128 c = fn_apply(thread_prefix, s_cin);
+    uint64_t *out_s = W0;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const u128 v = s[k] + c;
+        c = v >> 64;
+        out_s[spad(q0 + k)] = (uint64_t)v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < K; r++) {
+        const int q = r * T + tid;
+        const long long pos = base + q;
+        if (pos < a.n_out) a.out64[pos] = out_s[spad(q)];
+    }
+    if (err) atomicOr(a.error, err);
+}
+
+cudaError_t launch_garner_carry64(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out)
+{
+    const long long nt = carry_tiles64(args.n_out);
+    if (ntiles_out) *ntiles_out = nt;
+    if (nt == 0) return cudaSuccess;
+    garner_carry64_kernel<<<(unsigned)nt, kCarry64Threads, 0, stream>>>(args);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_garner_carry(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out)

@@ -85,6 +85,16 @@ __device__ __forceinline__ void dft_reg(uint64_t (&x)[1 << LOG_R], const uint64_
     }
 }
 
+// Residue of a 64-bit limb (zero beyond n_limbs): limb < 2^64 < 2p, so one
+// conditional subtract reduces it (the reference reduces with a 128-bit %,
+// ntt/lib/arith/bigint.c:286-294).
+template <int PI>
+__device__ __forceinline__ uint64_t limb64_residue(const PassArgs &a, long long addr)
+{
+    uint64_t v = addr < a.n_limbs ? __ldg(a.limbs64 + addr) : 0ull;
+    return v >= Prime<PI>::P ? v - Prime<PI>::P : v;
+}
+
 template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
 __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const uint64_t *w64)
 {
@@ -113,6 +123,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
             const long long addr = base + it * stepg;
             uint64_t v;
             if (LD == LD_U32) v = addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
+            else if (LD == LD_U64LIMB) v = limb64_residue<PI>(a, addr);
             else if (LD == LD_PW) v = mont_mul<PI>(data[addr], a.other[PI][addr]);
             else v = data[addr];
             dst[it * (B + 1)] = v;
@@ -128,6 +139,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
             if (g < rows_left) {
                 const long long addr = base + e;
                 if (LD == LD_U32) v = addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
+                else if (LD == LD_U64LIMB) v = limb64_residue<PI>(a, addr);
                 else if (LD == LD_PW) v = mont_mul<PI>(data[addr], a.other[PI][addr]);
                 else v = data[addr];
             }
@@ -246,6 +258,9 @@ static cudaError_t launch_pass_l(int dir, int ld, const PassArgs &a, cudaStream_
         if (ld == LD_U32)
             fn = layout == LAYOUT_STRIDED ? ntt_pass_kernel<PI, LOG_L, 0, LD_U32, LAYOUT_STRIDED>
                                           : ntt_pass_kernel<PI, LOG_L, 0, LD_U32, LAYOUT_CONTIG>;
+        else if (ld == LD_U64LIMB)
+            fn = layout == LAYOUT_STRIDED ? ntt_pass_kernel<PI, LOG_L, 0, LD_U64LIMB, LAYOUT_STRIDED>
+                                          : ntt_pass_kernel<PI, LOG_L, 0, LD_U64LIMB, LAYOUT_CONTIG>;
         else
             fn = layout == LAYOUT_STRIDED ? ntt_pass_kernel<PI, LOG_L, 0, LD_U64, LAYOUT_STRIDED>
                                           : ntt_pass_kernel<PI, LOG_L, 0, LD_U64, LAYOUT_CONTIG>;

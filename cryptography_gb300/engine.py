@@ -40,6 +40,7 @@ EXPORTS = (
     "gbntt_workspace_bytes", "gbntt_transform_log", "gbntt_plan", "gbntt_mul_u32", "gbntt_sqr_u32",
     "gbntt_mul_u32_host", "gbntt_device_errors", "gbntt_debug_forward", "gbntt_last_error", "gbntt_stream",
     "gbntt_launch_log", "gbntt_launch_records", "gbntt_set_plan", "gbntt_debug_modops",
+    "gbntt_mul_u64", "gbntt_sqr_u64", "gbntt_mul_u64_host", "gbntt_set_coeff_bits", "gbntt_coeff_bits",
 )
 
 _lib = None
@@ -97,6 +98,15 @@ def lib():
     L.gbntt_debug_forward.restype = ctypes.c_int
     L.gbntt_debug_modops.argtypes = [ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _sz, _vp]
     L.gbntt_debug_modops.restype = ctypes.c_int
+    L.gbntt_mul_u64.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp]
+    L.gbntt_mul_u64.restype = ctypes.c_int
+    L.gbntt_sqr_u64.argtypes = [_vp, _vp, _sz, _vp]
+    L.gbntt_sqr_u64.restype = ctypes.c_int
+    L.gbntt_mul_u64_host.argtypes = [_u64p, _u64p, _sz, _u64p, _sz]
+    L.gbntt_mul_u64_host.restype = ctypes.c_int
+    L.gbntt_set_coeff_bits.argtypes = [ctypes.c_int]
+    L.gbntt_set_coeff_bits.restype = ctypes.c_int
+    L.gbntt_coeff_bits.restype = ctypes.c_int
     L.gbntt_set_plan.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.gbntt_set_plan.restype = ctypes.c_int
     L.gbntt_launch_log.argtypes = [ctypes.c_int]
@@ -184,6 +194,24 @@ def mul(a, b):
     _check(lib().gbntt_mul_u32_host(c.ctypes.data_as(_u32p), a.ctypes.data_as(_u32p), len(a),
                                     b.ctypes.data_as(_u32p), len(b)))
     return c
+
+
+def _u64(a):
+    return np.ascontiguousarray(a, dtype=np.uint64)
+
+
+def mul64(a, b):
+    """Packed-mode product of two uint64 limb vectors; returns na+nb limbs."""
+    a = _u64(a)
+    b = a if b is a else _u64(b)
+    c = np.zeros(len(a) + len(b), dtype=np.uint64)
+    _check(lib().gbntt_mul_u64_host(c.ctypes.data_as(_u64p), a.ctypes.data_as(_u64p), len(a),
+                                    b.ctypes.data_as(_u64p), len(b)))
+    return c
+
+
+def set_coeff_bits(bits):
+    _check(lib().gbntt_set_coeff_bits(int(bits)))
 
 
 def sqr(a):

@@ -126,6 +126,21 @@ int gbntt_mul_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t 
                   void *stream);
 int gbntt_sqr_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, void *stream);
 
+/* Packed mode: one 64-bit limb per coefficient (the reference engine's own
+ * granularity, ntt/lib/arith/bigint.h:30-43). Operands and product are
+ * 64-bit limb arrays (na, nb counted in 64-bit limbs; d_c gets na + nb
+ * limbs); the transform length is the smallest power of two >= na + nb - 1,
+ * half that of the 32-bit form for the same integers. Stream-ordered. */
+int gbntt_mul_u64(uint64_t *d_c, const uint64_t *d_a, size_t na, const uint64_t *d_b, size_t nb, void *stream);
+int gbntt_sqr_u64(uint64_t *d_c, const uint64_t *d_a, size_t na, void *stream);
+int gbntt_mul_u64_host(uint64_t *c, const uint64_t *a, size_t na, const uint64_t *b, size_t nb);
+
+/* Coefficient width (32 or 64 bits) used by the BigInt entry points
+ * (ntt_bigint_mul and friends). Default 32, or 64 when the environment sets
+ * GBNTT_COEFF_BITS=64 at initialisation. */
+int gbntt_set_coeff_bits(int bits);
+int gbntt_coeff_bits(void);
+
 /* Host-pointer form: copies in, multiplies, copies out, synchronises and
  * checks the device error flags. c must hold na + nb limbs. */
 int gbntt_mul_u32_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b, size_t nb);

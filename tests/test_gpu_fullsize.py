@@ -64,6 +64,18 @@ def test_full_size_square(big_engine):
     _check_product(a, a, c)
 
 
+@pytest.mark.gpu
+def test_full_size_packed_multiply(big_engine):
+    # the same 2^28 x 2^28 32-bit-limb integers as 2^27 x 2^27 64-bit limbs,
+    # one coefficient per 64-bit limb (transform length 2^28)
+    n = 1 << 28
+    a = synth.operand(n, 5)
+    b = synth.operand(n, 6)
+    c = big_engine.mul64(a.view(np.uint64), b.view(np.uint64)).view(np.uint32)
+    _check_product(a, b, c)
+    assert big_engine.device_errors() == 0
+
+
 def test_checksum_detects_corruption():
     # the property check itself is not vacuous: one flipped limb fails it
     # (planted on the CPU, in a copy of an oracle product)
