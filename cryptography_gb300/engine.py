@@ -41,6 +41,7 @@ EXPORTS = (
     "gbntt_mul_u32_host", "gbntt_device_errors", "gbntt_debug_forward", "gbntt_last_error", "gbntt_stream",
     "gbntt_launch_log", "gbntt_launch_records", "gbntt_set_plan", "gbntt_debug_modops",
     "gbntt_mul_u64", "gbntt_sqr_u64", "gbntt_mul_u64_host", "gbntt_set_coeff_bits", "gbntt_coeff_bits",
+    "gbntt_mul_u32_noalloc",
 )
 
 _lib = None
@@ -107,6 +108,8 @@ def lib():
     L.gbntt_set_coeff_bits.argtypes = [ctypes.c_int]
     L.gbntt_set_coeff_bits.restype = ctypes.c_int
     L.gbntt_coeff_bits.restype = ctypes.c_int
+    L.gbntt_mul_u32_noalloc.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp]
+    L.gbntt_mul_u32_noalloc.restype = ctypes.c_int
     L.gbntt_set_plan.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.gbntt_set_plan.restype = ctypes.c_int
     L.gbntt_launch_log.argtypes = [ctypes.c_int]

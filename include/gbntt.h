@@ -172,6 +172,21 @@ int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d
 int gbntt_launch_log(int enable);
 int gbntt_launch_records(int *kind, int *log_l, double *bytes, float *ms, int max_records);
 
+/* No counterpart in the reference. gbntt_mul_u32 without any allocation:
+ * for callers that cannot allocate device memory where they need a product
+ * (an application whose device allocator is owned by a pool or arena that
+ * forbids cudaMalloc/cudaFree, latency-critical loops where cudaMalloc would
+ * synchronise the device, or code that has no engine initialised).
+ * d_c[0 .. na+nb) = d_a * d_b for na + nb - 1 <= 2^16 (GBNTT_ERR_SIZE above
+ * that); needs no gbntt_init. All scratch (about 4.6 MB) is one static
+ * device array that every GPU loading this library keeps until exit. The
+ * first call on each device (with that device current) sets the array up
+ * with cudaGetSymbolAddress and cudaMemcpy, so make that first call before
+ * any stream capture. Calls share the array: calls that overlap on the GPU
+ * race; serialise them (one stream, one thread at a time). Stream-ordered. */
+int gbntt_mul_u32_noalloc(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb,
+                          void *stream);
+
 /* Last error message of this library. */
 const char *gbntt_last_error(void);
 
