@@ -19,6 +19,7 @@ from .engine import (  # noqa: F401
     GBNTT_ERR_NOT_INIT,
     GBNTT_ERR_SIZE,
     GBNTT_OK,
+    batch_mul_device,
     bigint_alloc,
     bigint_free,
     bigint_from_int,

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <mutex>
 #include <vector>
+#include <algorithm>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -55,6 +56,10 @@ struct Engine {
     uint64_t garner[4] = {0, 0, 0, 0};
     uint64_t q01_lo = 0, q01_hi = 0;   // q0 * q1
     int bigint_coeff_bits = 32;        // coefficient width used by the BigInt entry points
+    // batched calls: two slots of per-wave tables (device + pinned host)
+    uint64_t *d_btab = nullptr;
+    uint64_t *h_btab = nullptr;
+    cudaEvent_t btab_ev[2] = {nullptr, nullptr};
     unsigned long dispatch = 0;
     // profiling (NTT_PROFILE=1): host wall clock per phase
     int prof = 0;
@@ -175,9 +180,18 @@ static size_t workspace_bytes(int max_log)
     return spec + tw + ctl + io;
 }
 
+// Products per batched wave and the 8-byte words of one wave's tables:
+// limb pointers and lengths of A and B, output pointers and lengths,
+// carry tile starts (W + 1).
+constexpr int kMaxBatch = 16384;
+constexpr size_t kBtabWords = 7 * (size_t)kMaxBatch + 8;
+
 static void free_all()
 {
     if (g.stream) cudaStreamSynchronize(g.stream);
+    cudaFree(g.d_btab);
+    if (g.h_btab) cudaFreeHost(g.h_btab);
+    for (int i = 0; i < 2; i++) if (g.btab_ev[i]) cudaEventDestroy(g.btab_ev[i]);
     cudaFree(g.d_spec);
     cudaFree(g.d_tw);
     cudaFree(g.d_ctl);
@@ -215,6 +229,14 @@ static int init_impl(int max_log)
         return GBNTT_ERR_ALLOC;
     }
     CK(cudaMemset(g.d_ctl, 0, (2 + g.n_status) * sizeof(unsigned)));
+    if (cudaMalloc(&g.d_btab, 2 * kBtabWords * sizeof(uint64_t)) != cudaSuccess ||
+        cudaMallocHost(&g.h_btab, 2 * kBtabWords * sizeof(uint64_t)) != cudaSuccess) {
+        set_err("gbntt_init: batch table allocation failed");
+        cudaGetLastError();
+        free_all();
+        return GBNTT_ERR_ALLOC;
+    }
+    for (int i = 0; i < 2; i++) CK(cudaEventCreateWithFlags(&g.btab_ev[i], cudaEventDisableTiming));
 
     // Twiddle tables and the w_64 constants.
     const size_t tw_words = 3 * 2 * 2 * (size_t)kTwSize;
@@ -274,7 +296,8 @@ static TwTables tables(int dir)
 
 // Forward transform of one operand: limbs -> 3 spectra at spec[pi * stride].
 static int forward(uint64_t *spec, size_t stride, const void *limbs, size_t n, int L, cudaStream_t st,
-                   bool packed = false)
+                   bool packed = false, long long W = 1, const uint32_t *const *limb_tab = nullptr,
+                   const long long *len_tab = nullptr)
 {
     int pl[3];
     const int np = plan_passes(L, pl);
@@ -284,14 +307,17 @@ static int forward(uint64_t *spec, size_t stride, const void *limbs, size_t n, i
     a.limbs = packed ? nullptr : (const uint32_t *)limbs;
     a.limbs64 = packed ? (const uint64_t *)limbs : nullptr;
     a.n_limbs = (long long)n;
+    a.limb_tab = limb_tab;
+    a.len_tab = len_tab;
+    a.log_n_prod = L;
     a.tw = tables(0);
     int log_m = L;
     for (int i = 0; i < np; i++) {
         a.log_m = log_m;
         a.log_s = log_m - pl[i];
-        a.ncols = (long long)1 << (L - pl[i]);
+        a.ncols = W << (L - pl[i]);
         a.twiddle = a.log_s > 0;
-        const double nb8 = 8.0 * (double)((size_t)1 << L);
+        const double nb8 = 8.0 * (double)((size_t)1 << L) * (double)W;
         for (int pi = 0; pi < 3; pi++) {
             rec_begin(st, i == 0 ? 0 : 1, pl[i], i == 0 ? (packed ? 8.0 : 4.0) * (double)n + nb8 : 2.0 * nb8);
             CK(launch_pass_any(pi, pl[i], 0, i == 0 ? (packed ? LD_U64LIMB : LD_U32) : LD_U64, a, st));
@@ -303,7 +329,8 @@ static int forward(uint64_t *spec, size_t stride, const void *limbs, size_t n, i
 }
 
 // Pointwise product of the spectra and inverse transform, in place in specA.
-static int inverse(uint64_t *specA, const uint64_t *specB, size_t stride, int L, cudaStream_t st, bool square)
+static int inverse(uint64_t *specA, const uint64_t *specB, size_t stride, int L, cudaStream_t st, bool square,
+                   long long W = 1)
 {
     int pl[3];
     const int np = plan_passes(L, pl);
@@ -325,10 +352,10 @@ static int inverse(uint64_t *specA, const uint64_t *specB, size_t stride, int L,
     for (int i = np - 1; i >= 0; i--) {
         a.log_m = log_ms[i];
         a.log_s = log_ms[i] - pl[i];
-        a.ncols = (long long)1 << (L - pl[i]);
+        a.ncols = W << (L - pl[i]);
         a.twiddle = a.log_s > 0;
         a.use_scale = (i == 0);
-        const double nb8 = 8.0 * (double)((size_t)1 << L);
+        const double nb8 = 8.0 * (double)((size_t)1 << L) * (double)W;
         const bool first = (i == np - 1);
         for (int pi = 0; pi < 3; pi++) {
             rec_begin(st, first ? 2 : 3, pl[i], first ? (square ? 2.0 : 3.0) * nb8 : 2.0 * nb8);
@@ -439,6 +466,95 @@ static int mul_dev64(uint64_t *d_c, const uint64_t *d_a, size_t na, const uint64
     rc = inverse(specA, square ? specA : specB, g.n_max, L, st, square);
     if (rc) return rc;
     return carry64(d_c, n_out, specA, g.n_max, L, st);
+}
+
+// Batched products: bucket by transform length, then run waves of up to
+// W = min(kMaxBatch, n_max / N) products through the same pass kernels (a
+// wave of W transforms of N points is, for a pass, W N / 2^l columns) and the
+// batched carry kernel. Per-product pointers and lengths travel in device
+// tables, so every launch of a wave has fixed arguments.
+static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const size_t *na,
+                     const uint32_t *const *d_b, const size_t *nb, int count, cudaStream_t st)
+{
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    if (count < 0 || (count > 0 && (!d_c || !d_a || !na || !d_b || !nb))) { set_err("bad batch arguments"); return GBNTT_ERR_ARG; }
+    if (!st) st = g.stream;
+    std::vector<std::pair<int, int>> order;   // (log N, index)
+    order.reserve(count);
+    for (int i = 0; i < count; i++) {
+        if (na[i] == 0 || nb[i] == 0) {
+            if (na[i] + nb[i]) CK(cudaMemsetAsync(d_c[i], 0, (na[i] + nb[i]) * sizeof(uint32_t), st));
+            continue;
+        }
+        const int L = choose_log(na[i], nb[i]);
+        if (L > g.max_log) {
+            set_err("batch product %d needs 2^%d coefficients; engine initialised for 2^%d", i, L, g.max_log);
+            return GBNTT_ERR_SIZE;
+        }
+        order.push_back({L, i});
+    }
+    std::stable_sort(order.begin(), order.end());
+    int slot = 0;
+    size_t pos = 0;
+    while (pos < order.size()) {
+        const int L = order[pos].first;
+        size_t end = pos;
+        while (end < order.size() && order[end].first == L) end++;
+        const long long wmax = std::min<long long>(kMaxBatch, (long long)(g.n_max >> L));
+        for (size_t w0 = pos; w0 < end; w0 += (size_t)wmax) {
+            const long long W = std::min<long long>(wmax, (long long)(end - w0));
+            // tables of this wave in host slot `slot` (wait until its previous upload finished)
+            CK(cudaEventSynchronize(g.btab_ev[slot]));
+            uint64_t *h = g.h_btab + slot * kBtabWords;
+            uint64_t *dtab = g.d_btab + slot * kBtabWords;
+            uint64_t *hA = h, *hLA = h + W, *hB = h + 2 * W, *hLB = h + 3 * W, *hC = h + 4 * W, *hNC = h + 5 * W,
+                     *hTS = h + 6 * W;
+            long long tiles = 0;
+            for (long long k = 0; k < W; k++) {
+                const int i = order[w0 + k].second;
+                hA[k] = (uint64_t)(uintptr_t)d_a[i];
+                hLA[k] = (uint64_t)na[i];
+                hB[k] = (uint64_t)(uintptr_t)d_b[i];
+                hLB[k] = (uint64_t)nb[i];
+                hC[k] = (uint64_t)(uintptr_t)d_c[i];
+                hNC[k] = (uint64_t)(na[i] + nb[i]);
+                hTS[k] = (uint64_t)tiles;
+                tiles += carry_tiles((long long)(na[i] + nb[i]));
+            }
+            hTS[W] = (uint64_t)tiles;
+            CK(cudaMemcpyAsync(dtab, h, (7 * (size_t)W + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+            CK(cudaEventRecord(g.btab_ev[slot], st));
+            uint64_t *specA = g.d_spec, *specB = g.d_spec + 3 * g.n_max;
+            int rc = forward(specA, g.n_max, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab),
+                             (const long long *)(dtab + W));
+            if (rc) return rc;
+            rc = forward(specB, g.n_max, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab + 2 * W),
+                         (const long long *)(dtab + 3 * W));
+            if (rc) return rc;
+            rc = inverse(specA, specB, g.n_max, L, st, false, W);
+            if (rc) return rc;
+            CarryArgs c;
+            memset(&c, 0, sizeof c);
+            for (int pi = 0; pi < 3; pi++) c.res[pi] = specA + pi * g.n_max;
+            c.ticket = g.d_ctl;
+            c.error = g.d_ctl + 1;
+            c.status = g.d_ctl + 2;
+            for (int q = 0; q < 4; q++) c.garner[q] = g.garner[q];
+            c.tile_start = (const long long *)(dtab + 6 * W);
+            c.out_tab = (uint32_t *const *)(dtab + 4 * W);
+            c.nout_tab = (const long long *)(dtab + 5 * W);
+            c.nprod = (int)W;
+            c.log_n_prod = L;
+            CK(cudaMemsetAsync(g.d_ctl, 0, sizeof(unsigned), st));
+            CK(cudaMemsetAsync(g.d_ctl + 2, 0, (size_t)tiles * sizeof(unsigned), st));
+            rec_begin(st, 4, 0, (3.0 * 8.0 * (double)((size_t)1 << L) + 4.0 * (double)(1 << L)) * (double)W);
+            CK(launch_garner_carry_batch(c, tiles, st));
+            rec_end(st);
+            slot ^= 1;
+        }
+        pos = end;
+    }
+    return GBNTT_OK;
 }
 
 static int read_errors(unsigned *flags)
@@ -670,6 +786,13 @@ int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d
     return GBNTT_OK;
 }
 
+int gbntt_fill_operand(uint32_t *d, size_t n, uint64_t seed, void *stream)
+{
+    cudaStream_t st = stream ? (cudaStream_t)stream : (g.ready ? g.stream : (cudaStream_t)0);
+    CK(launch_fill_splitmix(d, (long long)n, seed, st));
+    return GBNTT_OK;
+}
+
 int gbntt_launch_log(int enable)
 {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
@@ -739,6 +862,13 @@ int gbntt_set_coeff_bits(int bits)
 }
 
 int gbntt_coeff_bits(void) { return g.bigint_coeff_bits; }
+
+int gbntt_batch_mul_u32(uint32_t *const *d_c, const uint32_t *const *d_a, const size_t *na,
+                        const uint32_t *const *d_b, const size_t *nb, int count, void *stream)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    return batch_mul(d_c, d_a, na, d_b, nb, count, (cudaStream_t)stream);
+}
 
 int gbntt_sqr_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, void *stream)
 {

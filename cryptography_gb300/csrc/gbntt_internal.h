@@ -27,6 +27,11 @@ struct PassArgs {
     const uint64_t *other[3];   // second spectrum for the fused pointwise product
     const uint32_t *limbs;      // 32-bit limbs for the fused decomposition
     const uint64_t *limbs64;    // 64-bit limbs (one per coefficient) for the packed mode
+    // batched first pass: product b's limbs are limb_tab[b][0 .. len_tab[b]),
+    // its coefficients occupy [b 2^log_n_prod, (b+1) 2^log_n_prod)
+    const uint32_t *const *limb_tab;
+    const long long *len_tab;
+    int log_n_prod;
     long long n_limbs;          // limbs beyond this index read as zero
     TwTables tw;
     uint64_t scale[3];          // Montgomery constant folded into inverse twiddles
@@ -50,6 +55,14 @@ struct CarryArgs {
     unsigned int *error;        // sticky error bits
     uint64_t garner[4];         // Montgomery Garner constants (see engine)
     uint64_t q01_lo, q01_hi;    // q0 * q1 as 128 bits (64-bit coefficient mode)
+    // batched mode: products of 2^log_n_prod coefficients laid end to end in
+    // res[]; global tile t belongs to product b with tile_start[b] <= t <
+    // tile_start[b+1]; product b writes out_tab[b][0 .. nout_tab[b])
+    const long long *tile_start;
+    uint32_t *const *out_tab;
+    const long long *nout_tab;
+    int nprod;
+    int log_n_prod;
 };
 
 enum ErrorBits : unsigned int {
@@ -62,8 +75,10 @@ template <int PI>
 cudaError_t launch_pass_prime(int log_l, int dir, int ld, const PassArgs &a, cudaStream_t st);
 cudaError_t launch_garner_carry(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out);
 cudaError_t launch_garner_carry64(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out);
+cudaError_t launch_garner_carry_batch(const CarryArgs &args, long long grid_tiles, cudaStream_t stream);
 long long carry_tiles(long long n_out);
 long long carry_tiles64(long long n_out);
+cudaError_t launch_fill_splitmix(uint32_t *d, long long n, uint64_t seed, cudaStream_t st);
 cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *b, uint64_t *out, long long n,
                           cudaStream_t stream);
 

@@ -57,6 +57,34 @@ cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *
 // ---------------------------------------------------------------------------
 // Garner + carry
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// Seeded synthetic operands on the device: limb i is the low 32 bits of
+// splitmix64 at seed + (i + 1) * 0x9E3779B97F4A7C15, the top limb gets bit 31
+// (the same limbs as cryptography_gb300/synth.py produces on the host).
+// ---------------------------------------------------------------------------
+__global__ void fill_splitmix_kernel(uint32_t *d, long long n, uint64_t seed)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint64_t z = seed + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        uint32_t v = (uint32_t)z;
+        if (i == n - 1) v |= 0x80000000u;
+        d[i] = v;
+    }
+}
+
+cudaError_t launch_fill_splitmix(uint32_t *d, long long n, uint64_t seed, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    long long grid = (n + 255) / 256;
+    if (grid > 152 * 64) grid = 152 * 64;
+    fill_splitmix_kernel<<<(unsigned)grid, 256, 0, st>>>(d, n, seed);
+    return cudaGetLastError();
+}
+
 constexpr int kCarryThreads = 256;
 constexpr int kCarryPerThread = 8;
 constexpr int kCarryTile = kCarryThreads * kCarryPerThread;   // limbs per tile
@@ -136,17 +164,42 @@ __device__ __forceinline__ void garner_coef(const CarryArgs &a, long long j, uin
     w2 = (uint32_t)hi;
 }
 
-__global__ void __launch_bounds__(kCarryThreads) garner_carry_kernel(CarryArgs a)
+template <bool BATCH>
+__global__ void __launch_bounds__(kCarryThreads) garner_carry_kernel_t(CarryArgs a)
 {
     constexpr int T = kCarryThreads, K = kCarryPerThread, TILE = kCarryTile;
     constexpr int SW = TILE + 2 + (TILE + 2) / 32 + 1;
     __shared__ uint32_t W0[SW], W1[SW], W2[SW];
     __shared__ unsigned s_warp[T / 32];
     __shared__ unsigned s_tile, s_cin;
+    __shared__ long long s_prod;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) s_tile = atomicAdd(a.ticket, 1u);
+    if (tid == 0) {
+        s_tile = atomicAdd(a.ticket, 1u);
+        if (BATCH) {
+            // product owning this global tile (binary search of tile_start)
+            long long lo = 0, hi = a.nprod;   // tile_start[lo] <= t < tile_start[hi]
+            const long long t = s_tile;
+            while (hi - lo > 1) {
+                const long long mid = (lo + hi) >> 1;
+                if (a.tile_start[mid] <= t) lo = mid; else hi = mid;
+            }
+            s_prod = t < a.tile_start[a.nprod] ? lo : -1;
+        }
+    }
     __syncthreads();
-    const long long tile = s_tile;
+    if (BATCH) {
+        // tickets beyond the batch's tiles (the grid is an upper bound) exit
+        if (s_prod < 0) return;
+        const long long b = s_prod;
+        const long long off = b << a.log_n_prod;
+        for (int pi = 0; pi < 3; pi++) a.res[pi] += off;
+        a.out = a.out_tab[b];
+        a.n_out = a.nout_tab[b];
+        a.n_coef = 1LL << a.log_n_prod;
+        a.status += a.tile_start[b];
+    }
+    const long long tile = BATCH ? (long long)s_tile - a.tile_start[s_prod] : (long long)s_tile;
     const long long base = tile * TILE;
     unsigned err = 0;
 
@@ -383,7 +436,14 @@ cudaError_t launch_garner_carry(const CarryArgs &args, cudaStream_t stream, long
     const long long nt = carry_tiles(args.n_out);
     if (ntiles_out) *ntiles_out = nt;
     if (nt == 0) return cudaSuccess;
-    garner_carry_kernel<<<(unsigned)nt, kCarryThreads, 0, stream>>>(args);
+    garner_carry_kernel_t<false><<<(unsigned)nt, kCarryThreads, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_garner_carry_batch(const CarryArgs &args, long long grid_tiles, cudaStream_t stream)
+{
+    if (grid_tiles <= 0) return cudaSuccess;
+    garner_carry_kernel_t<true><<<(unsigned)grid_tiles, kCarryThreads, 0, stream>>>(args);
     return cudaGetLastError();
 }
 

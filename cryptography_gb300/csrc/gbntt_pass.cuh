@@ -95,6 +95,18 @@ __device__ __forceinline__ uint64_t limb64_residue(const PassArgs &a, long long 
     return v >= Prime<PI>::P ? v - Prime<PI>::P : v;
 }
 
+// 32-bit limb of coefficient `addr` (zero beyond the operand): one flat
+// operand, or, in a batch, the operand of product addr >> log_n_prod.
+__device__ __forceinline__ uint64_t limb32_at(const PassArgs &a, long long addr)
+{
+    if (a.limb_tab) {
+        const long long b = addr >> a.log_n_prod;
+        const long long local = addr & ((1LL << a.log_n_prod) - 1);
+        return local < __ldg(a.len_tab + b) ? (uint64_t)__ldg(a.limb_tab[b] + local) : 0ull;
+    }
+    return addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
+}
+
 template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
 __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const uint64_t *w64)
 {
@@ -122,7 +134,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
         for (int it = 0; it < A; it++) {
             const long long addr = base + it * stepg;
             uint64_t v;
-            if (LD == LD_U32) v = addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
+            if (LD == LD_U32) v = limb32_at(a, addr);
             else if (LD == LD_U64LIMB) v = limb64_residue<PI>(a, addr);
             else if (LD == LD_PW) v = mont_mul<PI>(data[addr], a.other[PI][addr]);
             else v = data[addr];
@@ -138,7 +150,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
             uint64_t v = 0;
             if (g < rows_left) {
                 const long long addr = base + e;
-                if (LD == LD_U32) v = addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
+                if (LD == LD_U32) v = limb32_at(a, addr);
                 else if (LD == LD_U64LIMB) v = limb64_residue<PI>(a, addr);
                 else if (LD == LD_PW) v = mont_mul<PI>(data[addr], a.other[PI][addr]);
                 else v = data[addr];

@@ -41,7 +41,7 @@ EXPORTS = (
     "gbntt_mul_u32_host", "gbntt_device_errors", "gbntt_debug_forward", "gbntt_last_error", "gbntt_stream",
     "gbntt_launch_log", "gbntt_launch_records", "gbntt_set_plan", "gbntt_debug_modops",
     "gbntt_mul_u64", "gbntt_sqr_u64", "gbntt_mul_u64_host", "gbntt_set_coeff_bits", "gbntt_coeff_bits",
-    "gbntt_mul_u32_noalloc",
+    "gbntt_mul_u32_noalloc", "gbntt_batch_mul_u32", "gbntt_fill_operand",
 )
 
 _lib = None
@@ -108,6 +108,10 @@ def lib():
     L.gbntt_set_coeff_bits.argtypes = [ctypes.c_int]
     L.gbntt_set_coeff_bits.restype = ctypes.c_int
     L.gbntt_coeff_bits.restype = ctypes.c_int
+    L.gbntt_fill_operand.argtypes = [_vp, _sz, ctypes.c_uint64, _vp]
+    L.gbntt_fill_operand.restype = ctypes.c_int
+    L.gbntt_batch_mul_u32.argtypes = [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]
+    L.gbntt_batch_mul_u32.restype = ctypes.c_int
     L.gbntt_mul_u32_noalloc.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp]
     L.gbntt_mul_u32_noalloc.restype = ctypes.c_int
     L.gbntt_set_plan.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
@@ -211,6 +215,14 @@ def mul64(a, b):
     _check(lib().gbntt_mul_u64_host(c.ctypes.data_as(_u64p), a.ctypes.data_as(_u64p), len(a),
                                     b.ctypes.data_as(_u64p), len(b)))
     return c
+
+
+def batch_mul_device(c_ptrs, a_ptrs, na, b_ptrs, nb, stream=None):
+    """Batched device products: lists of raw device addresses and sizes."""
+    n = len(a_ptrs)
+    P = ctypes.c_uint64 * n
+    S = ctypes.c_size_t * n
+    _check(lib().gbntt_batch_mul_u32(P(*c_ptrs), P(*a_ptrs), S(*na), P(*b_ptrs), S(*nb), n, stream))
 
 
 def set_coeff_bits(bits):

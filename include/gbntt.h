@@ -126,6 +126,16 @@ int gbntt_mul_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t 
                   void *stream);
 int gbntt_sqr_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, void *stream);
 
+/* Batched products (no reference counterpart; the reference runs one
+ * product at a time): d_c[i][0 .. na[i]+nb[i]) = d_a[i] * d_b[i] for
+ * i < count. The arrays are host arrays of device pointers and sizes. The
+ * engine groups the products by transform length and runs each group in
+ * waves that fit its workspace, one launch per pass and prime per wave.
+ * Stream-ordered; results are bit-identical to gbntt_mul_u32 per product.
+ * Outputs must not overlap inputs or each other. */
+int gbntt_batch_mul_u32(uint32_t *const *d_c, const uint32_t *const *d_a, const size_t *na,
+                        const uint32_t *const *d_b, const size_t *nb, int count, void *stream);
+
 /* Packed mode: one 64-bit limb per coefficient (the reference engine's own
  * granularity, ntt/lib/arith/bigint.h:30-43). Operands and product are
  * 64-bit limb arrays (na, nb counted in 64-bit limbs; d_c gets na + nb
@@ -161,6 +171,11 @@ int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log
  * 2 and 5). Stream-ordered. */
 int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t n,
                        void *stream);
+
+/* Seeded synthetic operand on the device (benchmarks): d[i] = low 32 bits of
+ * splitmix64 at seed + (i + 1) * 0x9E3779B97F4A7C15, bit 31 of d[n-1] set.
+ * Stream-ordered. */
+int gbntt_fill_operand(uint32_t *d, size_t n, uint64_t seed, void *stream);
 
 /* Per-launch timing for roofline reports. gbntt_launch_log(1) makes every
  * following kernel launch record CUDA events (kind: 0 first forward pass,
