@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--batch-pairs", type=int, default=4096)
     ap.add_argument("--batch-reps", type=int, default=2)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-products leg")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
+    ap.add_argument("--serve-requests", type=int, default=10000)
+    ap.add_argument("--serve-saturation", type=int, default=3000)
+    ap.add_argument("--serve-slots", type=int, default=4)
     return ap.parse_args()
 
 
@@ -265,6 +269,88 @@ def run_batched_leg(g, cudart, args, stream):
     return out
 
 
+def run_serving_leg(g, cudart, args, stream):
+    """Poisson arrivals of multiply requests (sizes log-uniform 2^8..2^24
+    limbs per operand, seeded) against the continuous-batching server, at
+    0.7 x the serial capacity of the plain path; then a saturation run."""
+    L = g.lib()
+    rng = np.random.default_rng(5150)
+    nreq = args.serve_requests
+    warm = 200
+    na = np.floor(2.0 ** rng.uniform(8, 24, nreq + warm + 300)).astype(np.int64)
+    nb = np.floor(2.0 ** rng.uniform(8, 24, nreq + warm + 300)).astype(np.int64)
+    pool = cudart.DeviceBuffer(4 << 25)
+    L.gbntt_fill_operand(pool.ptr, 1 << 25, 99, None)
+    arena_limbs = 1 << 32
+    arena = cudart.DeviceBuffer(4 * arena_limbs)
+    cudart.synchronize()
+    a_ptr = pool.ptr
+    b_ptr = pool.ptr + 4 * (1 << 24)
+
+    # serial capacity of the plain path on the same size mix
+    t_plain = []
+    for i in range(nreq + warm, nreq + warm + 300):
+        t0 = time.perf_counter()
+        g.mul_device(arena.ptr, a_ptr, int(na[i]), b_ptr, int(nb[i]), None)
+        cudart.stream_sync(stream)
+        t_plain.append(time.perf_counter() - t0)
+    t_plain = float(np.mean(t_plain[20:]))
+    cap_plain = 1.0 / t_plain
+
+    srv = g.Server(slots=args.serve_slots, slot_log=26)
+    try:
+        def run(indices, rate):
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, len(indices))) if rate else np.zeros(len(indices))
+            head, inflight, tickets = 0, [], []
+            start = time.perf_counter()
+            for k, i in enumerate(indices):
+                n_out = int(na[i] + nb[i])
+                if head + n_out > arena_limbs:
+                    head = 0
+                # wait for in-flight requests whose output overlaps [head, head + n_out)
+                while inflight and inflight[0][1] < head + n_out and inflight[0][1] + inflight[0][2] > head:
+                    srv.wait(inflight.pop(0)[0], 120.0)
+                now = time.perf_counter() - start
+                if arrivals[k] > now:
+                    while time.perf_counter() - start < arrivals[k]:
+                        pass
+                t = srv.submit(arena.ptr + 4 * head, a_ptr, int(na[i]), b_ptr, int(nb[i]))
+                tickets.append(t)
+                inflight.append((t, head, n_out))
+                head += n_out
+            for t in tickets:
+                srv.wait(t, 300.0)
+            wall = time.perf_counter() - start
+            lat = np.array([srv.query(t)[1] for t in tickets]) / 1e3
+            return wall, lat
+
+        run(list(range(nreq, nreq + warm)), 0.7 * cap_plain)
+        rate = 0.7 * cap_plain
+        wall, lat = run(list(range(nreq)), rate)
+        st = srv.stats()
+        sat_n = min(nreq, args.serve_saturation)
+        sat_wall, sat_lat = run(list(range(sat_n)), None)
+        st2 = srv.stats()
+    finally:
+        srv.stop()
+    pool.free()
+    arena.free()
+    return {"requests": nreq, "sizes": "log2(n) uniform in [8, 24] per operand, seed 5150", "warmup_requests": warm,
+            "offered_rate_per_s": rate, "served_products_per_s": nreq / wall,
+            "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
+            "latency_ms_mean": float(lat.mean()),
+            "serial_plain_products_per_s": cap_plain, "serial_plain_ms_per_product": t_plain * 1e3,
+            "saturation": {"requests": sat_n, "products_per_s": sat_n / sat_wall,
+                           "vs_serial_plain": (sat_n / sat_wall) / cap_plain,
+                           "latency_ms_p50": float(np.percentile(sat_lat, 50)),
+                           "latency_ms_p99": float(np.percentile(sat_lat, 99))},
+            "slots": args.serve_slots, "slot_coefficients": 1 << 26,
+            "waves": st2["waves"], "products_per_wave": st2["wave_products"] / max(1, st2["waves"]),
+            "device_error_flags": st2["device_errors"],
+            "latency": "submit -> completion observed by the server thread (host clock)",
+            "load": "0.7 x serial capacity of the plain path (gbntt_mul_u32 + sync per request)"}
+
+
 def run_reference(args, dist):
     if dist.rank != 0:
         return 0
@@ -359,6 +445,11 @@ def run_gpu(args, dist):
         batched = run_batched_leg(g, cudart, args, stream)
         flags |= batched["device_error_flags"]
 
+    serving = None
+    if not args.no_serving and dist.rank == 0:
+        serving = run_serving_leg(g, cudart, args, stream)
+        flags |= serving["device_error_flags"]
+
     # per-launch breakdown of one multiply (separate, instrumented run)
     g.launch_log(True)
     step()
@@ -445,6 +536,7 @@ def run_gpu(args, dist):
                                        "pointwise product and Garner+carry)"},
         "packed_64bit_coefficients": packed,
         "batched": batched,
+        "serving": serving,
         "launch_breakdown": by_kind,
         "gpu_launches": launches_per_step * args.steps,
         "device_error_flags": flags,

@@ -9,6 +9,7 @@ limb API. There is no CPU fallback: if the library is missing or no CUDA
 device is present, calls fail with an exception.
 """
 from .engine import (  # noqa: F401
+    Server,
     BigInt,
     EngineError,
     GBNTT_ERR_ALLOC,

@@ -12,6 +12,11 @@
 #include <mutex>
 #include <vector>
 #include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -469,10 +474,82 @@ static int mul_dev64(uint64_t *d_c, const uint64_t *d_a, size_t na, const uint64
 }
 
 // Batched products: bucket by transform length, then run waves of up to
-// W = min(kMaxBatch, n_max / N) products through the same pass kernels (a
+// W = min(kMaxBatch, cap / N) products through the same pass kernels (a
 // wave of W transforms of N points is, for a pass, W N / 2^l columns) and the
 // batched carry kernel. Per-product pointers and lengths travel in device
-// tables, so every launch of a wave has fixed arguments.
+// tables, so every launch of a wave has fixed arguments. A context is one
+// workspace (the engine's, or a slice of it owned by a serving slot).
+struct BatchCtx {
+    uint64_t *spec;              // 6 x cap words: A (3 x cap) then B (3 x cap)
+    size_t cap;                  // coefficients per prime per operand
+    unsigned *ctl;               // [0] ticket, [1] error, [2..] carry tile status
+    uint64_t *d_btab, *h_btab;   // two table slots (device, pinned host)
+    cudaEvent_t *btab_ev;        // two events guarding the host slots
+    int *slot;
+};
+
+struct BatchItem {
+    uint32_t *c;
+    const uint32_t *a, *b;
+    size_t na, nb;
+};
+
+// One wave of W products, all of transform length 2^L, on stream st.
+static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, cudaStream_t st)
+{
+    const int slot = *x.slot;
+    CK(cudaEventSynchronize(x.btab_ev[slot]));
+    uint64_t *h = x.h_btab + slot * kBtabWords;
+    uint64_t *dtab = x.d_btab + slot * kBtabWords;
+    uint64_t *hA = h, *hLA = h + W, *hB = h + 2 * W, *hLB = h + 3 * W, *hC = h + 4 * W, *hNC = h + 5 * W,
+             *hTS = h + 6 * W;
+    long long tiles = 0;
+    for (long long k = 0; k < W; k++) {
+        const BatchItem &it = items[k];
+        hA[k] = (uint64_t)(uintptr_t)it.a;
+        hLA[k] = (uint64_t)it.na;
+        hB[k] = (uint64_t)(uintptr_t)it.b;
+        hLB[k] = (uint64_t)it.nb;
+        hC[k] = (uint64_t)(uintptr_t)it.c;
+        hNC[k] = (uint64_t)(it.na + it.nb);
+        hTS[k] = (uint64_t)tiles;
+        tiles += carry_tiles((long long)(it.na + it.nb));
+    }
+    hTS[W] = (uint64_t)tiles;
+    CK(cudaMemcpyAsync(dtab, h, (7 * (size_t)W + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(x.btab_ev[slot], st));
+    *x.slot = slot ^ 1;
+    uint64_t *specA = x.spec, *specB = x.spec + 3 * x.cap;
+    int rc = forward(specA, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab),
+                     (const long long *)(dtab + W));
+    if (rc) return rc;
+    rc = forward(specB, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab + 2 * W),
+                 (const long long *)(dtab + 3 * W));
+    if (rc) return rc;
+    rc = inverse(specA, specB, x.cap, L, st, false, W);
+    if (rc) return rc;
+    CarryArgs c;
+    memset(&c, 0, sizeof c);
+    for (int pi = 0; pi < 3; pi++) c.res[pi] = specA + pi * x.cap;
+    c.ticket = x.ctl;
+    c.error = x.ctl + 1;
+    c.status = x.ctl + 2;
+    for (int q = 0; q < 4; q++) c.garner[q] = g.garner[q];
+    c.tile_start = (const long long *)(dtab + 6 * W);
+    c.out_tab = (uint32_t *const *)(dtab + 4 * W);
+    c.nout_tab = (const long long *)(dtab + 5 * W);
+    c.nprod = (int)W;
+    c.log_n_prod = L;
+    CK(cudaMemsetAsync(x.ctl, 0, sizeof(unsigned), st));
+    CK(cudaMemsetAsync(x.ctl + 2, 0, (size_t)tiles * sizeof(unsigned), st));
+    rec_begin(st, 4, 0, (3.0 * 8.0 * (double)((size_t)1 << L) + 4.0 * (double)(1 << L)) * (double)W);
+    CK(launch_garner_carry_batch(c, tiles, st));
+    rec_end(st);
+    return GBNTT_OK;
+}
+
+static int g_batch_slot = 0;
+
 static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const size_t *na,
                      const uint32_t *const *d_b, const size_t *nb, int count, cudaStream_t st)
 {
@@ -494,7 +571,8 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
         order.push_back({L, i});
     }
     std::stable_sort(order.begin(), order.end());
-    int slot = 0;
+    BatchCtx x{g.d_spec, g.n_max, g.d_ctl, g.d_btab, g.h_btab, g.btab_ev, &g_batch_slot};
+    std::vector<BatchItem> items;
     size_t pos = 0;
     while (pos < order.size()) {
         const int L = order[pos].first;
@@ -503,59 +581,146 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
         const long long wmax = std::min<long long>(kMaxBatch, (long long)(g.n_max >> L));
         for (size_t w0 = pos; w0 < end; w0 += (size_t)wmax) {
             const long long W = std::min<long long>(wmax, (long long)(end - w0));
-            // tables of this wave in host slot `slot` (wait until its previous upload finished)
-            CK(cudaEventSynchronize(g.btab_ev[slot]));
-            uint64_t *h = g.h_btab + slot * kBtabWords;
-            uint64_t *dtab = g.d_btab + slot * kBtabWords;
-            uint64_t *hA = h, *hLA = h + W, *hB = h + 2 * W, *hLB = h + 3 * W, *hC = h + 4 * W, *hNC = h + 5 * W,
-                     *hTS = h + 6 * W;
-            long long tiles = 0;
+            items.clear();
             for (long long k = 0; k < W; k++) {
                 const int i = order[w0 + k].second;
-                hA[k] = (uint64_t)(uintptr_t)d_a[i];
-                hLA[k] = (uint64_t)na[i];
-                hB[k] = (uint64_t)(uintptr_t)d_b[i];
-                hLB[k] = (uint64_t)nb[i];
-                hC[k] = (uint64_t)(uintptr_t)d_c[i];
-                hNC[k] = (uint64_t)(na[i] + nb[i]);
-                hTS[k] = (uint64_t)tiles;
-                tiles += carry_tiles((long long)(na[i] + nb[i]));
+                items.push_back({d_c[i], d_a[i], d_b[i], na[i], nb[i]});
             }
-            hTS[W] = (uint64_t)tiles;
-            CK(cudaMemcpyAsync(dtab, h, (7 * (size_t)W + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-            CK(cudaEventRecord(g.btab_ev[slot], st));
-            uint64_t *specA = g.d_spec, *specB = g.d_spec + 3 * g.n_max;
-            int rc = forward(specA, g.n_max, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab),
-                             (const long long *)(dtab + W));
+            const int rc = batch_wave(x, items.data(), W, L, st);
             if (rc) return rc;
-            rc = forward(specB, g.n_max, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab + 2 * W),
-                         (const long long *)(dtab + 3 * W));
-            if (rc) return rc;
-            rc = inverse(specA, specB, g.n_max, L, st, false, W);
-            if (rc) return rc;
-            CarryArgs c;
-            memset(&c, 0, sizeof c);
-            for (int pi = 0; pi < 3; pi++) c.res[pi] = specA + pi * g.n_max;
-            c.ticket = g.d_ctl;
-            c.error = g.d_ctl + 1;
-            c.status = g.d_ctl + 2;
-            for (int q = 0; q < 4; q++) c.garner[q] = g.garner[q];
-            c.tile_start = (const long long *)(dtab + 6 * W);
-            c.out_tab = (uint32_t *const *)(dtab + 4 * W);
-            c.nout_tab = (const long long *)(dtab + 5 * W);
-            c.nprod = (int)W;
-            c.log_n_prod = L;
-            CK(cudaMemsetAsync(g.d_ctl, 0, sizeof(unsigned), st));
-            CK(cudaMemsetAsync(g.d_ctl + 2, 0, (size_t)tiles * sizeof(unsigned), st));
-            rec_begin(st, 4, 0, (3.0 * 8.0 * (double)((size_t)1 << L) + 4.0 * (double)(1 << L)) * (double)W);
-            CK(launch_garner_carry_batch(c, tiles, st));
-            rec_end(st);
-            slot ^= 1;
         }
         pos = end;
     }
     return GBNTT_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Serving loop (continuous batching). A server thread owns K workspace
+// slots, each with its own stream, carry control words and batch tables.
+// Requests (device pointers) queue in arrival order; whenever a slot is
+// free, the server takes the oldest pending request's transform length and
+// admits, in arrival order, every pending request of that length whose
+// spectra still fit the slot (the HBM-footprint admission: 48 N bytes per
+// product against the slot's 48 cap bytes), and launches them as one wave on
+// the slot's stream. Waves in different slots overlap on the device;
+// requests that arrive meanwhile are admitted as slots free up. A request is
+// done when the server observes its wave's completion event; latency is
+// submit -> that observation. Results are bit-identical to gbntt_mul_u32.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct SrvRequest {
+    BatchItem item;
+    int L = 0;
+    int state = 0;   // 0 pending, 1 running, 2 done
+    std::chrono::steady_clock::time_point t_submit, t_done;
+};
+
+struct SrvSlot {
+    BatchCtx ctx;
+    uint64_t *spec = nullptr;
+    unsigned *ctl = nullptr;
+    uint64_t *d_btab = nullptr, *h_btab = nullptr;
+    cudaEvent_t btab_ev[2] = {nullptr, nullptr};
+    int tab_slot = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    bool busy = false;
+    std::vector<uint64_t> ids;
+};
+
+struct Server {
+    std::thread th;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<uint64_t> pending;
+    std::deque<SrvRequest> reqs;       // indexed by ticket (stable references)
+    std::vector<SrvSlot> slots;
+    size_t cap = 0;
+    int slot_log = 0;
+    bool stop = false;
+    std::atomic<uint64_t> completed{0}, waves{0}, wave_products{0};
+    int error = 0;
+};
+
+Server *g_srv = nullptr;
+
+void server_loop(Server *S)
+{
+    std::vector<BatchItem> items;
+    std::vector<uint64_t> ids;
+    for (;;) {
+        bool did = false;
+        for (auto &sl : S->slots) {
+            if (sl.busy && cudaEventQuery(sl.done) == cudaSuccess) {
+                const auto now = std::chrono::steady_clock::now();
+                std::lock_guard<std::mutex> lk(S->mu);
+                for (uint64_t id : sl.ids) { S->reqs[id].state = 2; S->reqs[id].t_done = now; }
+                S->completed += sl.ids.size();
+                sl.ids.clear();
+                sl.busy = false;
+                did = true;
+                S->cv.notify_all();
+            }
+        }
+        for (auto &sl : S->slots) {
+            if (sl.busy) continue;
+            ids.clear();
+            int L = 0;
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                if (S->pending.empty()) break;
+                L = S->reqs[S->pending.front()].L;
+                const size_t wmax = std::min<size_t>(kMaxBatch, S->cap >> L);
+                std::deque<uint64_t> rest;
+                for (uint64_t id : S->pending) {
+                    if (ids.size() < wmax && S->reqs[id].L == L) { ids.push_back(id); S->reqs[id].state = 1; }
+                    else rest.push_back(id);
+                }
+                S->pending.swap(rest);
+                items.clear();
+                for (uint64_t id : ids) items.push_back(S->reqs[id].item);
+            }
+            const int rc = batch_wave(sl.ctx, items.data(), (long long)items.size(), L, sl.stream);
+            if (rc) S->error = rc;
+            cudaEventRecord(sl.done, sl.stream);
+            sl.ids = ids;
+            sl.busy = true;
+            S->waves++;
+            S->wave_products += ids.size();
+            did = true;
+        }
+        if (!did) {
+            std::unique_lock<std::mutex> lk(S->mu);
+            bool any_busy = false;
+            for (auto &sl : S->slots) any_busy |= sl.busy;
+            if (S->stop && S->pending.empty() && !any_busy) return;
+            if (any_busy) {
+                lk.unlock();
+                std::this_thread::sleep_for(std::chrono::microseconds(5));
+            } else {
+                S->cv.wait_for(lk, std::chrono::milliseconds(2));
+            }
+        }
+    }
+}
+
+void server_free(Server *S)
+{
+    for (auto &sl : S->slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        cudaFree(sl.spec);
+        cudaFree(sl.ctl);
+        cudaFree(sl.d_btab);
+        if (sl.h_btab) cudaFreeHost(sl.h_btab);
+        for (int i = 0; i < 2; i++) if (sl.btab_ev[i]) cudaEventDestroy(sl.btab_ev[i]);
+        if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
+    delete S;
+}
+
+}  // namespace
 
 static int read_errors(unsigned *flags)
 {
@@ -868,6 +1033,126 @@ int gbntt_batch_mul_u32(uint32_t *const *d_c, const uint32_t *const *d_a, const 
 {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     return batch_mul(d_c, d_a, na, d_b, nb, count, (cudaStream_t)stream);
+}
+
+int gbntt_server_start(int slots, int slot_log)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    if (g_srv) { set_err("server already running"); return GBNTT_ERR_ARG; }
+    if (slots < 1 || slots > 16 || slot_log < kMinLog || slot_log > g.max_log) {
+        set_err("gbntt_server_start: 1..16 slots of 2^%d..2^%d coefficients", kMinLog, g.max_log);
+        return GBNTT_ERR_ARG;
+    }
+    Server *S = new Server();
+    S->cap = (size_t)1 << slot_log;
+    S->slot_log = slot_log;
+    S->slots.resize(slots);
+    const size_t nstat = (size_t)carry_tiles((long long)S->cap + 1) + 64;
+    for (auto &sl : S->slots) {
+        bool ok = cudaMalloc(&sl.spec, 6 * S->cap * sizeof(uint64_t)) == cudaSuccess &&
+                  cudaMalloc(&sl.ctl, (2 + nstat) * sizeof(unsigned)) == cudaSuccess &&
+                  cudaMalloc(&sl.d_btab, 2 * kBtabWords * sizeof(uint64_t)) == cudaSuccess &&
+                  cudaMallocHost(&sl.h_btab, 2 * kBtabWords * sizeof(uint64_t)) == cudaSuccess &&
+                  cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&sl.btab_ev[0], cudaEventDisableTiming) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&sl.btab_ev[1], cudaEventDisableTiming) == cudaSuccess &&
+                  cudaMemset(sl.ctl, 0, (2 + nstat) * sizeof(unsigned)) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            set_err("gbntt_server_start: allocation of %d slots of 2^%d coefficients failed", slots, slot_log);
+            server_free(S);
+            return GBNTT_ERR_ALLOC;
+        }
+        sl.ctx = BatchCtx{sl.spec, S->cap, sl.ctl, sl.d_btab, sl.h_btab, sl.btab_ev, &sl.tab_slot};
+    }
+    g_srv = S;
+    S->th = std::thread(server_loop, S);
+    return GBNTT_OK;
+}
+
+int gbntt_server_submit(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb,
+                        uint64_t *ticket)
+{
+    Server *S = g_srv;
+    if (!S) { set_err("server not running"); return GBNTT_ERR_NOT_INIT; }
+    if (!d_c || !d_a || !d_b || !ticket || na == 0 || nb == 0) { set_err("bad request"); return GBNTT_ERR_ARG; }
+    const int L = choose_log(na, nb);
+    if (L > S->slot_log) { set_err("request needs 2^%d coefficients; slots hold 2^%d", L, S->slot_log); return GBNTT_ERR_SIZE; }
+    std::lock_guard<std::mutex> lk(S->mu);
+    const uint64_t id = S->reqs.size();
+    S->reqs.emplace_back();
+    SrvRequest &r = S->reqs.back();
+    r.item = BatchItem{d_c, d_a, d_b, na, nb};
+    r.L = L;
+    r.t_submit = std::chrono::steady_clock::now();
+    S->pending.push_back(id);
+    *ticket = id;
+    S->cv.notify_all();
+    return GBNTT_OK;
+}
+
+int gbntt_server_query(uint64_t ticket, int *state, double *latency_us)
+{
+    Server *S = g_srv;
+    if (!S) { set_err("server not running"); return GBNTT_ERR_NOT_INIT; }
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (ticket >= S->reqs.size()) { set_err("unknown ticket"); return GBNTT_ERR_ARG; }
+    const SrvRequest &r = S->reqs[ticket];
+    if (state) *state = r.state;
+    if (latency_us)
+        *latency_us = r.state == 2 ? std::chrono::duration<double, std::micro>(r.t_done - r.t_submit).count() : -1.0;
+    return S->error ? S->error : GBNTT_OK;
+}
+
+int gbntt_server_wait(uint64_t ticket, double timeout_s)
+{
+    Server *S = g_srv;
+    if (!S) { set_err("server not running"); return GBNTT_ERR_NOT_INIT; }
+    std::unique_lock<std::mutex> lk(S->mu);
+    if (ticket >= S->reqs.size()) { set_err("unknown ticket"); return GBNTT_ERR_ARG; }
+    const bool ok = S->cv.wait_for(lk, std::chrono::duration<double>(timeout_s),
+                                   [&] { return S->reqs[ticket].state == 2 || S->error; });
+    if (S->error) return S->error;
+    if (!ok) { set_err("gbntt_server_wait: timeout"); return GBNTT_ERR_ARG; }
+    return GBNTT_OK;
+}
+
+int gbntt_server_stats(uint64_t *completed, uint64_t *waves, uint64_t *wave_products, unsigned *device_errors)
+{
+    Server *S = g_srv;
+    if (!S) { set_err("server not running"); return GBNTT_ERR_NOT_INIT; }
+    if (completed) *completed = S->completed;
+    if (waves) *waves = S->waves;
+    if (wave_products) *wave_products = S->wave_products;
+    if (device_errors) {
+        unsigned acc = 0;
+        for (auto &sl : S->slots) {
+            unsigned v = 0;
+            CK(cudaMemcpy(&v, sl.ctl + 1, sizeof v, cudaMemcpyDeviceToHost));   // synchronous: finished waves only
+            acc |= v;
+        }
+        *device_errors = acc;
+    }
+    return GBNTT_OK;
+}
+
+int gbntt_server_stop(void)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    Server *S = g_srv;
+    if (!S) return GBNTT_OK;
+    {
+        std::lock_guard<std::mutex> l2(S->mu);
+        S->stop = true;
+        S->cv.notify_all();
+    }
+    S->th.join();
+    const int err = S->error;
+    g_srv = nullptr;
+    server_free(S);
+    return err;
 }
 
 int gbntt_sqr_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, void *stream)

@@ -42,6 +42,8 @@ EXPORTS = (
     "gbntt_launch_log", "gbntt_launch_records", "gbntt_set_plan", "gbntt_debug_modops",
     "gbntt_mul_u64", "gbntt_sqr_u64", "gbntt_mul_u64_host", "gbntt_set_coeff_bits", "gbntt_coeff_bits",
     "gbntt_mul_u32_noalloc", "gbntt_batch_mul_u32", "gbntt_fill_operand",
+    "gbntt_server_start", "gbntt_server_submit", "gbntt_server_query", "gbntt_server_wait", "gbntt_server_stats",
+    "gbntt_server_stop",
 )
 
 _lib = None
@@ -108,6 +110,17 @@ def lib():
     L.gbntt_set_coeff_bits.argtypes = [ctypes.c_int]
     L.gbntt_set_coeff_bits.restype = ctypes.c_int
     L.gbntt_coeff_bits.restype = ctypes.c_int
+    L.gbntt_server_start.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.gbntt_server_start.restype = ctypes.c_int
+    L.gbntt_server_submit.argtypes = [_vp, _vp, _sz, _vp, _sz, ctypes.POINTER(ctypes.c_uint64)]
+    L.gbntt_server_submit.restype = ctypes.c_int
+    L.gbntt_server_query.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+    L.gbntt_server_query.restype = ctypes.c_int
+    L.gbntt_server_wait.argtypes = [ctypes.c_uint64, ctypes.c_double]
+    L.gbntt_server_wait.restype = ctypes.c_int
+    L.gbntt_server_stats.argtypes = [ctypes.POINTER(ctypes.c_uint64)] * 3 + [ctypes.POINTER(ctypes.c_uint)]
+    L.gbntt_server_stats.restype = ctypes.c_int
+    L.gbntt_server_stop.restype = ctypes.c_int
     L.gbntt_fill_operand.argtypes = [_vp, _sz, ctypes.c_uint64, _vp]
     L.gbntt_fill_operand.restype = ctypes.c_int
     L.gbntt_batch_mul_u32.argtypes = [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]
@@ -223,6 +236,35 @@ def batch_mul_device(c_ptrs, a_ptrs, na, b_ptrs, nb, stream=None):
     P = ctypes.c_uint64 * n
     S = ctypes.c_size_t * n
     _check(lib().gbntt_batch_mul_u32(P(*c_ptrs), P(*a_ptrs), S(*na), P(*b_ptrs), S(*nb), n, stream))
+
+
+class Server:
+    """Continuous-batching request loop of the engine (see gbntt.h)."""
+
+    def __init__(self, slots=4, slot_log=26):
+        _check(lib().gbntt_server_start(int(slots), int(slot_log)))
+
+    def submit(self, c_ptr, a_ptr, na, b_ptr, nb):
+        t = ctypes.c_uint64(0)
+        _check(lib().gbntt_server_submit(c_ptr, a_ptr, na, b_ptr, nb, ctypes.byref(t)))
+        return t.value
+
+    def query(self, ticket):
+        st, lat = ctypes.c_int(0), ctypes.c_double(0)
+        _check(lib().gbntt_server_query(ticket, ctypes.byref(st), ctypes.byref(lat)))
+        return st.value, lat.value
+
+    def wait(self, ticket, timeout_s=60.0):
+        _check(lib().gbntt_server_wait(ticket, timeout_s))
+
+    def stats(self):
+        v = [ctypes.c_uint64(0) for _ in range(3)]
+        e = ctypes.c_uint(0)
+        _check(lib().gbntt_server_stats(*[ctypes.byref(x) for x in v], ctypes.byref(e)))
+        return {"completed": v[0].value, "waves": v[1].value, "wave_products": v[2].value, "device_errors": e.value}
+
+    def stop(self):
+        _check(lib().gbntt_server_stop())
 
 
 def set_coeff_bits(bits):

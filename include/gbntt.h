@@ -136,6 +136,27 @@ int gbntt_sqr_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, void *stream);
 int gbntt_batch_mul_u32(uint32_t *const *d_c, const uint32_t *const *d_a, const size_t *na,
                         const uint32_t *const *d_b, const size_t *nb, int count, void *stream);
 
+/* Serving loop (continuous batching; no reference counterpart). Starts a
+ * server thread owning `slots` workspaces of 2^slot_log coefficients (48 x
+ * 2^slot_log bytes of device memory each, on their own streams). Requests
+ * are device-pointer products queued in arrival order; whenever a slot is
+ * free the server admits, in arrival order, the pending requests of the
+ * oldest request's transform length that fit the slot and runs them as one
+ * wave, so requests arriving while others run are admitted as slots free
+ * up and their work overlaps on the device. Results are bit-identical to
+ * gbntt_mul_u32. Latency = submit -> completion observed by the server.
+ * The engine must be initialised; the ordinary entry points stay usable. */
+int gbntt_server_start(int slots, int slot_log);
+int gbntt_server_submit(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb,
+                        uint64_t *ticket);
+/* state: 0 pending, 1 running, 2 done; latency_us < 0 until done. */
+int gbntt_server_query(uint64_t ticket, int *state, double *latency_us);
+int gbntt_server_wait(uint64_t ticket, double timeout_s);
+/* device_errors: OR of the slots' device check flags (see gbntt_device_errors). */
+int gbntt_server_stats(uint64_t *completed, uint64_t *waves, uint64_t *wave_products, unsigned *device_errors);
+/* Drains the queue, joins the thread and frees the slots. */
+int gbntt_server_stop(void);
+
 /* Packed mode: one 64-bit limb per coefficient (the reference engine's own
  * granularity, ntt/lib/arith/bigint.h:30-43). Operands and product are
  * 64-bit limb arrays (na, nb counted in 64-bit limbs; d_c gets na + nb
