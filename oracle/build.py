@@ -62,6 +62,38 @@ def build_ref(force=False):
     return REF_SO
 
 
+REF_E = os.path.join(REF_DIR, "compute_e_ref")
+
+
+def build_ref_compute_e(force=False):
+    """The reference's host compute_e (main.c with -DCOMPUTE_E_HOST, the
+    arith layer, binary splitting) linked with ref_e_gmp_shim.c, compiled by
+    path from the reference checkout. None when the checkout is absent or
+    libgmp.so.10 cannot be linked."""
+    if not reference_available():
+        return None
+    ce = os.path.join(REFERENCE_ROOT, "ntt", "app", "compute_e")
+    lib = os.path.join(REFERENCE_ROOT, "ntt", "lib")
+    arith = os.path.join(lib, "arith")
+    srcs = [os.path.join(ce, f) for f in ("main.c", "binary_split.c", "mem_pool.c")] + \
+           [os.path.join(arith, f) for f in ("bigint.c", "multiply.c", "newton.c", "base_convert.c")] + \
+           [os.path.join(HERE, "ref_e_gmp_shim.c")]
+    if not (force or _stale(REF_E, srcs + [__file__])):
+        return REF_E
+    os.makedirs(REF_DIR, exist_ok=True)
+    objs = []
+    for src in srcs:
+        obj = os.path.join(REF_DIR, "e_" + os.path.basename(src)[:-2] + ".o")
+        subprocess.check_call(["gcc", "-O3", "-fopenmp", "-DCOMPUTE_E_HOST=1", "-I", lib, "-I", arith, "-I", ce,
+                               "-c", src, "-o", obj])
+        objs.append(obj)
+    tmp = REF_E + ".tmp"
+    subprocess.check_call(["gcc"] + objs + ["-lm", "-fopenmp", "-l:libgmp.so.10", "-o", tmp])
+    os.replace(tmp, REF_E)
+    return REF_E
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     print(build_ref(force=True))
+    print(build_ref_compute_e(force=True))
