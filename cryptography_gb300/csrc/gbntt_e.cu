@@ -1,0 +1,1183 @@
+// gbntt_e.cu — e to D decimal digits, every large product on the GPU engine.
+//
+// The reference application (ntt/app/compute_e/main.c:150-345) computes
+//   K   = split_terms_needed(D + 20)                (binary_split.c:96-108)
+//   P,B = binary_split(1, K + 1)                    (binary_split.c:26-86)
+//   R   = floor((B + P) * 10^(D+20) / B)            (main.c:262-296, newton.c)
+// and prints the first D decimal digits of R as "2.718..." (main.c:340-345,
+// base_convert.c). Since floor(floor(x) / 10^21) = floor(x / 10^21), those
+// digits are exactly the decimal digits of Q = floor((B + P) 10^(D-1) / B),
+// which is what this file computes, with the reference's K.
+//
+// GB300 design. All integers stay in HBM as 32-bit limbs; the host only
+// plans, launches and reads lengths and flags.
+//  * Product tree: leaf groups of up to 64 consecutive terms are folded by
+//    one thread each (bs_leaf_kernel: P = P k + 1, B = B k); then the tree
+//    is merged level by level, each level's 2 m products (B_L B_R and
+//    P_L B_R) going to the engine as ONE batch (gbntt_batch_mul_u32: waves
+//    of equal-length transforms), P_L B_R + P_R as one batched add kernel.
+//    Any tree shape gives the same P and B: P / B = sum_{k=a}^{b-1}
+//    (a-1)!/k! with B = (b-1)!/(a-1)!.
+//  * 10^(D-1) = 5^(D-1) 2^(D-1): 5^(D-1) by GPU squarings; the power of two
+//    is a bit shift (extract_kernel).
+//  * Division (reference newton.c): reciprocal Y = floor(beta^2k / T) of the
+//    normalised divisor by Newton iteration with precision doubling (two
+//    GPU products per step), made exact by a bounded correction; quotient
+//    q' = top bits of x Y is exact or one below, fixed by a conditional
+//    subtract (add/subtract kernel with decoupled look-back carry).
+//  * Decimal conversion (reference base_convert.c, divide and conquer on
+//    powers of ten): pieces are split by d_j = 10^(9 2^j) level by level; a
+//    level's pieces are divided together (batched products against one
+//    reciprocal), leading pieces known to be zero are skipped, and pieces of
+//    576 digits are written out by one thread each (dec_leaf_kernel).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+#include <algorithm>
+#include <chrono>
+#include <vector>
+
+#include "gbntt.h"
+#include "gbntt_bn.h"
+#include "gbntt_carry.cuh"
+#include "gbntt_internal.h"
+
+namespace gbntt {
+
+constexpr unsigned ERR_E_OVERFLOW = 4u;   // conditional increment ran off the top
+
+// ---------------------------------------------------------------------------
+// Device kernels
+// ---------------------------------------------------------------------------
+
+// out = x + y or x - y (mod beta^nout) for a batch of items. Limb i of the
+// operands reads as 0 at or beyond nx / ny. Subtraction adds the complement
+// of y plus one, so the carry out of the top limb is 1 exactly when x >= y;
+// that carry is stored in *flag. In-place use (out == x or out == y) is safe:
+// a limb is read and written by the same thread.
+struct AddItem {
+    const uint32_t *x, *y;
+    uint32_t *out;
+    unsigned *flag;
+    long long nx, ny, nout;
+    long long tile_start;
+};
+
+constexpr int kAddThreads = 256, kAddPer = 8, kAddTile = kAddThreads * kAddPer;
+
+__global__ void __launch_bounds__(kAddThreads)
+    addsub_kernel(const AddItem *items, int nitems, int sub, unsigned *ticket, unsigned *status, unsigned *error)
+{
+    constexpr int T = kAddThreads, K = kAddPer;
+    __shared__ unsigned s_warp[T / 32];
+    __shared__ long long s_t;
+    __shared__ int s_item;
+    __shared__ unsigned s_cin;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        const long long t = atomicAdd(ticket, 1u);
+        int lo = 0, hi = nitems;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (items[mid].tile_start <= t) lo = mid; else hi = mid;
+        }
+        s_t = t;
+        s_item = lo;
+    }
+    __syncthreads();
+    const AddItem it = items[s_item];
+    const long long tile = s_t - it.tile_start;
+    const long long base = tile * kAddTile + (long long)tid * K;
+    uint64_t s[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const long long pos = base + k;
+        uint64_t v = 0;
+        if (pos < it.nout) {
+            const uint32_t xv = pos < it.nx ? it.x[pos] : 0u;
+            uint32_t yv = pos < it.ny ? it.y[pos] : 0u;
+            if (sub) yv = ~yv;
+            v = (uint64_t)xv + yv + ((sub && pos == 0) ? 1u : 0u);
+        }
+        s[k] = v;
+    }
+    unsigned block_agg;
+    const unsigned prefix = block_scan_transfer<T>(run_transfer<K>(s), s_warp, &block_agg);
+    unsigned err = 0;
+    if (tid == 0) s_cin = lookback_carry(status + it.tile_start, tile, block_agg, err);
+    __syncthreads();
+    uint64_t c = fn_apply(prefix, s_cin);
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const long long pos = base + k;
+        const uint64_t v = s[k] + c;
+        c = v >> 32;
+        if (pos < it.nout) {
+            it.out[pos] = (uint32_t)v;
+            if (pos == it.nout - 1 && it.flag) *it.flag = (unsigned)c;
+        }
+    }
+    if (err) atomicOr(error, err);
+}
+
+// out limb i = bits [off + 32 i, off + 32 i + 32) of x (bits outside
+// [0, 32 nx) read as 0), for i < nout: shifts, truncations, zero-padded
+// copies. An item with a condition word runs only when it is nonzero. out
+// must not overlap x unless off == 0.
+struct ExtractItem {
+    const uint32_t *x;
+    uint32_t *out;
+    const unsigned *cond;
+    long long nx, nout, off;
+    long long blk_start;
+};
+
+constexpr int kExtThreads = 256, kExtPer = 4, kExtBlock = kExtThreads * kExtPer;
+
+__global__ void __launch_bounds__(kExtThreads) extract_kernel(const ExtractItem *items, int nitems)
+{
+    __shared__ int s_item;
+    if (threadIdx.x == 0) {
+        const long long b = blockIdx.x;
+        int lo = 0, hi = nitems;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (items[mid].blk_start <= b) lo = mid; else hi = mid;
+        }
+        s_item = lo;
+    }
+    __syncthreads();
+    const ExtractItem it = items[s_item];
+    if (it.cond && *it.cond == 0) return;
+    const long long i0 = ((long long)blockIdx.x - it.blk_start) * kExtBlock;
+#pragma unroll
+    for (int r = 0; r < kExtPer; r++) {
+        const long long i = i0 + r * kExtThreads + threadIdx.x;
+        if (i >= it.nout) continue;
+        const long long bit = it.off + 32 * i;
+        const long long w = bit >> 5;          // floor division (arithmetic shift)
+        const int sh = (int)(bit & 31);
+        const uint32_t lo = (w >= 0 && w < it.nx) ? it.x[w] : 0u;
+        const uint32_t hi = (w + 1 >= 0 && w + 1 < it.nx) ? it.x[w + 1] : 0u;
+        it.out[i] = sh ? ((lo >> sh) | (hi << (32 - sh))) : lo;
+    }
+}
+
+// Exact limb count (leading zero limbs dropped) of each item.
+struct TrimItem {
+    const uint32_t *x;
+    long long n;
+};
+
+__global__ void trim_kernel(const TrimItem *items, int nitems, long long *lens)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nitems) return;
+    const uint32_t *x = items[i].x;
+    long long n = items[i].n;
+    while (n > 0 && x[n - 1] == 0) n--;
+    lens[i] = n;
+}
+
+// x += 1 (mod beta^n) where *cond is nonzero; running off the top sets an
+// error bit.
+struct IncItem {
+    uint32_t *x;
+    const unsigned *cond;
+    long long n;
+};
+
+__global__ void cond_inc_kernel(const IncItem *items, int nitems, unsigned *error)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nitems) return;
+    const IncItem it = items[i];
+    if (it.cond && *it.cond == 0) return;
+    long long j = 0;
+    for (; j < it.n; j++)
+        if (++it.x[j] != 0) break;
+    if (j == it.n) atomicOr(error, ERR_E_OVERFLOW);
+}
+
+// Leaf groups of the product tree: thread i folds the terms
+// [a + i G, min(a + (i+1) G, b)) as P <- P k + 1, B <- B k (the reference's
+// leaf P = 1, B = a merged term by term, binary_split.c:44-51 and :60-71),
+// writing P at out + 2 i S and B at out + (2 i + 1) S (S = kLeafLimbs) and
+// their limb counts to lens[2 i], lens[2 i + 1]. The host picks G so that B
+// stays below 2^(32 (kLeafLimbs - 2)).
+constexpr int kLeafLimbs = 64;
+
+__global__ void bs_leaf_kernel(unsigned long long a, unsigned long long b, int G, long long nleaf, uint32_t *out,
+                               long long *lens)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nleaf) return;
+    const unsigned long long lo = a + (unsigned long long)i * (unsigned long long)G;
+    const unsigned long long hi = lo + G < b ? lo + G : b;
+    uint32_t p[kLeafLimbs], q[kLeafLimbs];
+    int np = 0, nq = 1;
+    q[0] = 1;
+    for (unsigned long long k = lo; k < hi; k++) {
+        const uint32_t m = (uint32_t)k;
+        uint64_t c = 1;
+        for (int j = 0; j < np; j++) {
+            c += (uint64_t)p[j] * m;
+            p[j] = (uint32_t)c;
+            c >>= 32;
+        }
+        if (c && np < kLeafLimbs) p[np++] = (uint32_t)c;
+        c = 0;
+        for (int j = 0; j < nq; j++) {
+            c += (uint64_t)q[j] * m;
+            q[j] = (uint32_t)c;
+            c >>= 32;
+        }
+        if (c && nq < kLeafLimbs) q[nq++] = (uint32_t)c;
+    }
+    uint32_t *P = out + 2 * i * kLeafLimbs, *B = P + kLeafLimbs;
+    for (int j = 0; j < np; j++) P[j] = p[j];
+    for (int j = 0; j < nq; j++) B[j] = q[j];
+    lens[2 * i] = np;
+    lens[2 * i + 1] = nq;
+}
+
+// Decimal leaves: piece i (i >= first), `stride` limbs at pieces + i stride,
+// holds a value below 10^(9 groups); its 9 groups digits (zero padded) go to
+// digits + 9 groups i, by repeated division by 10^9.
+__global__ void dec_leaf_kernel(const uint32_t *pieces, int stride, long long first, long long npieces, int groups,
+                                char *digits)
+{
+    const long long i = first + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= npieces) return;
+    uint32_t x[kLeafLimbs];
+    const uint32_t *src = pieces + i * stride;
+    int n = stride;
+    for (int j = 0; j < n; j++) x[j] = src[j];
+    while (n > 0 && x[n - 1] == 0) n--;
+    char *o = digits + i * (long long)groups * 9;
+    for (int g = groups - 1; g >= 0; g--) {
+        uint64_t rem = 0;
+        for (int j = n - 1; j >= 0; j--) {
+            const uint64_t cur = (rem << 32) | x[j];
+            x[j] = (uint32_t)(cur / 1000000000u);
+            rem = cur % 1000000000u;
+        }
+        while (n > 0 && x[n - 1] == 0) n--;
+        uint32_t r = (uint32_t)rem;
+        for (int d = 8; d >= 0; d--) {
+            o[g * 9 + d] = (char)('0' + r % 10u);
+            r /= 10u;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host orchestration
+// ---------------------------------------------------------------------------
+namespace {
+
+struct EFail {
+    int code;
+};
+
+[[noreturn]] void efail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    set_error_message(buf);
+    throw EFail{code};
+}
+
+#define ECK(expr)                                                                                            \
+    do {                                                                                                     \
+        cudaError_t _e = (expr);                                                                             \
+        if (_e != cudaSuccess)                                                                               \
+            efail(GBNTT_ERR_CUDA, "CUDA error %d (%s) at %s:%d: %s", (int)_e, cudaGetErrorString(_e), __FILE__, \
+                  __LINE__, #expr);                                                                          \
+    } while (0)
+
+#define ERC(expr)                                                                                            \
+    do {                                                                                                     \
+        const int _r = (expr);                                                                               \
+        if (_r != GBNTT_OK) efail(_r, "%s", gbntt_last_error());                                             \
+    } while (0)
+
+cudaStream_t g_st = nullptr;   // stream of the running pipeline call
+
+// Device limb buffer, stream-ordered allocation on g_st.
+struct DBuf {
+    uint32_t *p = nullptr;
+    size_t cap = 0;
+    DBuf() = default;
+    explicit DBuf(size_t n) { alloc(n); }
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    DBuf(DBuf &&o) noexcept : p(o.p), cap(o.cap) { o.p = nullptr; o.cap = 0; }
+    DBuf &operator=(DBuf &&o) noexcept
+    {
+        if (this != &o) {
+            release();
+            p = o.p;
+            cap = o.cap;
+            o.p = nullptr;
+            o.cap = 0;
+        }
+        return *this;
+    }
+    ~DBuf() { release(); }
+    void alloc(size_t n)
+    {
+        release();
+        void *q = nullptr;
+        ECK(cudaMallocAsync(&q, std::max<size_t>(n, 1) * sizeof(uint32_t), g_st));
+        p = (uint32_t *)q;
+        cap = n;
+    }
+    void release()
+    {
+        if (p) cudaFreeAsync(p, g_st);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+// Host vector mirrored to a stream-ordered device array (upload on creation).
+template <class T>
+struct DTab {
+    T *p = nullptr;
+    explicit DTab(const std::vector<T> &v)
+    {
+        void *q = nullptr;
+        ECK(cudaMallocAsync(&q, std::max<size_t>(v.size(), 1) * sizeof(T), g_st));
+        p = (T *)q;
+        if (!v.empty()) ECK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, g_st));
+    }
+    explicit DTab(size_t n)
+    {
+        void *q = nullptr;
+        ECK(cudaMallocAsync(&q, std::max<size_t>(n, 1) * sizeof(T), g_st));
+        p = (T *)q;
+    }
+    DTab(const DTab &) = delete;
+    DTab &operator=(const DTab &) = delete;
+    ~DTab()
+    {
+        if (p) cudaFreeAsync(p, g_st);
+    }
+};
+
+struct Pipe {
+    unsigned *d_err = nullptr;   // sticky device error bits of this call
+
+    Pipe()
+    {
+        void *q = nullptr;
+        ECK(cudaMallocAsync(&q, sizeof(unsigned), g_st));
+        d_err = (unsigned *)q;
+        ECK(cudaMemsetAsync(d_err, 0, sizeof(unsigned), g_st));
+    }
+    ~Pipe()
+    {
+        if (d_err) cudaFreeAsync(d_err, g_st);
+    }
+
+    void sync() { ECK(cudaStreamSynchronize(g_st)); }
+
+    void check_errors()
+    {
+        unsigned e = 0;
+        ECK(cudaMemcpyAsync(&e, d_err, sizeof e, cudaMemcpyDeviceToHost, g_st));
+        sync();
+        if (e) efail(GBNTT_ERR_DEVICE, "e pipeline device check failed (flags 0x%x)", e);
+    }
+
+    uint32_t read_limb(const uint32_t *p)
+    {
+        uint32_t v = 0;
+        ECK(cudaMemcpyAsync(&v, p, sizeof v, cudaMemcpyDeviceToHost, g_st));
+        sync();
+        return v;
+    }
+
+    // exact limb count of p[0 .. n)
+    size_t trim_top(const uint32_t *p, size_t n)
+    {
+        while (n > 0 && read_limb(p + n - 1) == 0) n--;
+        return n;
+    }
+
+    DBuf upload(const bn::Num &v, size_t n_out)
+    {
+        DBuf d(n_out);
+        ECK(cudaMemsetAsync(d.p, 0, n_out * sizeof(uint32_t), g_st));
+        if (!v.empty()) ECK(cudaMemcpyAsync(d.p, v.data(), std::min(v.size(), n_out) * 4, cudaMemcpyHostToDevice, g_st));
+        sync();   // v may be a temporary
+        return d;
+    }
+
+    // ---- kernel wrappers ----
+    void addsub(std::vector<AddItem> &items, bool sub)
+    {
+        std::vector<AddItem> run;
+        run.reserve(items.size());
+        long long tiles = 0;
+        for (auto it : items) {
+            if (it.nout <= 0) continue;
+            it.tile_start = tiles;
+            tiles += (it.nout + kAddTile - 1) / kAddTile;
+            run.push_back(it);
+        }
+        if (run.empty()) return;
+        if (tiles > 0x7FFFFFFFLL) efail(GBNTT_ERR_SIZE, "add/subtract batch too large");
+        DTab<AddItem> d(run);
+        DTab<unsigned> ctl((size_t)tiles + 1);
+        ECK(cudaMemsetAsync(ctl.p, 0, ((size_t)tiles + 1) * sizeof(unsigned), g_st));
+        addsub_kernel<<<(unsigned)tiles, kAddThreads, 0, g_st>>>(d.p, (int)run.size(), sub ? 1 : 0, ctl.p, ctl.p + 1,
+                                                                 d_err);
+        ECK(cudaGetLastError());
+    }
+    void add1(uint32_t *out, size_t nout, const uint32_t *x, size_t nx, const uint32_t *y, size_t ny, bool sub,
+              unsigned *flag = nullptr)
+    {
+        std::vector<AddItem> v{{x, y, out, flag, (long long)nx, (long long)ny, (long long)nout, 0}};
+        addsub(v, sub);
+    }
+
+    void extract(std::vector<ExtractItem> &items)
+    {
+        std::vector<ExtractItem> run;
+        run.reserve(items.size());
+        long long blks = 0;
+        for (auto it : items) {
+            if (it.nout <= 0) continue;
+            it.blk_start = blks;
+            blks += (it.nout + kExtBlock - 1) / kExtBlock;
+            run.push_back(it);
+        }
+        if (run.empty()) return;
+        if (blks > 0x7FFFFFFFLL) efail(GBNTT_ERR_SIZE, "extract batch too large");
+        DTab<ExtractItem> d(run);
+        extract_kernel<<<(unsigned)blks, kExtThreads, 0, g_st>>>(d.p, (int)run.size());
+        ECK(cudaGetLastError());
+    }
+    void extract1(uint32_t *out, size_t nout, const uint32_t *x, size_t nx, long long off)
+    {
+        std::vector<ExtractItem> v{{x, out, nullptr, (long long)nx, (long long)nout, off, 0}};
+        extract(v);
+    }
+
+    std::vector<long long> trim(const std::vector<TrimItem> &items)
+    {
+        std::vector<long long> lens(items.size());
+        if (items.empty()) return lens;
+        DTab<TrimItem> d(items);
+        DTab<long long> dl(items.size());
+        trim_kernel<<<(unsigned)((items.size() + 255) / 256), 256, 0, g_st>>>(d.p, (int)items.size(), dl.p);
+        ECK(cudaGetLastError());
+        ECK(cudaMemcpyAsync(lens.data(), dl.p, items.size() * sizeof(long long), cudaMemcpyDeviceToHost, g_st));
+        sync();
+        return lens;
+    }
+
+    void cond_inc(const std::vector<IncItem> &items)
+    {
+        if (items.empty()) return;
+        DTab<IncItem> d(items);
+        cond_inc_kernel<<<(unsigned)((items.size() + 255) / 256), 256, 0, g_st>>>(d.p, (int)items.size(), d_err);
+        ECK(cudaGetLastError());
+    }
+
+    void mul(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b, size_t nb)
+    {
+        ERC(gbntt_mul_u32(c, a, na, b, nb, (void *)g_st));
+    }
+
+    struct Prod {
+        uint32_t *c;
+        const uint32_t *a, *b;
+        size_t na, nb;
+    };
+    void batch_mul(const std::vector<Prod> &v)
+    {
+        if (v.empty()) return;
+        std::vector<uint32_t *> c(v.size());
+        std::vector<const uint32_t *> a(v.size()), b(v.size());
+        std::vector<size_t> na(v.size()), nb(v.size());
+        for (size_t i = 0; i < v.size(); i++) {
+            c[i] = v[i].c;
+            a[i] = v[i].a;
+            b[i] = v[i].b;
+            na[i] = v[i].na;
+            nb[i] = v[i].nb;
+        }
+        ERC(gbntt_batch_mul_u32(c.data(), a.data(), na.data(), b.data(), nb.data(), (int)v.size(), (void *)g_st));
+    }
+
+    // ---- binary splitting (reference binary_split.c) ----
+    // P and B of [a, b) on the device, exact limb counts.
+    void binary_split(unsigned long long a, unsigned long long b, DBuf &P, size_t &nP, DBuf &B, size_t &nB)
+    {
+        if (b <= a) {   // empty range: P = 0, B = 1 (binary_split.c:37-43)
+            P = upload(bn::Num(), 1);
+            nP = 0;
+            B = upload(bn::from_u64(1), 1);
+            nB = 1;
+            return;
+        }
+        if (b - 1 > 0xFFFFFFFFull) efail(GBNTT_ERR_ARG, "binary_split: terms must stay below 2^32");
+        const int kbits = 64 - __builtin_clzll(b - 1);
+        const int G = std::max(1, std::min(64, (kLeafLimbs - 2) * 32 / kbits));
+        const long long nleaf = (long long)((b - a + G - 1) / G);
+        DBuf lev((size_t)nleaf * 2 * kLeafLimbs);
+        std::vector<long long> lens((size_t)nleaf * 2);
+        {
+            DTab<long long> dl((size_t)nleaf * 2);
+            bs_leaf_kernel<<<(unsigned)((nleaf + 127) / 128), 128, 0, g_st>>>(a, b, G, nleaf, lev.p, dl.p);
+            ECK(cudaGetLastError());
+            ECK(cudaMemcpyAsync(lens.data(), dl.p, lens.size() * sizeof(long long), cudaMemcpyDeviceToHost, g_st));
+            sync();
+        }
+        struct Node {
+            uint32_t *P, *B;
+            size_t nP, nB;
+        };
+        std::vector<Node> nodes((size_t)nleaf);
+        for (long long i = 0; i < nleaf; i++)
+            nodes[i] = {lev.p + 2 * i * kLeafLimbs, lev.p + (2 * i + 1) * kLeafLimbs, (size_t)lens[2 * i],
+                        (size_t)lens[2 * i + 1]};
+        while (nodes.size() > 1) {
+            const size_t m = nodes.size() / 2;
+            const bool odd = nodes.size() & 1;
+            std::vector<size_t> capB(m), capP(m);
+            size_t total = 0;
+            for (size_t i = 0; i < m; i++) {
+                const Node &L = nodes[2 * i], &R = nodes[2 * i + 1];
+                capB[i] = L.nB + R.nB;
+                capP[i] = std::max(L.nP + R.nB, R.nP) + 1;
+                total += capB[i] + capP[i];
+            }
+            if (odd) total += nodes.back().nP + nodes.back().nB;
+            DBuf next(total);
+            std::vector<Node> out(m + (odd ? 1 : 0));
+            std::vector<Prod> prods;
+            prods.reserve(2 * m);
+            std::vector<AddItem> adds;
+            adds.reserve(m);
+            size_t off = 0;
+            for (size_t i = 0; i < m; i++) {
+                const Node &L = nodes[2 * i], &R = nodes[2 * i + 1];
+                Node &o = out[i];
+                o.B = next.p + off;
+                off += capB[i];
+                o.P = next.p + off;
+                off += capP[i];
+                o.nB = capB[i];
+                o.nP = capP[i];
+                prods.push_back({o.B, L.B, R.B, L.nB, R.nB});   // B = B_L B_R
+                prods.push_back({o.P, L.P, R.B, L.nP, R.nB});   // P_L B_R
+            }
+            batch_mul(prods);
+            for (size_t i = 0; i < m; i++) {   // P = P_L B_R + P_R (in place)
+                const Node &L = nodes[2 * i], &R = nodes[2 * i + 1];
+                adds.push_back({out[i].P, R.P, out[i].P, nullptr, (long long)(L.nP + R.nB), (long long)R.nP,
+                                (long long)capP[i], 0});
+            }
+            addsub(adds, false);
+            if (odd) {   // the last node moves up unchanged
+                const Node &L = nodes.back();
+                Node &o = out[m];
+                o.P = next.p + off;
+                o.B = o.P + L.nP;
+                o.nP = L.nP;
+                o.nB = L.nB;
+                std::vector<ExtractItem> cp{{L.P, o.P, nullptr, (long long)L.nP, (long long)L.nP, 0, 0},
+                                            {L.B, o.B, nullptr, (long long)L.nB, (long long)L.nB, 0, 0}};
+                extract(cp);
+            }
+            std::vector<TrimItem> tr;
+            tr.reserve(2 * out.size());
+            for (auto &o : out) {
+                tr.push_back({o.P, (long long)o.nP});
+                tr.push_back({o.B, (long long)o.nB});
+            }
+            const std::vector<long long> nl = trim(tr);
+            for (size_t i = 0; i < out.size(); i++) {
+                out[i].nP = (size_t)nl[2 * i];
+                out[i].nB = (size_t)nl[2 * i + 1];
+            }
+            nodes.swap(out);
+            lev = std::move(next);
+        }
+        const Node &r = nodes[0];
+        nP = r.nP;
+        nB = r.nB;
+        P.alloc(std::max<size_t>(nP, 1));
+        B.alloc(std::max<size_t>(nB, 1));
+        std::vector<ExtractItem> cp{{r.P, P.p, nullptr, (long long)r.nP, (long long)r.nP, 0, 0},
+                                    {r.B, B.p, nullptr, (long long)r.nB, (long long)r.nB, 0, 0}};
+        extract(cp);
+    }
+
+    // ---- reciprocal (reference newton.c) ----
+    // Y ~ floor(beta^(2k) / T), within a few units, for T of k limbs with the
+    // top bit set; k + 1 limbs. Newton step from h = k/2 + 1 limbs:
+    //   U = T Yh, E = |beta^(k+h) - U| (< 6 beta^k), Y = Yh beta^(k-h) +- floor(Yh E / beta^(2h)).
+    DBuf recip_approx(const uint32_t *T, size_t k)
+    {
+        DBuf Y(k + 1);
+        if (k <= 2) {
+            uint32_t t[2] = {0, 0};
+            ECK(cudaMemcpyAsync(t, T, k * sizeof(uint32_t), cudaMemcpyDeviceToHost, g_st));
+            sync();
+            unsigned __int128 q;
+            if (k == 1) {
+                q = ((unsigned __int128)1 << 64) / t[0];
+            } else {
+                const uint64_t t64 = (uint64_t)t[0] | ((uint64_t)t[1] << 32);
+                q = (~(unsigned __int128)0) / t64;
+                if ((unsigned __int128)((q + 1) * t64) == 0) q += 1;   // t64 divides 2^128
+            }
+            uint32_t y[3] = {(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)(q >> 64)};
+            ECK(cudaMemcpyAsync(Y.p, y, (k + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, g_st));
+            sync();
+            return Y;
+        }
+        const size_t h = k / 2 + 1;
+        DBuf Yh = recip_approx(T + (k - h), h);
+        DBuf U(k + h + 1);
+        mul(U.p, T, k, Yh.p, h + 1);
+        const bool neg = read_limb(U.p + k + h) != 0;
+        DBuf E(k + 1);
+        if (neg) extract1(E.p, k + 1, U.p, k + h + 1, 0);              // U - beta^(k+h)
+        else add1(E.p, k + 1, nullptr, 0, U.p, k + 1, true);           // beta^(k+h) - U
+        U.release();
+        DBuf M(k + h + 2);
+        mul(M.p, Yh.p, h + 1, E.p, k + 1);
+        E.release();
+        extract1(Y.p, k + 1, Yh.p, h + 1, -32LL * (long long)(k - h));   // Yh beta^(k-h)
+        add1(Y.p, k + 1, Y.p, k + 1, M.p + 2 * h, k + 2 - h, neg);
+        return Y;
+    }
+
+    // Exact floor(beta^(2k) / T): start below it, then add T back while the
+    // remainder allows (bounded), and check the remainder is below T.
+    DBuf recip_exact(const uint32_t *T, size_t k)
+    {
+        DBuf Y = recip_approx(T, k);
+        const bn::Num eight = bn::from_u64(8);
+        DBuf c8 = upload(eight, 1);
+        add1(Y.p, k + 1, Y.p, k + 1, c8.p, 1, true);                 // Y -= 8
+        DBuf Z(2 * k + 1);
+        mul(Z.p, Y.p, k + 1, T, k);
+        DBuf R(k + 1), t(k + 1);
+        add1(R.p, k + 1, nullptr, 0, Z.p, k + 1, true);               // beta^(2k) - Z < 16 T
+        Z.release();
+        DTab<unsigned> flag(1);
+        for (int it = 0; it < 16; it++) {
+            add1(t.p, k + 1, R.p, k + 1, T, k, true, flag.p);         // flag: R >= T
+            std::vector<ExtractItem> cp{{t.p, R.p, flag.p, (long long)k + 1, (long long)k + 1, 0, 0}};
+            extract(cp);
+            cond_inc({{Y.p, flag.p, (long long)k + 1}});
+        }
+        add1(t.p, k + 1, R.p, k + 1, T, k, true, flag.p);
+        unsigned f = 0;
+        ECK(cudaMemcpyAsync(&f, flag.p, sizeof f, cudaMemcpyDeviceToHost, g_st));
+        sync();
+        if (f) efail(GBNTT_ERR_DEVICE, "reciprocal correction did not converge (k=%zu)", k);
+        return Y;
+    }
+
+    // ---- division by a shared divisor (reference bigint_div_newton) ----
+    struct Divisor {
+        const uint32_t *d = nullptr;   // divisor, nd limbs, top limb nonzero
+        size_t nd = 0;
+        int s = 0;                     // normalising left shift
+        size_t k = 0;                  // reciprocal precision in limbs, k >= nd
+        DBuf Y;                        // floor(beta^(k+nd) / (d 2^s)), k + 1 limbs
+    };
+    // Valid for dividends x with x 2^s < beta^(k+nd).
+    void make_divisor(Divisor &D, const uint32_t *d, size_t nd, size_t k)
+    {
+        D.d = d;
+        D.nd = nd;
+        D.k = k;
+        const uint32_t top = read_limb(d + nd - 1);
+        if (!top) efail(GBNTT_ERR_ARG, "divisor not trimmed");
+        D.s = __builtin_clz(top);
+        DBuf T(k);
+        extract1(T.p, k, d, nd, -(long long)D.s - 32LL * (long long)(k - nd));
+        D.Y = recip_exact(T.p, k);
+    }
+
+    struct DivItem {
+        const uint32_t *x;
+        size_t nx;
+        uint32_t *q;   // nq limbs
+        size_t nq;
+        uint32_t *r;   // nr limbs, nr >= nd + 1 (remainders before correction are below 2 d)
+        size_t nr;
+    };
+    void divide(const std::vector<DivItem> &items, const Divisor &D)
+    {
+        const size_t n = items.size();
+        if (!n) return;
+        size_t t1 = 0, t2 = 0, tr = 0;
+        for (auto &it : items) {
+            t1 += it.nx + D.k + 1;
+            t2 += it.nq + D.nd;
+            tr += it.nr;
+        }
+        DBuf T1(t1);
+        std::vector<Prod> pr;
+        pr.reserve(n);
+        std::vector<ExtractItem> ex;
+        ex.reserve(n);
+        size_t o = 0;
+        for (auto &it : items) {   // q' = floor(x Y / 2^(32 (k + nd) - s))
+            pr.push_back({T1.p + o, it.x, D.Y.p, it.nx, D.k + 1});
+            ex.push_back({T1.p + o, it.q, nullptr, (long long)(it.nx + D.k + 1), (long long)it.nq,
+                          32LL * (long long)(D.k + D.nd) - D.s, 0});
+            o += it.nx + D.k + 1;
+        }
+        batch_mul(pr);
+        extract(ex);
+        T1.release();
+        DBuf T2(t2);
+        pr.clear();
+        std::vector<AddItem> ad;
+        ad.reserve(n);
+        o = 0;
+        for (auto &it : items) {   // r = x - q' d (mod beta^nr)
+            pr.push_back({T2.p + o, it.q, D.d, it.nq, D.nd});
+            ad.push_back({it.x, T2.p + o, it.r, nullptr, (long long)it.nx, (long long)(it.nq + D.nd),
+                          (long long)it.nr, 0});
+            o += it.nq + D.nd;
+        }
+        batch_mul(pr);
+        addsub(ad, true);
+        T2.release();
+        DBuf Tt(tr);
+        DTab<unsigned> flags(n);
+        std::vector<AddItem> sb;
+        std::vector<ExtractItem> cp;
+        std::vector<IncItem> inc;
+        o = 0;
+        for (size_t i = 0; i < n; i++) {   // while r >= d: r -= d, q += 1
+            const DivItem &it = items[i];
+            sb.push_back({it.r, D.d, Tt.p + o, flags.p + i, (long long)it.nr, (long long)D.nd, (long long)it.nr, 0});
+            cp.push_back({Tt.p + o, it.r, flags.p + i, (long long)it.nr, (long long)it.nr, 0, 0});
+            inc.push_back({it.q, flags.p + i, (long long)it.nq});
+            o += it.nr;
+        }
+        for (int round = 0; round < 2; round++) {
+            addsub(sb, true);
+            extract(cp);
+            cond_inc(inc);
+        }
+        addsub(sb, true);   // every remainder must now be below d
+        std::vector<unsigned> f(n);
+        ECK(cudaMemcpyAsync(f.data(), flags.p, n * sizeof(unsigned), cudaMemcpyDeviceToHost, g_st));
+        sync();
+        for (size_t i = 0; i < n; i++)
+            if (f[i]) efail(GBNTT_ERR_DEVICE, "division correction did not converge (item %zu of %zu)", i, n);
+    }
+
+    // ---- powers ----
+    // 5^e: leading bits on the host, then GPU squarings and x 5 = (x << 2) + x.
+    DBuf pow5(unsigned long long e, size_t &n)
+    {
+        int i = 63;
+        while (i >= 0 && !((e >> i) & 1)) i--;
+        unsigned long long v = 0;
+        while (i >= 0 && v * 2 + ((e >> i) & 1) <= 27) {
+            v = v * 2 + ((e >> i) & 1);
+            i--;
+        }
+        unsigned long long x0 = 1;
+        for (unsigned long long j = 0; j < v; j++) x0 *= 5;
+        DBuf x = upload(bn::from_u64(x0), 2);
+        n = x0 >> 32 ? 2 : 1;
+        for (; i >= 0; i--) {
+            DBuf y(2 * n);
+            mul(y.p, x.p, n, x.p, n);
+            n = trim_top(y.p, 2 * n);
+            x = std::move(y);
+            if ((e >> i) & 1) {
+                DBuf z(n + 1);
+                extract1(z.p, n + 1, x.p, n, -2);
+                add1(z.p, n + 1, z.p, n + 1, x.p, n, false);
+                n = trim_top(z.p, n + 1);
+                x = std::move(z);
+            }
+        }
+        return x;
+    }
+
+    // 10^e = 5^e 2^e
+    DBuf pow10(unsigned long long e, size_t &n)
+    {
+        size_t n5 = 0;
+        DBuf f = pow5(e, n5);
+        const size_t cap = n5 + (size_t)(e / 32) + 1;
+        DBuf t(cap);
+        extract1(t.p, cap, f.p, n5, -(long long)e);
+        n = trim_top(t.p, cap);
+        return t;
+    }
+
+    // ---- decimal conversion (reference base_convert.c) ----
+    // Decimal digits of x (no leading zeros; "0" for zero) into digits.
+    void to_decimal(const uint32_t *x, size_t nx, std::vector<char> &digits)
+    {
+        nx = trim_top(x, nx);
+        if (nx == 0) {
+            digits.assign(1, '0');
+            return;
+        }
+        const uint32_t top = read_limb(x + nx - 1);
+        const double bits = 32.0 * (double)(nx - 1) + (32 - __builtin_clz(top));
+        const long long dub = (long long)floor(bits * 0.30102999566398120) + 2;   // digit count upper bound
+        int J = 0;
+        while (9LL << (J + 1) < dub) J++;
+        const int jl = std::min(J + 1, 6);        // leaf pieces: 9 * 2^jl digits
+        const long long TD = 9LL << (J + 1);      // padded digit count
+        const long long Z = TD - dub;             // leading digits known to be zero
+        const long long LD = 9LL << jl;
+        const long long nleaf = 1LL << (J + 1 - jl);
+        DTab<char> dig((size_t)TD);
+        if (jl == J + 1) {   // one leaf: x itself
+            if (nx > (size_t)kLeafLimbs) efail(GBNTT_ERR_SIZE, "decimal leaf too large");
+            dec_leaf_kernel<<<1, 32, 0, g_st>>>(x, (int)nx, 0, 1, (int)(1 << jl), dig.p);
+            ECK(cudaGetLastError());
+        } else {
+            // d_j = 10^(9 2^j) for j = jl .. J; nd_j limbs; pieces of level j
+            // are below d_j^2 and stored at stride W_j = 2 nd_j + 1
+            bn::Num half, low;
+            {
+                bn::Num v = bn::from_u64(1);
+                for (int g = 0; g < (1 << (jl - 1)); g++) bn::mul_small_add(v, 1000000000u, 0);
+                half = v;
+                for (int g = 0; g < (1 << (jl - 1)); g++) bn::mul_small_add(v, 1000000000u, 0);
+                low = v;
+            }
+            const size_t w_leaf = 2 * half.size() + 1;
+            if (w_leaf > (size_t)kLeafLimbs) efail(GBNTT_ERR_SIZE, "decimal leaf stride too large");
+            std::vector<DBuf> pw(J + 1);
+            std::vector<size_t> nd(J + 1, 0);
+            pw[jl] = upload(low, low.size());
+            nd[jl] = low.size();
+            for (int j = jl + 1; j <= J; j++) {
+                pw[j].alloc(2 * nd[j - 1]);
+                mul(pw[j].p, pw[j - 1].p, nd[j - 1], pw[j - 1].p, nd[j - 1]);
+                nd[j] = trim_top(pw[j].p, 2 * nd[j - 1]);
+            }
+            auto stride = [&](int j) -> size_t { return j >= jl ? 2 * nd[j] + 1 : w_leaf; };
+            DBuf lev(stride(J));
+            extract1(lev.p, stride(J), x, nx, 0);
+            for (int j = J; j >= jl; j--) {
+                Divisor D;
+                make_divisor(D, pw[j].p, nd[j], nd[j]);
+                const long long cnt = 1LL << (J - j);
+                const size_t W = stride(j), Wc = stride(j - 1);
+                DBuf child((size_t)(2 * cnt) * Wc);
+                const long long i0 = Z / (9LL << (j + 1));
+                std::vector<DivItem> items;
+                items.reserve((size_t)(cnt - i0));
+                for (long long i = i0; i < cnt; i++)
+                    items.push_back({lev.p + i * W, W, child.p + 2 * i * Wc, Wc, child.p + (2 * i + 1) * Wc, Wc});
+                divide(items, D);
+                lev = std::move(child);
+                pw[j].release();
+            }
+            const long long first = Z / LD;
+            const long long np = nleaf - first;
+            dec_leaf_kernel<<<(unsigned)((np + 127) / 128), 128, 0, g_st>>>(lev.p, (int)w_leaf, first, nleaf,
+                                                                              (int)(1 << jl), dig.p);
+            ECK(cudaGetLastError());
+        }
+        std::vector<char> all((size_t)(TD - Z));
+        ECK(cudaMemcpyAsync(all.data(), dig.p + Z, all.size(), cudaMemcpyDeviceToHost, g_st));
+        sync();
+        size_t lead = 0;
+        while (lead + 1 < all.size() && all[lead] == '0') lead++;
+        digits.assign(all.begin() + lead, all.end());
+    }
+};
+
+// reference split_terms_needed (ntt/app/compute_e/binary_split.c:96-108)
+long split_terms(long n_digits)
+{
+    const double target = (double)n_digits * log(10.0);
+    double N = target / log(target);
+    for (int i = 0; i < 50; i++) {
+        const double logN = log(N);
+        if (logN <= 1.0) {
+            N = target;
+            break;
+        }
+        N = target / (logN - 1.0);
+    }
+    return (long)(N * 1.05) + 64;
+}
+
+// 32-bit coefficient transform log the e pipeline needs for D digits.
+int e_required_log(long digits)
+{
+    const long K = split_terms(digits + 20);
+    const double lnB = lgamma((double)K + 1.0);
+    const double nB = lnB / log(2.0) / 32.0 + 4;
+    const double nX = nB + (double)(digits - 1) * 3.3219280948873623 / 32.0 + 4;
+    const double k = std::max(nB, nX + 1 - nB);
+    const double need = nX + k + 2 + 64;
+    int L = kMinLog;
+    while ((double)(1LL << L) < need) L++;
+    return L;
+}
+
+// Scoped use of the engine: initialise it when nobody has (torn down at the
+// end), refuse when it is initialised but too small.
+struct EngineUse {
+    bool owned = false;
+    explicit EngineUse(int need)
+    {
+        if (gbntt_is_ready()) {
+            if (gbntt_max_log() < need)
+                efail(GBNTT_ERR_SIZE, "engine initialised for 2^%d coefficients; this call needs 2^%d", gbntt_max_log(),
+                      need);
+        } else {
+            ERC(gbntt_init(need));
+            owned = true;
+        }
+        g_st = (cudaStream_t)gbntt_stream();
+    }
+    ~EngineUse()
+    {
+        if (g_st) cudaStreamSynchronize(g_st);
+        if (owned) gbntt_teardown();
+        g_st = nullptr;
+    }
+};
+
+struct Stopwatch {
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    double lap()
+    {
+        const auto t = std::chrono::steady_clock::now();
+        const double s = std::chrono::duration<double>(t - t0).count();
+        t0 = t;
+        return s;
+    }
+};
+
+size_t host_trim(const uint32_t *x, size_t n)
+{
+    while (n > 0 && x[n - 1] == 0) n--;
+    return n;
+}
+
+int copy_out(uint32_t *out, size_t cap, size_t *n_out, const uint32_t *d, size_t n)
+{
+    if (n_out) *n_out = n;
+    if (n > cap) efail(GBNTT_ERR_SIZE, "output needs %zu limbs, capacity %zu", n, cap);
+    if (n) ECK(cudaMemcpyAsync(out, d, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, g_st));
+    ECK(cudaStreamSynchronize(g_st));
+    return GBNTT_OK;
+}
+
+}  // namespace
+}  // namespace gbntt
+
+using namespace gbntt;
+
+extern "C" {
+
+long gbntt_split_terms_needed(long n_digits) { return split_terms(n_digits); }
+
+int gbntt_e_required_log(long digits) { return digits < 1 ? -GBNTT_ERR_ARG : e_required_log(digits); }
+
+int gbntt_binary_split(unsigned long long a, unsigned long long b, uint32_t *p, size_t p_cap, size_t *np, uint32_t *q,
+                       size_t q_cap, size_t *nq)
+{
+    try {
+        if (!gbntt_is_ready()) efail(GBNTT_ERR_NOT_INIT, "engine not initialised");
+        EngineUse eu(gbntt_max_log());
+        Pipe pp;
+        DBuf P, B;
+        size_t nP = 0, nB = 0;
+        pp.binary_split(a, b, P, nP, B, nB);
+        pp.check_errors();
+        copy_out(p, p_cap, np, P.p, nP);
+        return copy_out(q, q_cap, nq, B.p, nB);
+    } catch (const EFail &f) {
+        return f.code;
+    }
+}
+
+int gbntt_newton_reciprocal_u32(uint32_t *x, size_t x_cap, size_t *nx, const uint32_t *q, size_t nq)
+{
+    try {
+        if (!gbntt_is_ready()) efail(GBNTT_ERR_NOT_INIT, "engine not initialised");
+        nq = host_trim(q, nq);
+        if (nq == 0) efail(GBNTT_ERR_ARG, "newton_reciprocal: Q is zero");
+        EngineUse eu(gbntt_max_log());
+        Pipe pp;
+        bn::Num hq(q, q + nq);
+        DBuf dq = pp.upload(hq, nq);
+        const int s = __builtin_clz(q[nq - 1]);
+        DBuf T(nq);
+        pp.extract1(T.p, nq, dq.p, nq, -(long long)s);
+        DBuf Y = pp.recip_exact(T.p, nq);   // floor(2^(64 nq - s) / Q)
+        DBuf R(nq + 1);
+        pp.extract1(R.p, nq + 1, Y.p, nq + 1, s);   // floor(2^(2 bits(Q)) / Q)
+        pp.check_errors();
+        return copy_out(x, x_cap, nx, R.p, pp.trim_top(R.p, nq + 1));
+    } catch (const EFail &f) {
+        return f.code;
+    }
+}
+
+int gbntt_div_newton_u32(uint32_t *qout, size_t q_cap, size_t *nq, uint32_t *rout, size_t r_cap, size_t *nr,
+                         const uint32_t *n, size_t nn, const uint32_t *d, size_t nd)
+{
+    try {
+        if (!gbntt_is_ready()) efail(GBNTT_ERR_NOT_INIT, "engine not initialised");
+        nn = host_trim(n, nn);
+        nd = host_trim(d, nd);
+        if (nd == 0) efail(GBNTT_ERR_ARG, "division by zero");
+        EngineUse eu(gbntt_max_log());
+        Pipe pp;
+        if (nn < nd) {   // quotient 0, remainder n
+            if (nq) *nq = 0;
+            if (rout || nr) {
+                if (nr) *nr = nn;
+                if (nn > r_cap) efail(GBNTT_ERR_SIZE, "remainder needs %zu limbs", nn);
+                if (rout && nn) memcpy(rout, n, nn * sizeof(uint32_t));
+            }
+            return GBNTT_OK;
+        }
+        DBuf dn = pp.upload(bn::Num(n, n + nn), nn);
+        DBuf dd = pp.upload(bn::Num(d, d + nd), nd);
+        Pipe::Divisor D;
+        pp.make_divisor(D, dd.p, nd, std::max(nd, nn + 1 - nd));
+        const size_t cq = nn - nd + 1, cr = nd + 1;
+        DBuf Q(cq), R(cr);
+        pp.divide({{dn.p, nn, Q.p, cq, R.p, cr}}, D);
+        pp.check_errors();
+        copy_out(qout, q_cap, nq, Q.p, pp.trim_top(Q.p, cq));
+        if (rout || nr) {
+            const size_t lr = pp.trim_top(R.p, cr);
+            if (!rout) { if (nr) *nr = lr; return GBNTT_OK; }
+            copy_out(rout, r_cap, nr, R.p, lr);
+        }
+        return GBNTT_OK;
+    } catch (const EFail &f) {
+        return f.code;
+    }
+}
+
+int gbntt_pow10_u32(uint32_t *out, size_t cap, size_t *n_out, unsigned long long e)
+{
+    try {
+        if (!gbntt_is_ready()) efail(GBNTT_ERR_NOT_INIT, "engine not initialised");
+        EngineUse eu(gbntt_max_log());
+        Pipe pp;
+        size_t n = 0;
+        DBuf t = pp.pow10(e, n);
+        pp.check_errors();
+        return copy_out(out, cap, n_out, t.p, n);
+    } catch (const EFail &f) {
+        return f.code;
+    }
+}
+
+int gbntt_to_decimal_u32(char *out, size_t cap, size_t *len, const uint32_t *x, size_t nx)
+{
+    try {
+        if (!gbntt_is_ready()) efail(GBNTT_ERR_NOT_INIT, "engine not initialised");
+        nx = host_trim(x, nx);
+        EngineUse eu(gbntt_max_log());
+        Pipe pp;
+        DBuf dx = pp.upload(bn::Num(x, x + nx), std::max<size_t>(nx, 1));
+        std::vector<char> dig;
+        pp.to_decimal(dx.p, nx, dig);
+        pp.check_errors();
+        if (len) *len = dig.size();
+        if (dig.size() + 1 > cap) efail(GBNTT_ERR_SIZE, "decimal string needs %zu bytes", dig.size() + 1);
+        memcpy(out, dig.data(), dig.size());
+        out[dig.size()] = 0;
+        return GBNTT_OK;
+    } catch (const EFail &f) {
+        return f.code;
+    }
+}
+
+int gbntt_compute_e(long digits, char *out, size_t cap, double *phase_seconds)
+{
+    try {
+        if (digits < 1) efail(GBNTT_ERR_ARG, "digits must be >= 1");
+        if (!out || cap < (size_t)digits + 2) efail(GBNTT_ERR_ARG, "output buffer needs %ld bytes", digits + 2);
+        EngineUse eu(e_required_log(digits));
+        Pipe pp;
+        Stopwatch sw, total;
+        double ph[5] = {0, 0, 0, 0, 0};
+        const long K = split_terms(digits + 20);
+        // P, B of [1, K + 1): B = K!, P / B = sum_{k=1}^{K} 1/k!
+        DBuf P, B;
+        size_t nP = 0, nB = 0;
+        pp.binary_split(1, (unsigned long long)K + 1, P, nP, B, nB);
+        pp.sync();
+        ph[0] = sw.lap();
+        // x = (B + P) 10^(D-1) = ((B + P) 5^(D-1)) << (D-1)
+        const size_t cn = std::max(nB, nP) + 1;
+        DBuf num(cn);
+        pp.add1(num.p, cn, B.p, nB, P.p, nP, false);
+        P.release();
+        const size_t nn = pp.trim_top(num.p, cn);
+        size_t n5 = 0;
+        DBuf f5 = pp.pow5((unsigned long long)(digits - 1), n5);
+        DBuf X(nn + n5);
+        pp.mul(X.p, num.p, nn, f5.p, n5);
+        num.release();
+        f5.release();
+        const size_t nX = pp.trim_top(X.p, nn + n5);
+        const size_t cx = nX + (size_t)((digits - 1) / 32) + 1;
+        DBuf x(cx);
+        pp.extract1(x.p, cx, X.p, nX, -(long long)(digits - 1));
+        X.release();
+        const size_t nx = pp.trim_top(x.p, cx);
+        ph[1] = sw.lap();
+        // Q = floor(x / B)
+        Pipe::Divisor D;
+        pp.make_divisor(D, B.p, nB, std::max(nB, nx + 1 - nB));
+        const size_t cq = nx - nB + 1, cr = nB + 1;
+        DBuf Q(cq), R(cr);
+        pp.divide({{x.p, nx, Q.p, cq, R.p, cr}}, D);
+        x.release();
+        R.release();
+        D.Y.release();
+        const size_t nQ = pp.trim_top(Q.p, cq);
+        ph[2] = sw.lap();
+        std::vector<char> dig;
+        pp.to_decimal(Q.p, nQ, dig);
+        pp.check_errors();
+        ph[3] = sw.lap();
+        if ((long)dig.size() != digits)
+            efail(GBNTT_ERR_DEVICE, "quotient has %zu decimal digits, expected %ld", dig.size(), digits);
+        out[0] = dig[0];
+        out[1] = '.';
+        if (digits > 1) memcpy(out + 2, dig.data() + 1, (size_t)digits - 1);
+        out[digits + 1] = 0;
+        ph[4] = total.lap();
+        if (phase_seconds) memcpy(phase_seconds, ph, sizeof ph);
+        return GBNTT_OK;
+    } catch (const EFail &f) {
+        return f.code;
+    }
+}
+
+}  // extern "C"

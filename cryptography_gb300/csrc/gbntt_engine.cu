@@ -96,6 +96,8 @@ static void set_err(const char *fmt, ...)
     va_end(ap);
 }
 
+void set_error_message(const char *msg) { snprintf(g_err, sizeof g_err, "%s", msg); }
+
 #define CK(expr)                                                                              \
     do {                                                                                      \
         cudaError_t _e = (expr);                                                              \
@@ -175,21 +177,30 @@ static int choose_log(size_t na, size_t nb)
     return L;
 }
 
-static size_t workspace_bytes(int max_log)
-{
-    const size_t n = (size_t)1 << max_log;
-    const size_t spec = 6 * n * sizeof(uint64_t);
-    const size_t tw = 3 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t);
-    const size_t ctl = (2 + carry_tiles64((long long)n + 1) + 64) * sizeof(unsigned);
-    const size_t io = (4 * n + 64) * sizeof(uint32_t);
-    return spec + tw + ctl + io;
-}
-
 // Products per batched wave and the 8-byte words of one wave's tables:
 // limb pointers and lengths of A and B, output pointers and lengths,
 // carry tile starts (W + 1).
 constexpr int kMaxBatch = 16384;
 constexpr size_t kBtabWords = 7 * (size_t)kMaxBatch + 8;
+
+// Carry tile status words for a workspace of n coefficients per prime: one
+// product of n coefficients (64-bit limbs: n / 1024 tiles), or a batched
+// wave of W <= kMaxBatch products of 2^L coefficients with W 2^L <= n, whose
+// tiles sum to at most sum_b ceil((2^L + 1) / 2048) <= n / 2048 + 2 W.
+static size_t status_words(size_t n)
+{
+    return (size_t)std::max(carry_tiles64((long long)n + 1), carry_tiles((long long)n + 1) + 2 * (long long)kMaxBatch) + 64;
+}
+
+static size_t workspace_bytes(int max_log)
+{
+    const size_t n = (size_t)1 << max_log;
+    const size_t spec = 6 * n * sizeof(uint64_t);
+    const size_t tw = 3 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t);
+    const size_t ctl = (2 + status_words(n)) * sizeof(unsigned);
+    const size_t io = (4 * n + 64) * sizeof(uint32_t);
+    return spec + tw + ctl + io;
+}
 
 static void free_all()
 {
@@ -224,7 +235,7 @@ static int init_impl(int max_log)
         free_all();
         return GBNTT_ERR_ALLOC;
     }
-    g.n_status = (size_t)carry_tiles64((long long)g.n_max + 1) + 64;
+    g.n_status = status_words(g.n_max);
     g.io_words = 4 * g.n_max + 64;
     if (cudaMalloc(&g.d_ctl, (2 + g.n_status) * sizeof(unsigned)) != cudaSuccess ||
         cudaMalloc(&g.d_io, g.io_words * sizeof(uint32_t)) != cudaSuccess) {
@@ -483,6 +494,7 @@ struct BatchCtx {
     uint64_t *spec;              // 6 x cap words: A (3 x cap) then B (3 x cap)
     size_t cap;                  // coefficients per prime per operand
     unsigned *ctl;               // [0] ticket, [1] error, [2..] carry tile status
+    size_t n_status;             // status words after ctl[2]
     uint64_t *d_btab, *h_btab;   // two table slots (device, pinned host)
     cudaEvent_t *btab_ev;        // two events guarding the host slots
     int *slot;
@@ -516,6 +528,10 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
         tiles += carry_tiles((long long)(it.na + it.nb));
     }
     hTS[W] = (uint64_t)tiles;
+    if ((size_t)tiles > x.n_status) {
+        set_err("batched wave needs %lld carry tiles; workspace holds %zu", tiles, x.n_status);
+        return GBNTT_ERR_SIZE;
+    }
     CK(cudaMemcpyAsync(dtab, h, (7 * (size_t)W + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(x.btab_ev[slot], st));
     *x.slot = slot ^ 1;
@@ -571,7 +587,7 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
         order.push_back({L, i});
     }
     std::stable_sort(order.begin(), order.end());
-    BatchCtx x{g.d_spec, g.n_max, g.d_ctl, g.d_btab, g.h_btab, g.btab_ev, &g_batch_slot};
+    BatchCtx x{g.d_spec, g.n_max, g.d_ctl, g.n_status, g.d_btab, g.h_btab, g.btab_ev, &g_batch_slot};
     std::vector<BatchItem> items;
     size_t pos = 0;
     while (pos < order.size()) {
@@ -1048,7 +1064,7 @@ int gbntt_server_start(int slots, int slot_log)
     S->cap = (size_t)1 << slot_log;
     S->slot_log = slot_log;
     S->slots.resize(slots);
-    const size_t nstat = (size_t)carry_tiles((long long)S->cap + 1) + 64;
+    const size_t nstat = status_words(S->cap);
     for (auto &sl : S->slots) {
         bool ok = cudaMalloc(&sl.spec, 6 * S->cap * sizeof(uint64_t)) == cudaSuccess &&
                   cudaMalloc(&sl.ctl, (2 + nstat) * sizeof(unsigned)) == cudaSuccess &&
@@ -1065,7 +1081,7 @@ int gbntt_server_start(int slots, int slot_log)
             server_free(S);
             return GBNTT_ERR_ALLOC;
         }
-        sl.ctx = BatchCtx{sl.spec, S->cap, sl.ctl, sl.d_btab, sl.h_btab, sl.btab_ev, &sl.tab_slot};
+        sl.ctx = BatchCtx{sl.spec, S->cap, sl.ctl, nstat, sl.d_btab, sl.h_btab, sl.btab_ev, &sl.tab_slot};
     }
     g_srv = S;
     S->th = std::thread(server_loop, S);

@@ -82,4 +82,7 @@ cudaError_t launch_fill_splitmix(uint32_t *d, long long n, uint64_t seed, cudaSt
 cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *b, uint64_t *out, long long n,
                           cudaStream_t stream);
 
+// Message returned by gbntt_last_error (gbntt_engine.cu).
+void set_error_message(const char *msg);
+
 }  // namespace gbntt

@@ -15,6 +15,7 @@
 //    cells of ntt/lib/transfer_core.h:165-251, generalised to carries in
 //    {0, 1, 2}.
 #include "gbntt_arith.cuh"
+#include "gbntt_carry.cuh"
 #include "gbntt_internal.h"
 
 namespace gbntt {
@@ -88,55 +89,8 @@ cudaError_t launch_fill_splitmix(uint32_t *d, long long n, uint64_t seed, cudaSt
 constexpr int kCarryThreads = 256;
 constexpr int kCarryPerThread = 8;
 constexpr int kCarryTile = kCarryThreads * kCarryPerThread;   // limbs per tile
-constexpr int kLookbackSpinLimit = 1 << 21;                   // ~0.1 s with backoff
 
 long long carry_tiles(long long n_out) { return (n_out + kCarryTile - 1) / kCarryTile; }
-
-// Carry transfer function over carries {0,1,2}: 2 bits per input value.
-__device__ __forceinline__ unsigned fn_apply(unsigned f, unsigned c) { return (f >> (2 * c)) & 3u; }
-__device__ __forceinline__ unsigned fn_compose(unsigned g, unsigned f)   // g after f
-{
-    return fn_apply(g, fn_apply(f, 0)) | (fn_apply(g, fn_apply(f, 1)) << 2) | (fn_apply(g, fn_apply(f, 2)) << 4);
-}
-constexpr unsigned kFnIdentity = 0u | (1u << 2) | (2u << 4);
-
-__device__ __forceinline__ int spad(int q) { return q + (q >> 5); }
-
-// Decoupled look-back (one thread per tile): publishes this tile's carry
-// transfer function, walks predecessors until an inclusive carry (or a
-// constant composed function) is known, publishes its own inclusive carry
-// and returns the carry into the tile. Status word: bits 8-9 flag (1 =
-// aggregate function, 2 = inclusive carry), bits 0-5 value. Every wait is
-// bounded; on timeout the error bit is set and carry 0 is assumed.
-__device__ unsigned lookback_carry(unsigned *status, long long tile, unsigned block_agg, unsigned &err)
-{
-    unsigned cin = 0;
-    if (tile == 0) {
-        atomicExch(&status[0], (2u << 8) | fn_apply(block_agg, 0));
-        return 0;
-    }
-    atomicExch(&status[tile], (1u << 8) | block_agg);
-    unsigned acc = kFnIdentity;
-    long long j = tile - 1;
-    for (;;) {
-        unsigned w = 0;
-        int spins = 0;
-        for (;;) {
-            w = atomicAdd(&status[j], 0u);
-            if (w >> 8) break;
-            if (++spins > kLookbackSpinLimit) { err |= ERR_LOOKBACK_TIMEOUT; w = 2u << 8; break; }
-            __nanosleep(32);
-        }
-        const unsigned flag = w >> 8, val = w & 63u;
-        if (flag == 2) { cin = fn_apply(acc, val); break; }
-        acc = fn_compose(acc, val);
-        const unsigned c0 = fn_apply(acc, 0);
-        if (c0 == fn_apply(acc, 1) && c0 == fn_apply(acc, 2)) { cin = c0; break; }
-        --j;
-    }
-    atomicExch(&status[tile], (2u << 8) | fn_apply(block_agg, cin));
-    return cin;
-}
 
 // c_j from its residues (mixed radix, Garner): returns the three 32-bit words
 // of c_j < 2^96 and flags a nonzero third digit (c_j >= q0*q1 means the

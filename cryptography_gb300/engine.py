@@ -44,6 +44,8 @@ EXPORTS = (
     "gbntt_mul_u32_noalloc", "gbntt_batch_mul_u32", "gbntt_fill_operand",
     "gbntt_server_start", "gbntt_server_submit", "gbntt_server_query", "gbntt_server_wait", "gbntt_server_stats",
     "gbntt_server_stop",
+    "gbntt_split_terms_needed", "gbntt_e_required_log", "gbntt_binary_split", "gbntt_newton_reciprocal_u32",
+    "gbntt_div_newton_u32", "gbntt_pow10_u32", "gbntt_to_decimal_u32", "gbntt_compute_e",
 )
 
 _lib = None
@@ -134,6 +136,23 @@ def lib():
     L.gbntt_launch_records.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_float), ctypes.c_int]
     L.gbntt_launch_records.restype = ctypes.c_int
+    _szp = ctypes.POINTER(_sz)
+    L.gbntt_split_terms_needed.argtypes = [ctypes.c_long]
+    L.gbntt_split_terms_needed.restype = ctypes.c_long
+    L.gbntt_e_required_log.argtypes = [ctypes.c_long]
+    L.gbntt_e_required_log.restype = ctypes.c_int
+    L.gbntt_binary_split.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong, _u32p, _sz, _szp, _u32p, _sz, _szp]
+    L.gbntt_binary_split.restype = ctypes.c_int
+    L.gbntt_newton_reciprocal_u32.argtypes = [_u32p, _sz, _szp, _u32p, _sz]
+    L.gbntt_newton_reciprocal_u32.restype = ctypes.c_int
+    L.gbntt_div_newton_u32.argtypes = [_u32p, _sz, _szp, _u32p, _sz, _szp, _u32p, _sz, _u32p, _sz]
+    L.gbntt_div_newton_u32.restype = ctypes.c_int
+    L.gbntt_pow10_u32.argtypes = [_u32p, _sz, _szp, ctypes.c_ulonglong]
+    L.gbntt_pow10_u32.restype = ctypes.c_int
+    L.gbntt_to_decimal_u32.argtypes = [ctypes.c_char_p, _sz, _szp, _u32p, _sz]
+    L.gbntt_to_decimal_u32.restype = ctypes.c_int
+    L.gbntt_compute_e.argtypes = [ctypes.c_long, ctypes.c_char_p, _sz, ctypes.POINTER(ctypes.c_double)]
+    L.gbntt_compute_e.restype = ctypes.c_int
     L.gbntt_last_error.restype = ctypes.c_char_p
     L.gbntt_stream.restype = _vp
     _lib = L

@@ -223,6 +223,55 @@ int gbntt_launch_records(int *kind, int *log_l, double *bytes, float *ms, int ma
 int gbntt_mul_u32_noalloc(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb,
                           void *stream);
 
+/* ---- e pipeline and the arith layer above the multiply ----
+ * Host operands and results, 32-bit limbs little-endian; every product runs
+ * on the engine (batched where a level has many). All but gbntt_compute_e
+ * need an initialised engine large enough for their products. */
+
+/* Replaces split_terms_needed (ntt/app/compute_e/binary_split.c:96-108):
+ * number of series terms for n_digits digits, the same formula. */
+long gbntt_split_terms_needed(long n_digits);
+
+/* Transform log (32-bit coefficients) that gbntt_compute_e needs for
+ * `digits` digits; negative on bad input. */
+int gbntt_e_required_log(long digits);
+
+/* Replaces binary_split (ntt/app/compute_e/binary_split.c:26-86): P and B of
+ * [a, b) with B = (b-1)!/(a-1)! and P / B = sum_{k=a}^{b-1} (a-1)!/k!
+ * (empty range: P = 0, B = 1). b - 1 < 2^32. p[0 .. *np), q[0 .. *nq). */
+int gbntt_binary_split(unsigned long long a, unsigned long long b, uint32_t *p, size_t p_cap, size_t *np,
+                       uint32_t *q, size_t q_cap, size_t *nq);
+
+/* Replaces newton_reciprocal (ntt/lib/arith/newton.h:23, newton.c:119):
+ * x = floor(2^(2 bits(Q)) / Q), always exact here (the reference's may be
+ * one below). */
+int gbntt_newton_reciprocal_u32(uint32_t *x, size_t x_cap, size_t *nx, const uint32_t *q, size_t nq);
+
+/* Replaces bigint_div_newton (ntt/lib/arith/newton.h:28, newton.c:128):
+ * q = floor(n / d) and, when r or nr is given, r = n mod d. */
+int gbntt_div_newton_u32(uint32_t *q, size_t q_cap, size_t *nq, uint32_t *r, size_t r_cap, size_t *nr,
+                         const uint32_t *n, size_t nn, const uint32_t *d, size_t nd);
+
+/* Replaces base_convert_pow10_exact (ntt/lib/arith/base_convert.h:32):
+ * out = 10^e. */
+int gbntt_pow10_u32(uint32_t *out, size_t cap, size_t *n_out, unsigned long long e);
+
+/* Replaces bigint_to_decimal (ntt/lib/arith/base_convert.h:24): decimal
+ * digits of x, NUL-terminated, no leading zeros ("0" for zero); *len
+ * receives the digit count (cap >= len + 1). */
+int gbntt_to_decimal_u32(char *out, size_t cap, size_t *len, const uint32_t *x, size_t nx);
+
+/* Replaces the compute_e application (ntt/app/compute_e/main.c:150-345):
+ * writes "2.718..." with `digits` significant digits (the string main.c
+ * prints after "e = ", digits + 1 characters) and a NUL into out (cap >=
+ * digits + 2). Uses the reference's term count and guard digits, so the
+ * digits are the reference's. Initialises the engine for the call when it
+ * is not initialised (and tears it down after); fails with GBNTT_ERR_SIZE
+ * when it is initialised too small. phase_seconds, when not NULL, receives
+ * 5 wall times: product tree, numerator x 10^(D-1), division, decimal
+ * conversion, total. */
+int gbntt_compute_e(long digits, char *out, size_t cap, double *phase_seconds);
+
 /* Last error message of this library. */
 const char *gbntt_last_error(void);
 

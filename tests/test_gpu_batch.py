@@ -82,3 +82,39 @@ def test_device_operand_generator_matches_host(engine):
         cudart.synchronize()
         assert np.array_equal(d.download(np.uint32, n), synth.operand(n, seed))
         d.free()
+
+
+def test_batch_many_tiny_products_on_a_small_engine():
+    # a wave of W tiny products needs W carry tiles although W 2^L fits a
+    # small workspace: the status area must hold them (2^16 engine, W = 2048)
+    import json
+    import os
+    import subprocess
+    import sys
+    import textwrap
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    body = textwrap.dedent("""
+        import json, sys
+        sys.path.insert(0, %r)
+        import numpy as np
+        import cryptography_gb300 as g
+        from cryptography_gb300 import cudart
+        g.init(16)
+        rng = np.random.default_rng(77)
+        n = 5000
+        A = [rng.integers(0, 1 << 32, int(rng.integers(1, 16)), dtype=np.uint64).astype(np.uint32) for _ in range(n)]
+        B = [rng.integers(0, 1 << 32, int(rng.integers(1, 16)), dtype=np.uint64).astype(np.uint32) for _ in range(n)]
+        bufs = []
+        def up(a):
+            b = cudart.DeviceBuffer(max(4, 4 * len(a))); b.upload(a); bufs.append(b); return b
+        da = [up(a) for a in A]; db = [up(b) for b in B]
+        dc = [cudart.DeviceBuffer(4 * (len(a) + len(b))) for a, b in zip(A, B)]
+        g.batch_mul_device([c.ptr for c in dc], [x.ptr for x in da], [len(a) for a in A],
+                           [x.ptr for x in db], [len(b) for b in B])
+        cudart.synchronize()
+        ok = all(np.array_equal(c.download(np.uint32, len(a) + len(b)), g.mul(a, b)) for c, a, b in zip(dc, A, B))
+        print(json.dumps([ok, g.device_errors()]))
+    """ % root)
+    r = subprocess.run([sys.executable, "-c", body], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert json.loads(r.stdout.strip().splitlines()[-1]) == [True, 0]
