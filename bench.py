@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--serve-saturation", type=int, default=3000)
     ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--no-e", action="store_true", help="skip the e-digits leg")
+    ap.add_argument("--e-digits", type=int, default=10 ** 8)
+    ap.add_argument("--e-reps", type=int, default=3)
+    ap.add_argument("--e-cpu-digits", type=int, default=10 ** 7, help="CPU baseline sample of the e leg")
     return ap.parse_args()
 
 
@@ -351,6 +355,53 @@ def run_serving_leg(g, cudart, args, stream):
             "load": "0.7 x serial capacity of the plain path (gbntt_mul_u32 + sync per request)"}
 
 
+def run_e_leg(args):
+    """e to args.e_digits digits through gbntt_compute_e (the whole pipeline:
+    product tree, numerator x 10^(D-1), Newton division, decimal conversion;
+    the digit string lands in host memory), checked against the reference's
+    own digits (sha256 in tests/golden/e_digits.json); CPU baseline: the same
+    algorithm on GMP (oracle/e_gmp_oracle.c, one thread) at a bounded
+    sample."""
+    import hashlib
+    from cryptography_gb300 import arith
+    D = args.e_digits
+    gold = {}
+    gp = os.path.join(ROOT, "tests", "golden", "e_digits.json")
+    if os.path.exists(gp):
+        gold = json.load(open(gp)).get(str(D), {})
+    arith.compute_e(min(D, 10 ** 6))   # warm-up
+    runs = []
+    s = None
+    for _ in range(max(1, args.e_reps)):
+        t0 = time.perf_counter()
+        s, ph = arith.compute_e(D, phases=True)
+        runs.append((time.perf_counter() - t0, ph))
+    best = min(runs, key=lambda r: r[0])
+    digest = hashlib.sha256(s.encode()).hexdigest()
+    out = {"digits": D, "seconds": best[0], "seconds_all": [r[0] for r in runs],
+           "phases_s": dict(zip(("product_tree", "numerator_x_10pow", "division", "decimal", "total"), best[1])),
+           "sha256": digest, "matches_reference_digits": (digest == gold["sha256"]) if gold else None,
+           "api": "gbntt_compute_e (C ABI), digits to host memory",
+           "engine_transform_log_needed": arith.e_required_log(D)}
+    if gold:
+        out["reference_cpu_recorded"] = {"seconds": gold.get("reference_seconds"), "cores": gold.get("cores"),
+                                         "note": "reference host compute_e (GMP multiply shim) when the digits "
+                                                 "were recorded; other host"}
+    if not args.no_cpu and args.e_cpu_digits > 0:
+        try:
+            from oracle import e_oracle
+            cs, ct = e_oracle.gmp_e_string(args.e_cpu_digits)
+            cg = json.load(open(gp)).get(str(args.e_cpu_digits), {}) if os.path.exists(gp) else {}
+            out["cpu_baseline"] = {"value": ct, "unit": "s", "cores": 1, "kind": "port",
+                                   "sample": "e to %d digits, reference algorithm on GMP (e_gmp_oracle.c)"
+                                             % args.e_cpu_digits,
+                                   "matches_reference_digits": (hashlib.sha256(cs.encode()).hexdigest()
+                                                                == cg.get("sha256")) if cg else None}
+        except Exception as ex:   # the baseline is reported, never required
+            out["cpu_baseline"] = {"error": str(ex)}
+    return out
+
+
 def run_reference(args, dist):
     if dist.rank != 0:
         return 0
@@ -450,6 +501,11 @@ def run_gpu(args, dist):
         serving = run_serving_leg(g, cudart, args, stream)
         flags |= serving["device_error_flags"]
 
+    e_leg = None
+    if not args.no_e and dist.rank == 0:
+        e_leg = run_e_leg(args)
+        flags |= g.device_errors()
+
     # per-launch breakdown of one multiply (separate, instrumented run)
     g.launch_log(True)
     step()
@@ -537,6 +593,7 @@ def run_gpu(args, dist):
         "packed_64bit_coefficients": packed,
         "batched": batched,
         "serving": serving,
+        "e_digits": e_leg,
         "launch_breakdown": by_kind,
         "gpu_launches": launches_per_step * args.steps,
         "device_error_flags": flags,

@@ -35,6 +35,21 @@ def build_oracle(force=False):
     return ORACLE_SO
 
 
+E_ORACLE_SO = os.path.join(HERE, "libeoracle.so")
+
+
+def build_e_oracle(force=False):
+    """Compile e_gmp_oracle.c (the reference's compute_e path on GMP) into
+    oracle/libeoracle.so, linked against the system libgmp.so.10."""
+    src = os.path.join(HERE, "e_gmp_oracle.c")
+    if force or _stale(E_ORACLE_SO, [src, __file__]):
+        tmp = E_ORACLE_SO + ".tmp"
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-Wall", src, "-o", tmp,
+                               "-l:libgmp.so.10", "-lm"])
+        os.replace(tmp, E_ORACLE_SO)
+    return E_ORACLE_SO
+
+
 def reference_available():
     return os.path.isfile(os.path.join(REFERENCE_ROOT, "ntt", "lib", "garner.hip"))
 
@@ -95,5 +110,6 @@ def build_ref_compute_e(force=False):
 
 if __name__ == "__main__":
     print(build_oracle(force=True))
+    print(build_e_oracle(force=True))
     print(build_ref(force=True))
     print(build_ref_compute_e(force=True))

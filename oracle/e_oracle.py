@@ -7,12 +7,41 @@ Plain-Python restatement (small cases) of:
     floor((B + P) 10^(D+20) / B), printed as d0 "." d1..d(D-1)
   * newton_reciprocal    ntt/lib/arith/newton.h:15-23 (the exact floor; the
     reference's may be one below, never above)
+e_gmp_oracle.c restates the same path in C on GMP for large digit counts.
 Pinned by tests/golden/e_digits.json (sha256 of the reference's own printed
 digits, generated by tests/golden/make_e_golden.py from the reference's
 compiled host compute_e). Only tests/ and bench.py's CPU legs use it.
 """
+import ctypes
 import math
 import sys
+
+from . import build as _build
+
+_elib = None
+
+
+def _e_lib():
+    global _elib
+    if _elib is None:
+        L = ctypes.CDLL(_build.build_e_oracle())
+        L.oracle_e_digits.argtypes = [ctypes.c_long, ctypes.c_char_p, ctypes.c_size_t,
+                                      ctypes.POINTER(ctypes.c_double)]
+        L.oracle_e_digits.restype = ctypes.c_int
+        L.oracle_split_terms_needed.argtypes = [ctypes.c_long]
+        L.oracle_split_terms_needed.restype = ctypes.c_long
+        _elib = L
+    return _elib
+
+
+def gmp_e_string(digits):
+    """(string, seconds): the same e string from e_gmp_oracle.c (GMP, one
+    thread) — usable at 10^7..10^8 digits and as the CPU baseline."""
+    buf = ctypes.create_string_buffer(int(digits) + 2)
+    sec = ctypes.c_double(0)
+    if _e_lib().oracle_e_digits(int(digits), buf, int(digits) + 2, ctypes.byref(sec)) != 0:
+        raise RuntimeError("oracle_e_digits failed")
+    return buf.raw[:int(digits) + 1].decode(), sec.value
 
 
 def split_terms_needed(n_digits):

@@ -53,3 +53,10 @@ def test_library_e_required_log(built_lib):
     logs = [arith.e_required_log(d) for d in (1, 1000, 10 ** 6, 10 ** 8)]
     assert logs == sorted(logs) and logs[-1] <= 26
     assert built_lib.gbntt_e_required_log(0) < 0
+
+
+@pytest.mark.parametrize("D", [1000, 100000, 1000000])
+def test_gmp_port_matches_reference_digits(e_gold, D):
+    s, t = eo.gmp_e_string(D)
+    assert hashlib.sha256(s.encode()).hexdigest() == e_gold[str(D)]["sha256"]
+    assert t >= 0
