@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--serve-saturation", type=int, default=3000)
     ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--no-three-prime", action="store_true",
+                    help="skip timing the same multiply with the reference's three 64-bit primes")
+    ap.add_argument("--three-prime-steps", type=int, default=5)
     ap.add_argument("--no-e", action="store_true", help="skip the e-digits leg")
     ap.add_argument("--e-digits", type=int, default=10 ** 8)
     ap.add_argument("--e-reps", type=int, default=3)
@@ -467,6 +470,29 @@ def run_gpu(args, dist):
     total_ms = dist.max(total_ms)
     ms = total_ms / (args.steps * dist.world)
 
+    # the same multiply with the reference's prime set (three 64-bit primes)
+    three = None
+    if not args.no_three_prime and args.three_prime_steps > 0:
+        g.set_prime_set(3)
+        try:
+            for _ in range(2):
+                step()
+            t0, t1 = cudart.Event(), cudart.Event()
+            dist.barrier()
+            t0.record(stream)
+            for _ in range(args.three_prime_steps):
+                step()
+            t1.record(stream)
+            t1.synchronize()
+            dist.barrier()
+            tms = dist.max(t0.elapsed_ms(t1)) / (args.three_prime_steps * dist.world)
+        finally:
+            g.set_prime_set(2)
+        flags |= g.device_errors()
+        three = {"ms": tms, "steps": args.three_prime_steps,
+                 "primes": "2^64-2^b+1, b = 32, 34, 40 (the reference's set; 64-bit residues)",
+                 "note": "same product, same transform length; the headline uses two primes"}
+
     # packed mode (one 64-bit limb per coefficient, transform length 2^lg)
     packed = None
     if not args.no_packed:
@@ -536,6 +562,8 @@ def run_gpu(args, dist):
         except (ValueError, OSError):
             traffic = None
     bm = bytes_model(lg)
+    res_bytes = 12 if g.prime_set() == 2 else 24
+    bm_own = 10 * (1 << (lg + 1)) * res_bytes + 8 * (2 * n)
 
     # e2e through the reference-facing C ABI with pinned host BigInts
     e2e = None
@@ -578,8 +606,12 @@ def run_gpu(args, dist):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (seeded splitmix64 limbs; inputs resident in HBM)",
-        "config": {"workload": "multiply 2^%d x 2^%d 32-bit limbs, NTT length 2^%d per prime, 3 primes "
-                               "(2^64-2^b+1, b=32,34,40), uint64 residues" % (lg, lg, lg + 1),
+        "config": {"workload": "multiply 2^%d x 2^%d 32-bit limbs, NTT length 2^%d per prime, bit-exact"
+                               % (lg, lg, lg + 1),
+                   "primes": "q0 = 2^64-2^32+1 (uint64 residues) and p3 = 3*2^30+1 (uint32 residues); CRT "
+                             "modulus 2^95.6 > largest coefficient 2^92; the reference's three 64-bit primes "
+                             "are timed in three_prime_64bit" if g.prime_set() == 2 else
+                             "2^64-2^b+1, b = 32, 34, 40 (uint64 residues)",
                    "operand_limbs": n, "transform_log": lg + 1, "passes": g.plan(lg + 1),
                    "l2_policy": "inputs and 24 GiB spectra >> 129 MB L2; no flush", "parallelism": "replicas"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -589,7 +621,12 @@ def run_gpu(args, dist):
         "multiply_roofline": {"bytes_model": bm, "achieved_GBps": bm / (ms * 1e-3) / 1e9,
                               "frac": bm / (ms * 1e-3) / 1e9 / peak,
                               "model": "10*k*N*8 + 8*(n_a+n_b), k=3 (2-pass four-step with fused decomposition, "
-                                       "pointwise product and Garner+carry)"},
+                                       "pointwise product and Garner+carry)",
+                              "bytes_model_own_primes": bm_own,
+                              "frac_own_primes": bm_own / (ms * 1e-3) / 1e9 / peak,
+                              "model_own_primes": "the same model with this run's residue words "
+                                                  "(%d bytes per coefficient over all primes)" % res_bytes},
+        "three_prime_64bit": three,
         "packed_64bit_coefficients": packed,
         "batched": batched,
         "serving": serving,

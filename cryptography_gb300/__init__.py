@@ -37,6 +37,8 @@ from .engine import (  # noqa: F401
     mul_device,
     mul64,
     set_coeff_bits,
+    set_prime_set,
+    prime_set,
     plan,
     set_plan,
     sqr,

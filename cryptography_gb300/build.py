@@ -16,7 +16,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbntt.so")
 
-SOURCES = ["gbntt_pass_p0.cu", "gbntt_pass_p1.cu", "gbntt_pass_p2.cu", "gbntt_kernels.cu", "gbntt_engine.cu", "gbntt_noalloc.cu",
+SOURCES = ["gbntt_pass_p0.cu", "gbntt_pass_p1.cu", "gbntt_pass_p2.cu", "gbntt_pass_p3.cu", "gbntt_kernels.cu", "gbntt_engine.cu", "gbntt_noalloc.cu",
            "gbntt_e.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -32,6 +32,8 @@ def _flags():
     extra = []
     if os.environ.get("GBNTT_PASS_MIN_BLOCKS"):   # tuning knob: resident CTAs per SM of the pass kernels
         extra.append("-DGBNTT_PASS_MIN_BLOCKS=%d" % int(os.environ["GBNTT_PASS_MIN_BLOCKS"]))
+    if os.environ.get("GBNTT_PASS_MIN_BLOCKS32"):
+        extra.append("-DGBNTT_PASS_MIN_BLOCKS32=%d" % int(os.environ["GBNTT_PASS_MIN_BLOCKS32"]))
     return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
                    "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr"] + extra
 

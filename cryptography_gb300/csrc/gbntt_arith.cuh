@@ -158,10 +158,115 @@ __device__ __forceinline__ uint64_t mont_mul_ref(uint64_t a, uint64_t b)
     return r;
 }
 
+// ---------------------------------------------------------------------------
+// The 32-bit prime p3 = 3 * 2^30 + 1 (2-adicity 30, the only prime below
+// 2^32 with roots of unity of order 2^29 and 2^30). Together with q0 it
+// gives a CRT modulus q0 p3 ~ 2^95.6, above every coefficient of a product
+// of 32-bit limbs with up to 2^29 limbs in the shorter operand (< 2^93): the
+// 32-bit-coefficient products need only these two primes. p3 > 2^31, so
+// sums need 33 bits; the forms below never form them.
+//   add: a + b = a - (p - b), plus p on borrow.
+//   mul: signed Montgomery, R = 2^32: m = lo(a b) p^-1 mod 2^32 makes
+//        lo(m p) = lo(a b), so (a b - m p) / 2^32 = hi(a b) - hi(m p)
+//        exactly, in (-p, p); add p on borrow. Output canonical.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kP3 = 0xC0000001u;          // 3 * 2^30 + 1
+constexpr uint32_t kP3Inv = 0x40000001u;       // p3^-1 mod 2^32
+constexpr uint32_t kP3Neg = 0x3FFFFFFFu;       // -p3 mod 2^32
+
+__device__ __forceinline__ uint32_t p3_add(uint32_t a, uint32_t b)
+{
+    uint32_t r;
+    asm("{\n\t"
+        ".reg .u32 nb, d, bw;\n\t"
+        "sub.u32 nb, %3, %2;\n\t"
+        "sub.cc.u32 d, %1, nb;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "mad.lo.u32 %0, bw, %4, d;\n\t"
+        "}"
+        : "=r"(r) : "r"(a), "r"(b), "n"(kP3), "n"(kP3Neg));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t p3_sub(uint32_t a, uint32_t b)
+{
+    uint32_t r;
+    asm("{\n\t"
+        ".reg .u32 d, bw;\n\t"
+        "sub.cc.u32 d, %1, %2;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "mad.lo.u32 %0, bw, %3, d;\n\t"
+        "}"
+        : "=r"(r) : "r"(a), "r"(b), "n"(kP3Neg));
+    return r;
+}
+
+// a * b * 2^-32 mod p3 for a < 2^32, b < p3 (then hi(a b) < p3).
+__device__ __forceinline__ uint32_t p3_mul(uint32_t a, uint32_t b)
+{
+    uint32_t r;
+    asm("{\n\t"
+        ".reg .u32 t0, t1, m, h, d, bw;\n\t"
+        ".reg .u64 t;\n\t"
+        "mul.wide.u32 t, %1, %2;\n\t"
+        "mov.b64 {t0, t1}, t;\n\t"
+        "mul.lo.u32 m, t0, %3;\n\t"
+        "mul.hi.u32 h, m, %4;\n\t"
+        "sub.cc.u32 d, t1, h;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "mad.lo.u32 %0, bw, %5, d;\n\t"
+        "}"
+        : "=r"(r) : "r"(a), "r"(b), "n"(kP3Inv), "n"(kP3), "n"(kP3Neg));
+    return r;
+}
+
+// plain C++ forms for the device self-test
+__device__ __forceinline__ uint32_t p3_add_ref(uint32_t a, uint32_t b)
+{
+    const uint64_t s = (uint64_t)a + b;
+    return (uint32_t)(s >= kP3 ? s - kP3 : s);
+}
+__device__ __forceinline__ uint32_t p3_sub_ref(uint32_t a, uint32_t b) { return a >= b ? a - b : a + (kP3 - b); }
+__device__ __forceinline__ uint32_t p3_mul_ref(uint32_t a, uint32_t b)
+{
+    // a b 2^-32 mod p3 through the 64-bit remainder and 2^-32 mod p3
+    const uint64_t t = (uint64_t)a * b % kP3;
+    constexpr uint64_t kRinv = 0x90000000ull;   // 2^-32 mod p3
+    return (uint32_t)(t * kRinv % kP3);
+}
+
+// ---------------------------------------------------------------------------
+// Field policies for the pass kernels: prime index PI -> residue word T,
+// slot in the per-launch argument arrays, and the three operations. Primes
+// 0..2 are the 64-bit Montgomery primes above (slots 0..2); prime 3 is p3
+// (slot 1: it sits beside q0 in the two-prime set).
+// ---------------------------------------------------------------------------
+template <int PI>
+struct Field {
+    typedef uint64_t T;
+    static constexpr int SLOT = PI;
+    static constexpr uint64_t P = Prime<PI>::P;
+    static __device__ __forceinline__ T add(T a, T b) { return add_mod<PI>(a, b); }
+    static __device__ __forceinline__ T sub(T a, T b) { return sub_mod<PI>(a, b); }
+    static __device__ __forceinline__ T mul(T a, T b) { return mont_mul<PI>(a, b); }
+    static __device__ __forceinline__ T from_u32(uint32_t v) { return v; }   // v < 2^32 < p
+};
+template <>
+struct Field<3> {
+    typedef uint32_t T;
+    static constexpr int SLOT = 1;
+    static constexpr uint64_t P = kP3;
+    static __device__ __forceinline__ T add(T a, T b) { return p3_add(a, b); }
+    static __device__ __forceinline__ T sub(T a, T b) { return p3_sub(a, b); }
+    static __device__ __forceinline__ T mul(T a, T b) { return p3_mul(a, b); }
+    static __device__ __forceinline__ T from_u32(uint32_t v) { return v >= kP3 ? v - kP3 : v; }   // 2^32 < 2 p3
+};
+
 // Runtime prime dispatch helpers used by host-side tables.
 __host__ __device__ inline uint64_t prime_value(int pi)
 {
-    return pi == 0 ? 0xFFFFFFFF00000001ull : (pi == 1 ? 0xFFFFFFFC00000001ull : 0xFFFFFF0000000001ull);
+    return pi == 0 ? 0xFFFFFFFF00000001ull
+                   : (pi == 1 ? 0xFFFFFFFC00000001ull : (pi == 2 ? 0xFFFFFF0000000001ull : (uint64_t)kP3));
 }
 __host__ __device__ inline int prime_b(int pi) { return pi == 0 ? 32 : (pi == 1 ? 34 : 40); }
 

@@ -46,6 +46,19 @@ static uint64_t h_pow(uint64_t b, uint64_t e, uint64_t p)
 static uint64_t h_inv(uint64_t a, uint64_t p) { return h_pow(a % p, p - 2, p); }
 static uint64_t h_mont(uint64_t x, uint64_t p) { return (uint64_t)(((u128)(x % p) << 64) % p); }
 static const uint64_t kGen[3] = {7, 10, 19};   // reference PRIM_ROOT[0, 2, 3]
+static const uint64_t kGen3 = 5;                 // primitive root of p3 = 3 * 2^30 + 1
+static uint32_t h_mont3(uint64_t x) { return (uint32_t)(((x % kP3) << 32) % kP3); }   // x 2^32 mod p3
+
+// Prime sets. Two primes (q0 with 64-bit residues, p3 with 32-bit residues)
+// carry every product of 32-bit coefficients: q0 p3 ~ 2^95.6 exceeds the
+// largest coefficient (< 2^93). The reference's three 64-bit primes stay
+// for 64-bit coefficients (packed mode, bound 2^158) and on request.
+struct PrimeSet {
+    int n;
+    int pi[3];
+};
+static const PrimeSet kSet2 = {2, {0, 3, 0}};
+static const PrimeSet kSet3 = {3, {0, 1, 2}};
 
 struct Engine {
     bool ready = false;
@@ -53,6 +66,9 @@ struct Engine {
     size_t n_max = 0;
     uint64_t *d_spec = nullptr;     // 6 x n_max: spectra of operand A (3) then B (3)
     uint64_t *d_tw = nullptr;       // [prime][dir][hi|lo][2^15]
+    uint32_t *d_tw3 = nullptr;      // p3: [dir][hi|lo][2^15]
+    int prime_set = 2;              // primes used for 32-bit coefficients: 2 or 3
+    uint64_t garner2[2] = {0, 0};   // two-prime Garner constants (p3 Montgomery multipliers)
     unsigned *d_ctl = nullptr;      // [0] ticket, [1] error, [2..] tile status
     size_t n_status = 0;
     uint32_t *d_io = nullptr;       // staging for host-pointer calls
@@ -74,7 +90,7 @@ struct Engine {
 
 static Engine g;
 // Montgomery forms of w_64^i per prime and direction (kernel arguments).
-static uint64_t g_w64[3][2][64];
+static uint64_t g_w64[4][2][64];
 
 static cudaError_t launch_pass_any(int pi, int log_l, int dir, int ld, PassArgs &a, cudaStream_t st)
 {
@@ -82,7 +98,8 @@ static cudaError_t launch_pass_any(int pi, int log_l, int dir, int ld, PassArgs 
     switch (pi) {
     case 0: return launch_pass_prime<0>(log_l, dir, ld, a, st);
     case 1: return launch_pass_prime<1>(log_l, dir, ld, a, st);
-    default: return launch_pass_prime<2>(log_l, dir, ld, a, st);
+    case 2: return launch_pass_prime<2>(log_l, dir, ld, a, st);
+    default: return launch_pass_prime<3>(log_l, dir, ld, a, st);
     }
 }
 static std::recursive_mutex g_mu;
@@ -162,7 +179,10 @@ int plan_passes(int log_n, int *p)
     }
     if (log_n <= kMaxPassLog) { p[0] = log_n; return 1; }
     if (log_n <= 2 * kMaxPassLog) { p[0] = (log_n + 1) / 2; p[1] = log_n / 2; return 2; }
-    p[0] = (log_n + 2) / 3;
+    // smallest pass first: the first forward pass reads 32-bit limbs down
+    // columns, and a 2^9-point pass moves 8 adjacent columns (32 bytes) per
+    // row instead of 4 (measured 2^29: [9, 10, 10] 95 ms, [10, 10, 9] 99 ms)
+    p[0] = log_n / 3;
     const int rest = log_n - p[0];
     p[1] = (rest + 1) / 2;
     p[2] = rest / 2;
@@ -196,7 +216,7 @@ static size_t workspace_bytes(int max_log)
 {
     const size_t n = (size_t)1 << max_log;
     const size_t spec = 6 * n * sizeof(uint64_t);
-    const size_t tw = 3 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t);
+    const size_t tw = 3 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t) + 2 * 2 * (size_t)kTwSize * sizeof(uint32_t);
     const size_t ctl = (2 + status_words(n)) * sizeof(unsigned);
     const size_t io = (4 * n + 64) * sizeof(uint32_t);
     return spec + tw + ctl + io;
@@ -210,6 +230,7 @@ static void free_all()
     for (int i = 0; i < 2; i++) if (g.btab_ev[i]) cudaEventDestroy(g.btab_ev[i]);
     cudaFree(g.d_spec);
     cudaFree(g.d_tw);
+    cudaFree(g.d_tw3);
     cudaFree(g.d_ctl);
     cudaFree(g.d_io);
     if (g.stream) cudaStreamDestroy(g.stream);
@@ -229,7 +250,8 @@ static int init_impl(int max_log)
     g.n_max = (size_t)1 << max_log;
     CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
     if (cudaMalloc(&g.d_spec, 6 * g.n_max * sizeof(uint64_t)) != cudaSuccess ||
-        cudaMalloc(&g.d_tw, 3 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t)) != cudaSuccess) {
+        cudaMalloc(&g.d_tw, 3 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t)) != cudaSuccess ||
+        cudaMalloc(&g.d_tw3, 2 * 2 * (size_t)kTwSize * sizeof(uint32_t)) != cudaSuccess) {
         set_err("gbntt_init: device allocation of %zu bytes failed", workspace_bytes(max_log));
         cudaGetLastError();
         free_all();
@@ -258,7 +280,7 @@ static int init_impl(int max_log)
     const size_t tw_words = 3 * 2 * 2 * (size_t)kTwSize;
     uint64_t *h = (uint64_t *)malloc(tw_words * sizeof(uint64_t));
     if (!h) { set_err("gbntt_init: host allocation failed"); free_all(); return GBNTT_ERR_ALLOC; }
-    uint64_t (&w64)[3][2][64] = g_w64;
+    uint64_t (&w64)[4][2][64] = g_w64;
     for (int pi = 0; pi < 3; pi++) {
         const uint64_t p = prime_value(pi);
         const uint64_t w = h_pow(kGen[pi], (p - 1) >> kMaxLog, p);
@@ -282,6 +304,34 @@ static int init_impl(int max_log)
     cudaError_t e = cudaMemcpy(g.d_tw, h, tw_words * sizeof(uint64_t), cudaMemcpyHostToDevice);
     free(h);
     if (e != cudaSuccess) { set_err("gbntt_init: twiddle upload failed: %s", cudaGetErrorString(e)); free_all(); return GBNTT_ERR_CUDA; }
+    {
+        // p3: the same two-level tables in its Montgomery form (R = 2^32)
+        std::vector<uint32_t> h3(2 * 2 * (size_t)kTwSize);
+        const uint64_t p = kP3;
+        const uint64_t w = h_pow(kGen3, (p - 1) >> kMaxLog, p);
+        for (int dir = 0; dir < 2; dir++) {
+            const uint64_t wd = dir ? h_inv(w, p) : w;
+            uint32_t *hi = h3.data() + ((size_t)dir * 2 + 0) * kTwSize;
+            uint32_t *lo = h3.data() + ((size_t)dir * 2 + 1) * kTwSize;
+            const uint64_t wbig = h_pow(wd, (uint64_t)kTwSize, p);
+            uint64_t x = 1, y = 1;
+            for (int i = 0; i < kTwSize; i++) {
+                lo[i] = h_mont3(x);
+                hi[i] = h_mont3(y);
+                x = h_mul(x, wd, p);
+                y = h_mul(y, wbig, p);
+            }
+            const uint64_t r64 = h_pow(wd, (uint64_t)1 << (kMaxLog - 6), p);
+            uint64_t z = 1;
+            for (int i = 0; i < 64; i++) { w64[3][dir][i] = h_mont3(z); z = h_mul(z, r64, p); }
+        }
+        e = cudaMemcpy(g.d_tw3, h3.data(), h3.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { set_err("gbntt_init: twiddle upload failed: %s", cudaGetErrorString(e)); free_all(); return GBNTT_ERR_CUDA; }
+        // two-prime Garner: q0^-1 mod p3 and 2^64 mod p3 as p3 Montgomery multipliers
+        const uint64_t q0 = prime_value(0);
+        g.garner2[0] = h_mont3(h_inv(q0 % p, p));
+        g.garner2[1] = (uint64_t)(((u128)1 << 64) % p);
+    }
 
     // Garner constants (Montgomery forms):
     //   [0] q0^-1 mod q1, [1] q0 mod q2, [2] (q0 q1)^-1 mod q2.
@@ -298,45 +348,61 @@ static int init_impl(int max_log)
     {
         const char *cb = getenv("GBNTT_COEFF_BITS");
         g.bigint_coeff_bits = (cb && atoi(cb) == 64) ? 64 : 32;
+        const char *ps = getenv("GBNTT_PRIMES");
+        g.prime_set = (ps && atoi(ps) == 3) ? 3 : 2;
     }
     g.ready = true;
     return GBNTT_OK;
 }
 
-static TwTables tables(int dir)
+static TwTables tables(const PrimeSet &ps, int dir)
 {
     TwTables t;
-    for (int pi = 0; pi < 3; pi++) { t.hi[pi] = tw_ptr(pi, dir, 0); t.lo[pi] = tw_ptr(pi, dir, 1); }
+    memset(&t, 0, sizeof t);
+    for (int k = 0; k < ps.n; k++) {
+        const int pi = ps.pi[k];
+        if (pi < 3) {
+            t.hi[k] = tw_ptr(pi, dir, 0);
+            t.lo[k] = tw_ptr(pi, dir, 1);
+        } else {
+            t.hi[k] = (const uint64_t *)(g.d_tw3 + ((size_t)dir * 2 + 0) * kTwSize);
+            t.lo[k] = (const uint64_t *)(g.d_tw3 + ((size_t)dir * 2 + 1) * kTwSize);
+        }
+    }
     return t;
 }
 
-// Forward transform of one operand: limbs -> 3 spectra at spec[pi * stride].
-static int forward(uint64_t *spec, size_t stride, const void *limbs, size_t n, int L, cudaStream_t st,
-                   bool packed = false, long long W = 1, const uint32_t *const *limb_tab = nullptr,
+static const PrimeSet &coef32_set() { return g.prime_set == 3 ? kSet3 : kSet2; }
+static double word_bytes(int pi) { return pi == 3 ? 4.0 : 8.0; }
+
+// Forward transform of one operand: limbs -> one spectrum per prime of the
+// set at spec[k * stride] (k = slot; p3's 32-bit words fill half a slot).
+static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void *limbs, size_t n, int L,
+                   cudaStream_t st, bool packed = false, long long W = 1, const uint32_t *const *limb_tab = nullptr,
                    const long long *len_tab = nullptr)
 {
     int pl[3];
     const int np = plan_passes(L, pl);
     PassArgs a;
     memset(&a, 0, sizeof a);
-    for (int pi = 0; pi < 3; pi++) a.data[pi] = spec + pi * stride;
+    for (int k = 0; k < ps.n; k++) a.data[k] = spec + k * stride;
     a.limbs = packed ? nullptr : (const uint32_t *)limbs;
     a.limbs64 = packed ? (const uint64_t *)limbs : nullptr;
     a.n_limbs = (long long)n;
     a.limb_tab = limb_tab;
     a.len_tab = len_tab;
     a.log_n_prod = L;
-    a.tw = tables(0);
+    a.tw = tables(ps, 0);
     int log_m = L;
     for (int i = 0; i < np; i++) {
         a.log_m = log_m;
         a.log_s = log_m - pl[i];
         a.ncols = W << (L - pl[i]);
         a.twiddle = a.log_s > 0;
-        const double nb8 = 8.0 * (double)((size_t)1 << L) * (double)W;
-        for (int pi = 0; pi < 3; pi++) {
-            rec_begin(st, i == 0 ? 0 : 1, pl[i], i == 0 ? (packed ? 8.0 : 4.0) * (double)n + nb8 : 2.0 * nb8);
-            CK(launch_pass_any(pi, pl[i], 0, i == 0 ? (packed ? LD_U64LIMB : LD_U32) : LD_U64, a, st));
+        for (int k = 0; k < ps.n; k++) {
+            const double nbw = word_bytes(ps.pi[k]) * (double)((size_t)1 << L) * (double)W;
+            rec_begin(st, i == 0 ? 0 : 1, pl[i], i == 0 ? (packed ? 8.0 : 4.0) * (double)n + nbw : 2.0 * nbw);
+            CK(launch_pass_any(ps.pi[k], pl[i], 0, i == 0 ? (packed ? LD_U64LIMB : LD_U32) : LD_U64, a, st));
             rec_end(st);
         }
         log_m -= pl[i];
@@ -345,23 +411,24 @@ static int forward(uint64_t *spec, size_t stride, const void *limbs, size_t n, i
 }
 
 // Pointwise product of the spectra and inverse transform, in place in specA.
-static int inverse(uint64_t *specA, const uint64_t *specB, size_t stride, int L, cudaStream_t st, bool square,
-                   long long W = 1)
+static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, size_t stride, int L,
+                   cudaStream_t st, bool square, long long W = 1)
 {
     int pl[3];
     const int np = plan_passes(L, pl);
     PassArgs a;
     memset(&a, 0, sizeof a);
-    for (int pi = 0; pi < 3; pi++) {
-        a.data[pi] = specA + pi * stride;
-        a.other[pi] = specB + pi * stride;
+    for (int k = 0; k < ps.n; k++) {
+        const int pi = ps.pi[k];
+        a.data[k] = specA + k * stride;
+        a.other[k] = specB + k * stride;
         // N^-1 * R^2: with the R^-1 left by the Montgomery pointwise product
         // the inverse output is scaled by exactly N^-1.
         const uint64_t p = prime_value(pi);
         const uint64_t ninv = h_inv(((uint64_t)1 << L) % p, p);
-        a.scale[pi] = h_mont(h_mont(ninv, p), p);
+        a.scale[k] = pi < 3 ? h_mont(h_mont(ninv, p), p) : (uint64_t)h_mont3(h_mont3(ninv));
     }
-    a.tw = tables(1);
+    a.tw = tables(ps, 1);
     int log_ms[3];
     int log_m = L;
     for (int i = 0; i < np; i++) { log_ms[i] = log_m; log_m -= pl[i]; }
@@ -371,33 +438,48 @@ static int inverse(uint64_t *specA, const uint64_t *specB, size_t stride, int L,
         a.ncols = W << (L - pl[i]);
         a.twiddle = a.log_s > 0;
         a.use_scale = (i == 0);
-        const double nb8 = 8.0 * (double)((size_t)1 << L) * (double)W;
         const bool first = (i == np - 1);
-        for (int pi = 0; pi < 3; pi++) {
-            rec_begin(st, first ? 2 : 3, pl[i], first ? (square ? 2.0 : 3.0) * nb8 : 2.0 * nb8);
-            CK(launch_pass_any(pi, pl[i], 1, first ? LD_PW : LD_U64, a, st));
+        for (int k = 0; k < ps.n; k++) {
+            const double nbw = word_bytes(ps.pi[k]) * (double)((size_t)1 << L) * (double)W;
+            rec_begin(st, first ? 2 : 3, pl[i], first ? (square ? 2.0 : 3.0) * nbw : 2.0 * nbw);
+            CK(launch_pass_any(ps.pi[k], pl[i], 1, first ? LD_PW : LD_U64, a, st));
             rec_end(st);
         }
     }
     return GBNTT_OK;
 }
 
-static int carry(uint32_t *d_c, size_t n_out, const uint64_t *specA, size_t stride, int L, cudaStream_t st)
+// Garner constants and residue pointers of a prime set into c.
+static void carry_setup(CarryArgs &c, const PrimeSet &ps, const uint64_t *specA, size_t stride)
+{
+    for (int k = 0; k < ps.n; k++) c.res[k] = specA + k * stride;
+    c.mixed = ps.n == 2 ? 1 : 0;
+    if (c.mixed) {
+        c.garner[0] = g.garner2[0];
+        c.garner[1] = g.garner2[1];
+    } else {
+        for (int i = 0; i < 4; i++) c.garner[i] = g.garner[i];
+    }
+}
+
+static int carry(const PrimeSet &ps, uint32_t *d_c, size_t n_out, const uint64_t *specA, size_t stride, int L,
+                 cudaStream_t st)
 {
     CarryArgs c;
     memset(&c, 0, sizeof c);
-    for (int pi = 0; pi < 3; pi++) c.res[pi] = specA + pi * stride;
+    carry_setup(c, ps, specA, stride);
     c.out = d_c;
     c.n_coef = (long long)1 << L;
     c.n_out = (long long)n_out;
     c.ticket = g.d_ctl;
     c.error = g.d_ctl + 1;
     c.status = g.d_ctl + 2;
-    for (int i = 0; i < 4; i++) c.garner[i] = g.garner[i];
     const long long nt = carry_tiles((long long)n_out);
     CK(cudaMemsetAsync(g.d_ctl, 0, sizeof(unsigned), st));
     CK(cudaMemsetAsync(g.d_ctl + 2, 0, (size_t)nt * sizeof(unsigned), st));
-    rec_begin(st, 4, 0, 3.0 * 8.0 * (double)((size_t)1 << L) + 4.0 * (double)n_out);
+    double rb = 0;
+    for (int k = 0; k < ps.n; k++) rb += word_bytes(ps.pi[k]);
+    rec_begin(st, 4, 0, rb * (double)((size_t)1 << L) + 4.0 * (double)n_out);
     CK(launch_garner_carry(c, st, nullptr));
     rec_end(st);
     return GBNTT_OK;
@@ -420,15 +502,16 @@ static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t
     const bool square = (d_a == d_b && na == nb);
     uint64_t *specA = g.d_spec;
     uint64_t *specB = g.d_spec + 3 * g.n_max;
-    int rc = forward(specA, g.n_max, d_a, na, L, st);
+    const PrimeSet &ps = coef32_set();
+    int rc = forward(ps, specA, g.n_max, d_a, na, L, st);
     if (rc) return rc;
     if (!square) {
-        rc = forward(specB, g.n_max, d_b, nb, L, st);
+        rc = forward(ps, specB, g.n_max, d_b, nb, L, st);
         if (rc) return rc;
     }
-    rc = inverse(specA, square ? specA : specB, g.n_max, L, st, square);
+    rc = inverse(ps, specA, square ? specA : specB, g.n_max, L, st, square);
     if (rc) return rc;
-    return carry(d_c, n_out, specA, g.n_max, L, st);
+    return carry(ps, d_c, n_out, specA, g.n_max, L, st);
 }
 
 static int carry64(uint64_t *d_c, size_t n_out, const uint64_t *specA, size_t stride, int L, cudaStream_t st)
@@ -473,13 +556,13 @@ static int mul_dev64(uint64_t *d_c, const uint64_t *d_a, size_t na, const uint64
     const bool square = (d_a == d_b && na == nb);
     uint64_t *specA = g.d_spec;
     uint64_t *specB = g.d_spec + 3 * g.n_max;
-    int rc = forward(specA, g.n_max, d_a, na, L, st, true);
+    int rc = forward(kSet3, specA, g.n_max, d_a, na, L, st, true);
     if (rc) return rc;
     if (!square) {
-        rc = forward(specB, g.n_max, d_b, nb, L, st, true);
+        rc = forward(kSet3, specB, g.n_max, d_b, nb, L, st, true);
         if (rc) return rc;
     }
-    rc = inverse(specA, square ? specA : specB, g.n_max, L, st, square);
+    rc = inverse(kSet3, specA, square ? specA : specB, g.n_max, L, st, square);
     if (rc) return rc;
     return carry64(d_c, n_out, specA, g.n_max, L, st);
 }
@@ -536,21 +619,21 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
     CK(cudaEventRecord(x.btab_ev[slot], st));
     *x.slot = slot ^ 1;
     uint64_t *specA = x.spec, *specB = x.spec + 3 * x.cap;
-    int rc = forward(specA, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab),
+    const PrimeSet &ps = coef32_set();
+    int rc = forward(ps, specA, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab),
                      (const long long *)(dtab + W));
     if (rc) return rc;
-    rc = forward(specB, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab + 2 * W),
+    rc = forward(ps, specB, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab + 2 * W),
                  (const long long *)(dtab + 3 * W));
     if (rc) return rc;
-    rc = inverse(specA, specB, x.cap, L, st, false, W);
+    rc = inverse(ps, specA, specB, x.cap, L, st, false, W);
     if (rc) return rc;
     CarryArgs c;
     memset(&c, 0, sizeof c);
-    for (int pi = 0; pi < 3; pi++) c.res[pi] = specA + pi * x.cap;
+    carry_setup(c, ps, specA, x.cap);
     c.ticket = x.ctl;
     c.error = x.ctl + 1;
     c.status = x.ctl + 2;
-    for (int q = 0; q < 4; q++) c.garner[q] = g.garner[q];
     c.tile_start = (const long long *)(dtab + 6 * W);
     c.out_tab = (uint32_t *const *)(dtab + 4 * W);
     c.nout_tab = (const long long *)(dtab + 5 * W);
@@ -558,7 +641,9 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
     c.log_n_prod = L;
     CK(cudaMemsetAsync(x.ctl, 0, sizeof(unsigned), st));
     CK(cudaMemsetAsync(x.ctl + 2, 0, (size_t)tiles * sizeof(unsigned), st));
-    rec_begin(st, 4, 0, (3.0 * 8.0 * (double)((size_t)1 << L) + 4.0 * (double)(1 << L)) * (double)W);
+    double rb = 0;
+    for (int k = 0; k < ps.n; k++) rb += word_bytes(ps.pi[k]);
+    rec_begin(st, 4, 0, (rb * (double)((size_t)1 << L) + 4.0 * (double)(1 << L)) * (double)W);
     CK(launch_garner_carry_batch(c, tiles, st));
     rec_end(st);
     return GBNTT_OK;
@@ -961,7 +1046,7 @@ int gbntt_set_plan(int log_n, int npasses, const int *passes)
 int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t n,
                        void *stream)
 {
-    if (prime < 0 || prime > 2 || op < 0 || op > 5) { set_err("gbntt_debug_modops: bad prime/op"); return GBNTT_ERR_ARG; }
+    if (prime < 0 || prime > 3 || op < 0 || op > 5) { set_err("gbntt_debug_modops: bad prime/op"); return GBNTT_ERR_ARG; }
     cudaStream_t st = stream ? (cudaStream_t)stream : (g.ready ? g.stream : (cudaStream_t)0);
     CK(launch_modops(prime, op, d_a, d_b, d_out, (long long)n, st));
     return GBNTT_OK;
@@ -1032,6 +1117,18 @@ int gbntt_mul_u64_host(uint64_t *c, const uint64_t *a, size_t na, const uint64_t
     if (!c || (na && !a) || (nb && !b)) { set_err("null pointer"); return GBNTT_ERR_ARG; }
     return mul_host64(c, a, na, b, nb, nullptr, nullptr);
 }
+
+int gbntt_set_prime_set(int nprimes)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (nprimes != 2 && nprimes != 3) { set_err("gbntt_set_prime_set: 2 or 3 primes"); return GBNTT_ERR_ARG; }
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    cudaStreamSynchronize(g.stream);
+    g.prime_set = nprimes;
+    return GBNTT_OK;
+}
+
+int gbntt_prime_set(void) { return g.ready ? g.prime_set : 0; }
 
 int gbntt_set_coeff_bits(int bits)
 {
@@ -1196,7 +1293,7 @@ int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log
     if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
     if (log_n < kMinLog || log_n > g.max_log || n > ((size_t)1 << log_n)) { set_err("bad size"); return GBNTT_ERR_ARG; }
     cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
-    return forward(d_out, (size_t)1 << log_n, d_in, n, log_n, st);
+    return forward(kSet3, d_out, (size_t)1 << log_n, d_in, n, log_n, st);
 }
 
 // ---- reference-compatible entry points --------------------------------------

@@ -63,6 +63,7 @@ struct CarryArgs {
     const long long *nout_tab;
     int nprod;
     int log_n_prod;
+    int mixed;                  // two-prime set: res[0] q0 (64-bit), res[1] p3 (32-bit words)
 };
 
 enum ErrorBits : unsigned int {

@@ -43,6 +43,20 @@ __global__ void modops_kernel(int prime, int op, const uint64_t *a, const uint64
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t x = a[i], y = b[i];
+    if (prime == 3) {   // the 32-bit prime (operands in the low words)
+        const uint32_t u = (uint32_t)x, v = (uint32_t)y;
+        uint32_t r;
+        switch (op) {
+        case 0: r = p3_add(u, v); break;
+        case 1: r = p3_sub(u, v); break;
+        case 2: r = p3_mul(u, v); break;
+        case 3: r = p3_add_ref(u, v); break;
+        case 4: r = p3_sub_ref(u, v); break;
+        default: r = p3_mul_ref(u, v); break;
+        }
+        out[i] = r;
+        return;
+    }
     out[i] = prime == 0 ? modop<0>(op, x, y) : (prime == 1 ? modop<1>(op, x, y) : modop<2>(op, x, y));
 }
 
@@ -118,7 +132,40 @@ __device__ __forceinline__ void garner_coef(const CarryArgs &a, long long j, uin
     w2 = (uint32_t)hi;
 }
 
-template <bool BATCH>
+typedef unsigned __int128 u128;
+
+// Two-prime form (q0 and the 32-bit p3): c_j = r0 + q0 a1 with
+// a1 = (r1 - r0) q0^-1 mod p3, c_j < q0 p3 < 2^96. garner[0] = q0^-1 mod p3
+// and garner[1] = 2^64 mod p3, both as p3 Montgomery multipliers. A true
+// coefficient is below N 2^64 (N = the transform length, above the shorter
+// operand's limb count): a larger top word means corrupted residues.
+__device__ __forceinline__ void garner_coef2(const CarryArgs &a, long long j, uint32_t &w0, uint32_t &w1,
+                                             uint32_t &w2, unsigned &err)
+{
+    if (j < 0 || j >= a.n_coef) { w0 = w1 = w2 = 0; return; }
+    constexpr uint64_t q0 = Prime<0>::P;
+    const uint64_t r0 = a.res[0][j];
+    const uint32_t r1 = ((const uint32_t *)a.res[1])[j];
+    const uint32_t lo = (uint32_t)r0;
+    const uint32_t r0m = p3_add(p3_mul((uint32_t)(r0 >> 32), (uint32_t)a.garner[1]), lo >= kP3 ? lo - kP3 : lo);
+    const uint32_t a1 = p3_mul(p3_sub(r1, r0m), (uint32_t)a.garner[0]);
+    const u128 c = (u128)a1 * q0 + r0;
+    w0 = (uint32_t)c;
+    w1 = (uint32_t)(c >> 32);
+    const uint64_t top = (uint64_t)(c >> 64);
+    w2 = (uint32_t)top;
+    if (top >= (uint64_t)a.n_coef) err |= ERR_GARNER_DIGIT;
+}
+
+template <bool MIXED>
+__device__ __forceinline__ void garner_any(const CarryArgs &a, long long j, uint32_t &w0, uint32_t &w1, uint32_t &w2,
+                                           unsigned &err)
+{
+    if (MIXED) garner_coef2(a, j, w0, w1, w2, err);
+    else garner_coef(a, j, w0, w1, w2, err);
+}
+
+template <bool BATCH, bool MIXED>
 __global__ void __launch_bounds__(kCarryThreads) garner_carry_kernel_t(CarryArgs a)
 {
     constexpr int T = kCarryThreads, K = kCarryPerThread, TILE = kCarryTile;
@@ -147,7 +194,12 @@ __global__ void __launch_bounds__(kCarryThreads) garner_carry_kernel_t(CarryArgs
         if (s_prod < 0) return;
         const long long b = s_prod;
         const long long off = b << a.log_n_prod;
-        for (int pi = 0; pi < 3; pi++) a.res[pi] += off;
+        if (MIXED) {
+            a.res[0] += off;
+            a.res[1] = (const uint64_t *)((const uint32_t *)a.res[1] + off);
+        } else {
+            for (int pi = 0; pi < 3; pi++) a.res[pi] += off;
+        }
         a.out = a.out_tab[b];
         a.n_out = a.nout_tab[b];
         a.n_coef = 1LL << a.log_n_prod;
@@ -162,12 +214,12 @@ __global__ void __launch_bounds__(kCarryThreads) garner_carry_kernel_t(CarryArgs
     for (int r = 0; r < K; r++) {
         const int q = r * T + tid;
         uint32_t w0, w1, w2;
-        garner_coef(a, base + q, w0, w1, w2, err);
+        garner_any<MIXED>(a, base + q, w0, w1, w2, err);
         W0[spad(q + 2)] = w0; W1[spad(q + 2)] = w1; W2[spad(q + 2)] = w2;
     }
     if (tid < 2) {
         uint32_t w0, w1, w2;
-        garner_coef(a, base - 2 + tid, w0, w1, w2, err);
+        garner_any<MIXED>(a, base - 2 + tid, w0, w1, w2, err);
         W0[spad(tid)] = w0; W1[spad(tid)] = w1; W2[spad(tid)] = w2;
     }
     __syncthreads();
@@ -254,8 +306,6 @@ constexpr int kCarry64PerThread = 4;
 constexpr int kCarry64Tile = kCarry64Threads * kCarry64PerThread;
 
 long long carry_tiles64(long long n_out) { return (n_out + kCarry64Tile - 1) / kCarry64Tile; }
-
-typedef unsigned __int128 u128;
 
 __device__ __forceinline__ void garner_coef64(const CarryArgs &a, long long j, uint64_t &w0, uint64_t &w1,
                                               uint64_t &w2, unsigned &err)
@@ -390,14 +440,16 @@ cudaError_t launch_garner_carry(const CarryArgs &args, cudaStream_t stream, long
     const long long nt = carry_tiles(args.n_out);
     if (ntiles_out) *ntiles_out = nt;
     if (nt == 0) return cudaSuccess;
-    garner_carry_kernel_t<false><<<(unsigned)nt, kCarryThreads, 0, stream>>>(args);
+    if (args.mixed) garner_carry_kernel_t<false, true><<<(unsigned)nt, kCarryThreads, 0, stream>>>(args);
+    else garner_carry_kernel_t<false, false><<<(unsigned)nt, kCarryThreads, 0, stream>>>(args);
     return cudaGetLastError();
 }
 
 cudaError_t launch_garner_carry_batch(const CarryArgs &args, long long grid_tiles, cudaStream_t stream)
 {
     if (grid_tiles <= 0) return cudaSuccess;
-    garner_carry_kernel_t<true><<<(unsigned)grid_tiles, kCarryThreads, 0, stream>>>(args);
+    if (args.mixed) garner_carry_kernel_t<true, true><<<(unsigned)grid_tiles, kCarryThreads, 0, stream>>>(args);
+    else garner_carry_kernel_t<true, false><<<(unsigned)grid_tiles, kCarryThreads, 0, stream>>>(args);
     return cudaGetLastError();
 }
 

@@ -13,6 +13,10 @@
 // structure with explicit transposes (Bailey four-step,
 // ntt/lib/ntt_kernel.hip:835-925, :1172-1375).
 //
+// The kernels are generic over the prime's field policy (Field<PI> in
+// gbntt_arith.cuh): 64-bit Montgomery residues for q0..q2, 32-bit residues
+// for p3. Argument arrays are indexed by the policy's slot.
+//
 // Inside a CTA (128 threads, G columns): the 2^l-point DFT is A x B with
 // A = 2^ceil(l/2), B = 2^floor(l/2): step 1 runs one A-point register DFT
 // per (column, b), multiplies by w_L^(b k_a), step 2 runs A/B B-point
@@ -33,10 +37,17 @@ enum PassLayout { LAYOUT_STRIDED = 0, LAYOUT_CONTIG = 1 };
 #ifndef GBNTT_PASS_MIN_BLOCKS
 #define GBNTT_PASS_MIN_BLOCKS 5   // resident CTAs per SM the register budget targets (measured best of 3..6)
 #endif
+#ifndef GBNTT_PASS_MIN_BLOCKS32
+#define GBNTT_PASS_MIN_BLOCKS32 8  // the same for the 32-bit prime (measured 5..10 at 2^29: 8 within 1%, no spills of note)
+#endif
+template <int PI>
+struct PassMinBlocks {
+    static constexpr int value = sizeof(typename Field<PI>::T) == 4 ? GBNTT_PASS_MIN_BLOCKS32 : GBNTT_PASS_MIN_BLOCKS;
+};
 constexpr int kPassThreads = 128;
 constexpr int kLogPassThreads = 7;
 
-template <int LOG_L>
+template <int LOG_L, int WORD = 8>
 struct PassShape {
     static constexpr int L = 1 << LOG_L;
     static constexpr int LOG_A = (LOG_L + 1) / 2, LOG_B = LOG_L / 2;
@@ -44,8 +55,8 @@ struct PassShape {
     static constexpr int T = kPassThreads;
     static constexpr int LOG_G = kLogPassThreads - LOG_B;
     static constexpr int G = 1 << LOG_G;          // columns per CTA
-    static constexpr int RS = L + A + 1;          // odd row stride in 8-byte words
-    static constexpr size_t SMEM = (size_t)G * RS * 8;
+    static constexpr int RS = L + A + 1;          // odd row stride in words
+    static constexpr size_t SMEM = (size_t)G * RS * WORD;
 };
 
 __host__ __device__ constexpr int bitrev(int x, int bits)
@@ -57,17 +68,20 @@ __host__ __device__ constexpr int bitrev(int x, int bits)
 
 // w^E from the two-level tables (Montgomery form), E < 2^30.
 template <int PI>
-__device__ __forceinline__ uint64_t tw_exp(const uint64_t *hi, const uint64_t *lo, uint32_t e)
+__device__ __forceinline__ typename Field<PI>::T tw_exp(const typename Field<PI>::T *hi,
+                                                        const typename Field<PI>::T *lo, uint32_t e)
 {
-    return mont_mul<PI>(__ldg(hi + (e >> kTwBits)), __ldg(lo + (e & (kTwSize - 1))));
+    return Field<PI>::mul(__ldg(hi + (e >> kTwBits)), __ldg(lo + (e & (kTwSize - 1))));
 }
 
 // In-register radix-2 DIF DFT of 2^LOG_R points: natural order in,
 // bit-reversed order out (X[k] ends in x[bitrev(k)]). w64 = Montgomery forms
 // of the primitive 64th root's powers.
 template <int PI, int LOG_R>
-__device__ __forceinline__ void dft_reg(uint64_t (&x)[1 << LOG_R], const uint64_t *w64)
+__device__ __forceinline__ void dft_reg(typename Field<PI>::T (&x)[1 << LOG_R], const uint64_t *w64)
 {
+    using F = Field<PI>;
+    using T = typename F::T;
     constexpr int R = 1 << LOG_R;
 #pragma unroll
     for (int s = R / 2; s >= 1; s >>= 1) {
@@ -75,11 +89,11 @@ __device__ __forceinline__ void dft_reg(uint64_t (&x)[1 << LOG_R], const uint64_
         for (int blk = 0; blk < R; blk += 2 * s) {
 #pragma unroll
             for (int i = 0; i < s; i++) {
-                const uint64_t u = x[blk + i], v = x[blk + i + s];
-                x[blk + i] = add_mod<PI>(u, v);
-                const uint64_t d = sub_mod<PI>(u, v);
+                const T u = x[blk + i], v = x[blk + i + s];
+                x[blk + i] = F::add(u, v);
+                const T d = F::sub(u, v);
                 // w_{2s}^i = w_64^(i * 32 / s)
-                x[blk + i + s] = (i == 0) ? d : mont_mul<PI>(d, w64[i * (32 / s)]);
+                x[blk + i + s] = (i == 0) ? d : F::mul(d, (T)w64[i * (32 / s)]);
             }
         }
     }
@@ -92,7 +106,7 @@ template <int PI>
 __device__ __forceinline__ uint64_t limb64_residue(const PassArgs &a, long long addr)
 {
     uint64_t v = addr < a.n_limbs ? __ldg(a.limbs64 + addr) : 0ull;
-    return v >= Prime<PI>::P ? v - Prime<PI>::P : v;
+    return v >= Field<PI>::P ? v - Field<PI>::P : v;
 }
 
 // 32-bit limb of coefficient `addr` (zero beyond the operand): one flat
@@ -107,18 +121,39 @@ __device__ __forceinline__ uint64_t limb32_at(const PassArgs &a, long long addr)
     return addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
 }
 
-template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
-__device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const uint64_t *w64)
+// value of tile element at address addr for the load kind LD
+template <int PI, int LD>
+__device__ __forceinline__ typename Field<PI>::T load_elem(const PassArgs &a, const typename Field<PI>::T *data,
+                                                           const typename Field<PI>::T *other, long long addr)
 {
-    using S_ = PassShape<LOG_L>;
+    using F = Field<PI>;
+    if constexpr (LD == LD_U32) {
+        return F::from_u32((uint32_t)limb32_at(a, addr));
+    } else if constexpr (LD == LD_U64LIMB) {
+        if constexpr (sizeof(typename F::T) == 8) return limb64_residue<PI>(a, addr);
+        else return 0;
+    } else if constexpr (LD == LD_PW) {
+        return F::mul(data[addr], other[addr]);
+    } else {
+        return data[addr];
+    }
+}
+
+template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
+__device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>::T *sm, const uint64_t *w64)
+{
+    using F = Field<PI>;
+    using V = typename F::T;
+    using S_ = PassShape<LOG_L, sizeof(V)>;
     constexpr int L = S_::L, A = S_::A, B = S_::B, LOG_B = S_::LOG_B, G = S_::G, LOG_G = S_::LOG_G;
     constexpr int T = S_::T, RS = S_::RS;
     const int t = threadIdx.x;
     const long long col0 = (long long)blockIdx.x * G;
     const int log_s = a.log_s, log_m = a.log_m;
-    uint64_t *data = a.data[PI];
-    const uint64_t *twhi = a.tw.hi[PI];
-    const uint64_t *twlo = a.tw.lo[PI];
+    V *data = (V *)a.data[F::SLOT];
+    const V *other = (const V *)a.other[F::SLOT];
+    const V *twhi = (const V *)a.tw.hi[F::SLOT];
+    const V *twlo = (const V *)a.tw.lo[F::SLOT];
     const int sh = kMaxLog - log_m;
     // column index within the sub-problem of the first column of this CTA
     const uint64_t j0 = LAYOUT == LAYOUT_STRIDED ? (uint64_t)(col0 & ((1LL << log_s) - 1)) : 0ull;
@@ -129,17 +164,9 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
         const long long S = 1LL << log_s;
         const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
         const long long stepg = (long long)B * S;
-        uint64_t *dst = sm + g * RS + m0;
+        V *dst = sm + g * RS + m0;
 #pragma unroll 8
-        for (int it = 0; it < A; it++) {
-            const long long addr = base + it * stepg;
-            uint64_t v;
-            if (LD == LD_U32) v = limb32_at(a, addr);
-            else if (LD == LD_U64LIMB) v = limb64_residue<PI>(a, addr);
-            else if (LD == LD_PW) v = mont_mul<PI>(data[addr], a.other[PI][addr]);
-            else v = data[addr];
-            dst[it * (B + 1)] = v;
-        }
+        for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
     } else {
         const long long rows_left = a.ncols - col0;
         const long long base = col0 << LOG_L;
@@ -147,14 +174,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
         for (int it = 0; it < A; it++) {
             const int e = t + it * T;
             const int g = e >> LOG_L, m = e & (L - 1);
-            uint64_t v = 0;
-            if (g < rows_left) {
-                const long long addr = base + e;
-                if (LD == LD_U32) v = limb32_at(a, addr);
-                else if (LD == LD_U64LIMB) v = limb64_residue<PI>(a, addr);
-                else if (LD == LD_PW) v = mont_mul<PI>(data[addr], a.other[PI][addr]);
-                else v = data[addr];
-            }
+            V v = 0;
+            if (g < rows_left) v = load_elem<PI, LD>(a, data, other, base + e);
             sm[g * RS + m + (m >> LOG_B)] = v;
         }
     }
@@ -163,27 +184,27 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
     // ---- step 1: one A-point DFT per (g, b) over the high digit
     {
         const int g = t >> LOG_B, b = t & (B - 1);
-        uint64_t x[A];
+        V x[A];
 #pragma unroll
         for (int i = 0; i < A; i++) x[i] = sm[g * RS + i * (B + 1) + b];
         if (DIR == 1 && (a.twiddle || a.use_scale)) {
             // inverse pass: input twiddle w_M^-((iB + b) j), times the scale
             const uint64_t j = j0 + (uint64_t)(LAYOUT == LAYOUT_STRIDED ? g : 0);
-            uint64_t base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)b * j) << sh));
-            const uint64_t step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * j) << sh));
-            if (a.use_scale) base = mont_mul<PI>(base, a.scale[PI]);
+            V base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)b * j) << sh));
+            const V step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * j) << sh));
+            if (a.use_scale) base = F::mul(base, (V)a.scale[F::SLOT]);
 #pragma unroll
             for (int i = 0; i < A; i++) {
-                x[i] = mont_mul<PI>(x[i], base);
-                if (i + 1 < A) base = mont_mul<PI>(base, step);
+                x[i] = F::mul(x[i], base);
+                if (i + 1 < A) base = F::mul(base, step);
             }
         }
         dft_reg<PI, S_::LOG_A>(x, w64);
 #pragma unroll
         for (int ka = 0; ka < A; ka++) {
-            uint64_t v = x[bitrev(ka, S_::LOG_A)];
+            V v = x[bitrev(ka, S_::LOG_A)];
             if (ka > 0 && b > 0)   // w_L^(b ka)
-                v = mont_mul<PI>(v, __ldg(twhi + ((b * ka) << (kTwBits - LOG_L))));
+                v = F::mul(v, __ldg(twhi + ((b * ka) << (kTwBits - LOG_L))));
             sm[g * RS + ka * (B + 1) + b] = v;
         }
     }
@@ -193,8 +214,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
     {
         constexpr int R = A / B;
         const int g = t >> LOG_B, q = t & (B - 1);
-        uint64_t y[R][B];
-        uint64_t step = 0;
+        V y[R][B];
+        V step = 0;
         if (DIR == 0 && LAYOUT == LAYOUT_STRIDED && a.twiddle) {
             const uint64_t j = j0 + (uint64_t)g;
             step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)A * j) << sh));
@@ -208,12 +229,12 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
             if (DIR == 0 && LAYOUT == LAYOUT_STRIDED && a.twiddle) {
                 // forward pass: output twiddle w_M^((ka + A kb) j)
                 const uint64_t j = j0 + (uint64_t)g;
-                uint64_t base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)ka * j) << sh));
+                V base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)ka * j) << sh));
 #pragma unroll
                 for (int kb = 0; kb < B; kb++) {
                     const int idx = bitrev(kb, LOG_B);
-                    y[r][idx] = mont_mul<PI>(y[r][idx], base);
-                    if (kb + 1 < B) base = mont_mul<PI>(base, step);
+                    y[r][idx] = F::mul(y[r][idx], base);
+                    if (kb + 1 < B) base = F::mul(base, step);
                 }
             }
         }
@@ -236,7 +257,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
         const long long S = 1LL << log_s;
         const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
         const long long stepg = (long long)B * S;
-        const uint64_t *src = sm + g * RS + m0;
+        const V *src = sm + g * RS + m0;
 #pragma unroll 8
         for (int it = 0; it < A; it++) data[base + it * stepg] = src[it * (B + 1)];
     } else {
@@ -252,10 +273,10 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, uint64_t *sm, const
 }
 
 template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
-__global__ void __launch_bounds__(kPassThreads, GBNTT_PASS_MIN_BLOCKS) ntt_pass_kernel(PassArgs a)
+__global__ void __launch_bounds__(kPassThreads, PassMinBlocks<PI>::value) ntt_pass_kernel(PassArgs a)
 {
     extern __shared__ uint64_t sm[];
-    pass_tile<PI, LOG_L, DIR, LD, LAYOUT>(a, sm, a.w64);
+    pass_tile<PI, LOG_L, DIR, LD, LAYOUT>(a, reinterpret_cast<typename Field<PI>::T *>(sm), a.w64);
 }
 
 // Launcher for one prime (explicitly instantiated, one translation unit per
@@ -263,17 +284,18 @@ __global__ void __launch_bounds__(kPassThreads, GBNTT_PASS_MIN_BLOCKS) ntt_pass_
 template <int PI, int LOG_L>
 static cudaError_t launch_pass_l(int dir, int ld, const PassArgs &a, cudaStream_t st)
 {
-    using S_ = PassShape<LOG_L>;
+    using S_ = PassShape<LOG_L, sizeof(typename Field<PI>::T)>;
     const int layout = a.log_s == 0 ? LAYOUT_CONTIG : LAYOUT_STRIDED;
     void (*fn)(PassArgs) = nullptr;
     if (dir == 0) {
         if (ld == LD_U32)
             fn = layout == LAYOUT_STRIDED ? ntt_pass_kernel<PI, LOG_L, 0, LD_U32, LAYOUT_STRIDED>
                                           : ntt_pass_kernel<PI, LOG_L, 0, LD_U32, LAYOUT_CONTIG>;
-        else if (ld == LD_U64LIMB)
-            fn = layout == LAYOUT_STRIDED ? ntt_pass_kernel<PI, LOG_L, 0, LD_U64LIMB, LAYOUT_STRIDED>
-                                          : ntt_pass_kernel<PI, LOG_L, 0, LD_U64LIMB, LAYOUT_CONTIG>;
-        else
+        else if (ld == LD_U64LIMB) {
+            if constexpr (sizeof(typename Field<PI>::T) == 8)   // packed limbs: 64-bit primes only
+                fn = layout == LAYOUT_STRIDED ? ntt_pass_kernel<PI, LOG_L, 0, LD_U64LIMB, LAYOUT_STRIDED>
+                                              : ntt_pass_kernel<PI, LOG_L, 0, LD_U64LIMB, LAYOUT_CONTIG>;
+        } else
             fn = layout == LAYOUT_STRIDED ? ntt_pass_kernel<PI, LOG_L, 0, LD_U64, LAYOUT_STRIDED>
                                           : ntt_pass_kernel<PI, LOG_L, 0, LD_U64, LAYOUT_CONTIG>;
     } else {

@@ -46,6 +46,7 @@ EXPORTS = (
     "gbntt_server_stop",
     "gbntt_split_terms_needed", "gbntt_e_required_log", "gbntt_binary_split", "gbntt_newton_reciprocal_u32",
     "gbntt_div_newton_u32", "gbntt_pow10_u32", "gbntt_to_decimal_u32", "gbntt_compute_e",
+    "gbntt_set_prime_set", "gbntt_prime_set",
 )
 
 _lib = None
@@ -153,6 +154,9 @@ def lib():
     L.gbntt_to_decimal_u32.restype = ctypes.c_int
     L.gbntt_compute_e.argtypes = [ctypes.c_long, ctypes.c_char_p, _sz, ctypes.POINTER(ctypes.c_double)]
     L.gbntt_compute_e.restype = ctypes.c_int
+    L.gbntt_set_prime_set.argtypes = [ctypes.c_int]
+    L.gbntt_set_prime_set.restype = ctypes.c_int
+    L.gbntt_prime_set.restype = ctypes.c_int
     L.gbntt_last_error.restype = ctypes.c_char_p
     L.gbntt_stream.restype = _vp
     _lib = L
@@ -284,6 +288,15 @@ class Server:
 
     def stop(self):
         _check(lib().gbntt_server_stop())
+
+
+def set_prime_set(nprimes):
+    """2: q0 + the 32-bit p3 (default); 3: the reference's three 64-bit primes."""
+    _check(lib().gbntt_set_prime_set(int(nprimes)))
+
+
+def prime_set():
+    return int(lib().gbntt_prime_set())
 
 
 def set_coeff_bits(bits):

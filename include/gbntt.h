@@ -189,7 +189,9 @@ int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log
  * prime index 0..2 (2^64 - 2^b + 1, b = 32, 34, 40) and op 0 = (a+b) mod p,
  * 1 = (a-b) mod p, 2 = a*b*2^-64 mod p (Montgomery), 3..5 = the same with
  * the plain C++ forms. a, b canonical (a may be any 64-bit value for op
- * 2 and 5). Stream-ordered. */
+ * 2 and 5). Prime index 3 is p3 = 3 * 2^30 + 1 on the low 32 bits of each
+ * word, op 2 = a*b*2^-32 mod p3 (a may be any 32-bit value for op 2 and 5).
+ * Stream-ordered. */
 int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t n,
                        void *stream);
 
@@ -271,6 +273,18 @@ int gbntt_to_decimal_u32(char *out, size_t cap, size_t *len, const uint32_t *x, 
  * 5 wall times: product tree, numerator x 10^(D-1), division, decimal
  * conversion, total. */
 int gbntt_compute_e(long digits, char *out, size_t cap, double *phase_seconds);
+
+/* No counterpart in the reference (its engine always uses three 64-bit
+ * primes). Primes used for products of 32-bit coefficients (gbntt_mul_u32,
+ * batches, serving, the e pipeline and ntt_bigint_mul in its default
+ * mode): 2 = q0 = 2^64 - 2^32 + 1 (64-bit residues) with p3 = 3 * 2^30 + 1
+ * (32-bit residues), CRT modulus ~2^95.6 above every coefficient (< 2^93),
+ * the default; 3 = the reference's three 64-bit primes. Products are
+ * identical either way. Packed (64-bit coefficient) products always use
+ * three 64-bit primes. The default comes from GBNTT_PRIMES (2 or 3) at
+ * init. gbntt_prime_set returns 0 when no engine is initialised. */
+int gbntt_set_prime_set(int nprimes);
+int gbntt_prime_set(void);
 
 /* Last error message of this library. */
 const char *gbntt_last_error(void);

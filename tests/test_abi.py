@@ -40,7 +40,8 @@ def test_library_is_native_sm103a(built_lib):
 
 def test_pure_host_queries(built_lib):
     # no device needed: planning and sizing are host logic
-    assert engine.plan(29) == [10, 10, 9]
+    assert engine.plan(29) == [9, 10, 10]
+    assert engine.plan(30) == [10, 10, 10]
     assert engine.plan(21) == [7, 7, 7]
     assert engine.plan(12) == [6, 6]
     assert engine.plan(5) == [5]

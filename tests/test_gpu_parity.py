@@ -272,3 +272,36 @@ def test_device_modops(engine, prime):
         assert got == want[op % 3], (prime, op)
     for buf in (da, db, dw, dout):
         buf.free()
+
+
+def test_device_modops_p3(engine):
+    # the 32-bit prime p3 = 3 * 2^30 + 1 (signed Montgomery, R = 2^32): PTX
+    # and plain forms against Python integers, corners included
+    p = 3 * (1 << 30) + 1
+    rng = np.random.default_rng(43)
+    corners = [0, 1, 2, p - 1, p - 2, (1 << 31) - 1, 1 << 31, p >> 1, (1 << 30), p - (1 << 30)]
+    n = 1 << 16
+    a = rng.integers(0, p, n, dtype=np.uint64)
+    b = rng.integers(0, p, n, dtype=np.uint64)
+    k = len(corners)
+    a[:k * k] = np.repeat(np.array(corners, dtype=np.uint64), k)
+    b[:k * k] = np.tile(np.array(corners, dtype=np.uint64), k)
+    wide = a.copy()
+    wide[k * k:k * k + 100] = rng.integers(p, 1 << 32, 100, dtype=np.uint64)
+    wide[-3:] = [(1 << 32) - 1, p, p + 1]
+    da, db, dw, dout = (cudart.DeviceBuffer(8 * n) for _ in range(4))
+    da.upload(a)
+    db.upload(b)
+    dw.upload(wide)
+    rinv = pow(1 << 32, -1, p)
+    want = {0: [(int(x) + int(y)) % p for x, y in zip(a, b)],
+            1: [(int(x) - int(y)) % p for x, y in zip(a, b)],
+            2: [int(x) * int(y) * rinv % p for x, y in zip(wide, b)]}
+    for op in range(6):
+        src = dw if op % 3 == 2 else da
+        assert engine.lib().gbntt_debug_modops(3, op, src.ptr, db.ptr, dout.ptr, n, None) == 0
+        cudart.stream_sync(engine.lib().gbntt_stream())
+        got = [int(v) for v in dout.download(np.uint64, n)]
+        assert got == want[op % 3], op
+    for buf in (da, db, dw, dout):
+        buf.free()
