@@ -236,10 +236,127 @@ __device__ __forceinline__ uint32_t p3_mul_ref(uint32_t a, uint32_t b)
 }
 
 // ---------------------------------------------------------------------------
+// q0 = 2^64 - 2^32 + 1 in normal form with lazy residues: any 64-bit word x
+// stands for x mod q0 (EPS = 2^64 mod q0 = 2^32 - 1, 2^96 == -1). Products
+// fold the 128-bit result without multiplies:
+//   t = t0 + t1 2^32 + t2 2^64 + t3 2^96 == (t1:t0) - t3 + t2 EPS,
+// sums and differences fold their carry or borrow by EPS (at most twice).
+// Outputs lie in [0, 2^64); the Garner stage reduces them.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t gl_add(uint64_t a, uint64_t b)
+{
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 a0, a1, b0, b1, s0, s1, c, c2;\n\t"
+        "mov.b64 {a0, a1}, %1;\n\t"
+        "mov.b64 {b0, b1}, %2;\n\t"
+        "add.cc.u32 s0, a0, b0;\n\t"
+        "addc.cc.u32 s1, a1, b1;\n\t"
+        "addc.u32 c, 0, 0;\n\t"
+        "mad.lo.cc.u32 s0, c, 0xFFFFFFFF, s0;\n\t"
+        "addc.cc.u32 s1, s1, 0;\n\t"
+        "addc.u32 c2, 0, 0;\n\t"
+        "mad.lo.cc.u32 s0, c2, 0xFFFFFFFF, s0;\n\t"
+        "addc.u32 s1, s1, 0;\n\t"
+        "mov.b64 %0, {s0, s1};\n\t"
+        "}"
+        : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+__device__ __forceinline__ uint64_t gl_sub(uint64_t a, uint64_t b)
+{
+    // on borrow the wrapped difference is 2^64 too large: subtract EPS (== 2^64),
+    // and once more if that wraps as well
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 a0, a1, b0, b1, d0, d1, bw, bw2;\n\t"
+        "mov.b64 {a0, a1}, %1;\n\t"
+        "mov.b64 {b0, b1}, %2;\n\t"
+        "sub.cc.u32 d0, a0, b0;\n\t"
+        "subc.cc.u32 d1, a1, b1;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "sub.cc.u32 d0, d0, bw;\n\t"
+        "subc.cc.u32 d1, d1, 0;\n\t"
+        "subc.u32 bw2, 0, 0;\n\t"
+        "sub.cc.u32 d0, d0, bw2;\n\t"
+        "subc.u32 d1, d1, 0;\n\t"
+        "mov.b64 %0, {d0, d1};\n\t"
+        "}"
+        : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+__device__ __forceinline__ uint64_t gl_mul(uint64_t a, uint64_t b)
+{
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 a0, a1, b0, b1, z, l00, h00, l01, h01, l10, h10, t2, t3, x0, x1, bw, y0, y1, r0, r1, c;\n\t"
+        ".reg .u64 p00, p01, p10, p11, th, w;\n\t"
+        "mov.b64 {a0, a1}, %1;\n\t"
+        "mov.b64 {b0, b1}, %2;\n\t"
+        "mov.u32 z, 0;\n\t"
+        "mul.wide.u32 p00, a0, b0;\n\t"
+        "mov.b64 {l00, h00}, p00;\n\t"
+        "mov.b64 w, {h00, z};\n\t"
+        "mad.wide.u32 p01, a0, b1, w;\n\t"
+        "mov.b64 {l01, h01}, p01;\n\t"
+        "mov.b64 w, {l01, z};\n\t"
+        "mad.wide.u32 p10, a1, b0, w;\n\t"
+        "mov.b64 {l10, h10}, p10;\n\t"
+        "mov.b64 w, {h01, z};\n\t"
+        "mad.wide.u32 p11, a1, b1, w;\n\t"
+        "mad.wide.u32 th, h10, 1, p11;\n\t"
+        "mov.b64 {t2, t3}, th;\n\t"
+        // x = (l10:l00) - t3, + q0 on borrow (add 0xFFFFFFFF00000001 = -EPS)
+        "sub.cc.u32 x0, l00, t3;\n\t"
+        "subc.cc.u32 x1, l10, 0;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "mad.lo.cc.u32 x0, bw, 0xFFFFFFFF, x0;\n\t"
+        "madc.lo.u32 x1, bw, 1, x1;\n\t"
+        // y = t2 * EPS = (t2 << 32) - t2
+        "sub.cc.u32 y0, 0, t2;\n\t"
+        "subc.u32 y1, t2, 0;\n\t"
+        // r = x + y, + EPS on carry (no second carry)
+        "add.cc.u32 r0, x0, y0;\n\t"
+        "addc.cc.u32 r1, x1, y1;\n\t"
+        "addc.u32 c, 0, 0;\n\t"
+        "mad.lo.cc.u32 r0, c, 0xFFFFFFFF, r0;\n\t"
+        "addc.u32 r1, r1, 0;\n\t"
+        "mov.b64 %0, {r0, r1};\n\t"
+        "}"
+        : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+// canonical representative in [0, q0)
+__host__ __device__ __forceinline__ uint64_t gl_canon(uint64_t x)
+{
+    return x >= 0xFFFFFFFF00000001ull ? x - 0xFFFFFFFF00000001ull : x;
+}
+
+// plain C++ forms for the device self-test (canonical results)
+__device__ __forceinline__ uint64_t gl_add_ref(uint64_t a, uint64_t b)
+{
+    constexpr uint64_t P = 0xFFFFFFFF00000001ull;
+    return (uint64_t)(((unsigned __int128)a + b) % P);
+}
+__device__ __forceinline__ uint64_t gl_sub_ref(uint64_t a, uint64_t b)
+{
+    constexpr uint64_t P = 0xFFFFFFFF00000001ull;
+    return (uint64_t)(((unsigned __int128)(a % P) + P - (b % P)) % P);
+}
+__device__ __forceinline__ uint64_t gl_mul_ref(uint64_t a, uint64_t b)
+{
+    constexpr uint64_t P = 0xFFFFFFFF00000001ull;
+    return (uint64_t)(((unsigned __int128)a * b) % P);
+}
+
+// ---------------------------------------------------------------------------
 // Field policies for the pass kernels: prime index PI -> residue word T,
 // slot in the per-launch argument arrays, and the three operations. Primes
 // 0..2 are the 64-bit Montgomery primes above (slots 0..2); prime 3 is p3
-// (slot 1: it sits beside q0 in the two-prime set).
+// and prime 4 is lazy normal-form q0 (slots 1 and 0 of the two-prime set).
 // ---------------------------------------------------------------------------
 template <int PI>
 struct Field {
@@ -262,11 +379,24 @@ struct Field<3> {
     static __device__ __forceinline__ T from_u32(uint32_t v) { return v >= kP3 ? v - kP3 : v; }   // 2^32 < 2 p3
 };
 
+// Prime 4 is q0 again, in normal form with lazy residues (slot 0 of the
+// two-prime set); prime 0 (Montgomery q0) stays in the three-prime set.
+template <>
+struct Field<4> {
+    typedef uint64_t T;
+    static constexpr int SLOT = 0;
+    static constexpr uint64_t P = 0xFFFFFFFF00000001ull;
+    static __device__ __forceinline__ T add(T a, T b) { return gl_add(a, b); }
+    static __device__ __forceinline__ T sub(T a, T b) { return gl_sub(a, b); }
+    static __device__ __forceinline__ T mul(T a, T b) { return gl_mul(a, b); }
+    static __device__ __forceinline__ T from_u32(uint32_t v) { return v; }
+};
+
 // Runtime prime dispatch helpers used by host-side tables.
 __host__ __device__ inline uint64_t prime_value(int pi)
 {
-    return pi == 0 ? 0xFFFFFFFF00000001ull
-                   : (pi == 1 ? 0xFFFFFFFC00000001ull : (pi == 2 ? 0xFFFFFF0000000001ull : (uint64_t)kP3));
+    return (pi == 0 || pi == 4) ? 0xFFFFFFFF00000001ull
+                                : (pi == 1 ? 0xFFFFFFFC00000001ull : (pi == 2 ? 0xFFFFFF0000000001ull : (uint64_t)kP3));
 }
 __host__ __device__ inline int prime_b(int pi) { return pi == 0 ? 32 : (pi == 1 ? 34 : 40); }
 

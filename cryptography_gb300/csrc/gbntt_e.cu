@@ -958,6 +958,12 @@ struct EngineUse {
     ~EngineUse()
     {
         if (g_st) cudaStreamSynchronize(g_st);
+        // hand the stream-ordered pool's reserved memory back: the pipeline's
+        // temporaries reach several GB at 10^8 digits
+        int dev = 0;
+        cudaMemPool_t pool;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+            cudaMemPoolTrimTo(pool, 0);
         if (owned) gbntt_teardown();
         g_st = nullptr;
     }

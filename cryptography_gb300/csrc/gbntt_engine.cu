@@ -57,7 +57,8 @@ struct PrimeSet {
     int n;
     int pi[3];
 };
-static const PrimeSet kSet2 = {2, {0, 3, 0}};
+static const PrimeSet kSet2 = {2, {4, 3, 0}};       // lazy normal-form q0 + p3
+static const PrimeSet kSet2m = {2, {0, 3, 0}};      // Montgomery q0 + p3
 static const PrimeSet kSet3 = {3, {0, 1, 2}};
 
 struct Engine {
@@ -65,15 +66,19 @@ struct Engine {
     int max_log = 0;
     size_t n_max = 0;
     uint64_t *d_spec = nullptr;     // 6 x n_max: spectra of operand A (3) then B (3)
-    uint64_t *d_tw = nullptr;       // [prime][dir][hi|lo][2^15]
+    uint64_t *d_tw = nullptr;       // [prime 0..2, then normal-form q0][dir][hi|lo][2^15]
     uint32_t *d_tw3 = nullptr;      // p3: [dir][hi|lo][2^15]
     int prime_set = 2;              // primes used for 32-bit coefficients: 2 or 3
+    bool q0_lazy = false;           // two-prime set: q0 as prime 4 (lazy normal form) or 0 (Montgomery)
+    bool overlap = true;            // two-prime set: second prime's passes on stream2
     uint64_t garner2[2] = {0, 0};   // two-prime Garner constants (p3 Montgomery multipliers)
     unsigned *d_ctl = nullptr;      // [0] ticket, [1] error, [2..] tile status
     size_t n_status = 0;
     uint32_t *d_io = nullptr;       // staging for host-pointer calls
     size_t io_words = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;      // second prime's passes run here, overlapping the first's
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     uint64_t garner[4] = {0, 0, 0, 0};
     uint64_t q01_lo = 0, q01_hi = 0;   // q0 * q1
     int bigint_coeff_bits = 32;        // coefficient width used by the BigInt entry points
@@ -90,7 +95,7 @@ struct Engine {
 
 static Engine g;
 // Montgomery forms of w_64^i per prime and direction (kernel arguments).
-static uint64_t g_w64[4][2][64];
+static uint64_t g_w64[5][2][64];
 
 static cudaError_t launch_pass_any(int pi, int log_l, int dir, int ld, PassArgs &a, cudaStream_t st)
 {
@@ -99,7 +104,8 @@ static cudaError_t launch_pass_any(int pi, int log_l, int dir, int ld, PassArgs 
     case 0: return launch_pass_prime<0>(log_l, dir, ld, a, st);
     case 1: return launch_pass_prime<1>(log_l, dir, ld, a, st);
     case 2: return launch_pass_prime<2>(log_l, dir, ld, a, st);
-    default: return launch_pass_prime<3>(log_l, dir, ld, a, st);
+    case 3: return launch_pass_prime<3>(log_l, dir, ld, a, st);
+    default: return launch_pass_prime<4>(log_l, dir, ld, a, st);
     }
 }
 static std::recursive_mutex g_mu;
@@ -216,7 +222,7 @@ static size_t workspace_bytes(int max_log)
 {
     const size_t n = (size_t)1 << max_log;
     const size_t spec = 6 * n * sizeof(uint64_t);
-    const size_t tw = 3 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t) + 2 * 2 * (size_t)kTwSize * sizeof(uint32_t);
+    const size_t tw = 4 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t) + 2 * 2 * (size_t)kTwSize * sizeof(uint32_t);
     const size_t ctl = (2 + status_words(n)) * sizeof(unsigned);
     const size_t io = (4 * n + 64) * sizeof(uint32_t);
     return spec + tw + ctl + io;
@@ -233,6 +239,10 @@ static void free_all()
     cudaFree(g.d_tw3);
     cudaFree(g.d_ctl);
     cudaFree(g.d_io);
+    if (g.stream2) cudaStreamSynchronize(g.stream2);
+    if (g.ev_fork) cudaEventDestroy(g.ev_fork);
+    if (g.ev_join) cudaEventDestroy(g.ev_join);
+    if (g.stream2) cudaStreamDestroy(g.stream2);
     if (g.stream) cudaStreamDestroy(g.stream);
     g = Engine();
 }
@@ -249,8 +259,11 @@ static int init_impl(int max_log)
     g.max_log = max_log;
     g.n_max = (size_t)1 << max_log;
     CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&g.stream2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&g.ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&g.ev_join, cudaEventDisableTiming));
     if (cudaMalloc(&g.d_spec, 6 * g.n_max * sizeof(uint64_t)) != cudaSuccess ||
-        cudaMalloc(&g.d_tw, 3 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t)) != cudaSuccess ||
+        cudaMalloc(&g.d_tw, 4 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t)) != cudaSuccess ||
         cudaMalloc(&g.d_tw3, 2 * 2 * (size_t)kTwSize * sizeof(uint32_t)) != cudaSuccess) {
         set_err("gbntt_init: device allocation of %zu bytes failed", workspace_bytes(max_log));
         cudaGetLastError();
@@ -277,28 +290,31 @@ static int init_impl(int max_log)
     for (int i = 0; i < 2; i++) CK(cudaEventCreateWithFlags(&g.btab_ev[i], cudaEventDisableTiming));
 
     // Twiddle tables and the w_64 constants.
-    const size_t tw_words = 3 * 2 * 2 * (size_t)kTwSize;
+    const size_t tw_words = 4 * 2 * 2 * (size_t)kTwSize;
     uint64_t *h = (uint64_t *)malloc(tw_words * sizeof(uint64_t));
     if (!h) { set_err("gbntt_init: host allocation failed"); free_all(); return GBNTT_ERR_ALLOC; }
-    uint64_t (&w64)[4][2][64] = g_w64;
-    for (int pi = 0; pi < 3; pi++) {
+    uint64_t (&w64)[5][2][64] = g_w64;
+    // table slot 3 holds q0 in normal form (prime 4); slots 0..2 Montgomery
+    for (int ts = 0; ts < 4; ts++) {
+        const bool normal = ts == 3;
+        const int pi = normal ? 4 : ts;   // prime index of this table slot
         const uint64_t p = prime_value(pi);
-        const uint64_t w = h_pow(kGen[pi], (p - 1) >> kMaxLog, p);
+        const uint64_t w = h_pow(kGen[normal ? 0 : ts], (p - 1) >> kMaxLog, p);
         for (int dir = 0; dir < 2; dir++) {
             const uint64_t wd = dir ? h_inv(w, p) : w;
-            uint64_t *hi = h + (((size_t)pi * 2 + dir) * 2 + 0) * kTwSize;
-            uint64_t *lo = h + (((size_t)pi * 2 + dir) * 2 + 1) * kTwSize;
+            uint64_t *hi = h + (((size_t)ts * 2 + dir) * 2 + 0) * kTwSize;
+            uint64_t *lo = h + (((size_t)ts * 2 + dir) * 2 + 1) * kTwSize;
             const uint64_t wbig = h_pow(wd, (uint64_t)kTwSize, p);
             uint64_t x = 1, y = 1;
             for (int i = 0; i < kTwSize; i++) {
-                lo[i] = h_mont(x, p);
-                hi[i] = h_mont(y, p);
+                lo[i] = normal ? x : h_mont(x, p);
+                hi[i] = normal ? y : h_mont(y, p);
                 x = h_mul(x, wd, p);
                 y = h_mul(y, wbig, p);
             }
             const uint64_t r64 = h_pow(wd, (uint64_t)1 << (kMaxLog - 6), p);
             uint64_t z = 1;
-            for (int i = 0; i < 64; i++) { w64[pi][dir][i] = h_mont(z, p); z = h_mul(z, r64, p); }
+            for (int i = 0; i < 64; i++) { w64[pi][dir][i] = normal ? z : h_mont(z, p); z = h_mul(z, r64, p); }
         }
     }
     cudaError_t e = cudaMemcpy(g.d_tw, h, tw_words * sizeof(uint64_t), cudaMemcpyHostToDevice);
@@ -350,6 +366,12 @@ static int init_impl(int max_log)
         g.bigint_coeff_bits = (cb && atoi(cb) == 64) ? 64 : 32;
         const char *ps = getenv("GBNTT_PRIMES");
         g.prime_set = (ps && atoi(ps) == 3) ? 3 : 2;
+        // tuning knobs: q0 form in the two-prime set (Montgomery measured 94 ms
+        // against 101 ms lazy at 2^28 limbs) and the two-stream overlap
+        const char *qf = getenv("GBNTT_Q0_FORM");
+        g.q0_lazy = qf && qf[0] == 'l';
+        const char *ov = getenv("GBNTT_OVERLAP");
+        g.overlap = !(ov && ov[0] == '0');
     }
     g.ready = true;
     return GBNTT_OK;
@@ -361,9 +383,10 @@ static TwTables tables(const PrimeSet &ps, int dir)
     memset(&t, 0, sizeof t);
     for (int k = 0; k < ps.n; k++) {
         const int pi = ps.pi[k];
-        if (pi < 3) {
-            t.hi[k] = tw_ptr(pi, dir, 0);
-            t.lo[k] = tw_ptr(pi, dir, 1);
+        if (pi != 3) {
+            const int ts = pi == 4 ? 3 : pi;   // normal-form q0 tables sit in slot 3
+            t.hi[k] = tw_ptr(ts, dir, 0);
+            t.lo[k] = tw_ptr(ts, dir, 1);
         } else {
             t.hi[k] = (const uint64_t *)(g.d_tw3 + ((size_t)dir * 2 + 0) * kTwSize);
             t.lo[k] = (const uint64_t *)(g.d_tw3 + ((size_t)dir * 2 + 1) * kTwSize);
@@ -372,14 +395,34 @@ static TwTables tables(const PrimeSet &ps, int dir)
     return t;
 }
 
-static const PrimeSet &coef32_set() { return g.prime_set == 3 ? kSet3 : kSet2; }
+static const PrimeSet &coef32_set() { return g.prime_set == 3 ? kSet3 : (g.q0_lazy ? kSet2 : kSet2m); }
 static double word_bytes(int pi) { return pi == 3 ? 4.0 : 8.0; }
+
+// Overlap of the two-prime set: slot 1's passes go to an auxiliary stream
+// forked from st before the first forward pass and joined back before the
+// Garner+carry kernel, so the two primes' transforms share the SMs (q0's
+// kernels are bound by the integer pipes, p3's by memory latency). forward
+// and inverse take the forked stream (nullptr: everything on st).
+static cudaStream_t fork_aux(const PrimeSet &ps, cudaStream_t st, cudaStream_t aux)
+{
+    if (!aux || ps.n != 2 || !g.overlap) return nullptr;
+    if (cudaEventRecord(g.ev_fork, st) != cudaSuccess || cudaStreamWaitEvent(aux, g.ev_fork, 0) != cudaSuccess)
+        return nullptr;
+    return aux;
+}
+static int join_aux(cudaStream_t st, cudaStream_t aux)
+{
+    if (!aux) return GBNTT_OK;
+    CK(cudaEventRecord(g.ev_join, aux));
+    CK(cudaStreamWaitEvent(st, g.ev_join, 0));
+    return GBNTT_OK;
+}
 
 // Forward transform of one operand: limbs -> one spectrum per prime of the
 // set at spec[k * stride] (k = slot; p3's 32-bit words fill half a slot).
 static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void *limbs, size_t n, int L,
                    cudaStream_t st, bool packed = false, long long W = 1, const uint32_t *const *limb_tab = nullptr,
-                   const long long *len_tab = nullptr)
+                   const long long *len_tab = nullptr, cudaStream_t aux = nullptr)
 {
     int pl[3];
     const int np = plan_passes(L, pl);
@@ -401,9 +444,10 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
         a.twiddle = a.log_s > 0;
         for (int k = 0; k < ps.n; k++) {
             const double nbw = word_bytes(ps.pi[k]) * (double)((size_t)1 << L) * (double)W;
-            rec_begin(st, i == 0 ? 0 : 1, pl[i], i == 0 ? (packed ? 8.0 : 4.0) * (double)n + nbw : 2.0 * nbw);
-            CK(launch_pass_any(ps.pi[k], pl[i], 0, i == 0 ? (packed ? LD_U64LIMB : LD_U32) : LD_U64, a, st));
-            rec_end(st);
+            cudaStream_t sk = (aux && k == 1) ? aux : st;
+            rec_begin(sk, i == 0 ? 0 : 1, pl[i], i == 0 ? (packed ? 8.0 : 4.0) * (double)n + nbw : 2.0 * nbw);
+            CK(launch_pass_any(ps.pi[k], pl[i], 0, i == 0 ? (packed ? LD_U64LIMB : LD_U32) : LD_U64, a, sk));
+            rec_end(sk);
         }
         log_m -= pl[i];
     }
@@ -412,7 +456,7 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
 
 // Pointwise product of the spectra and inverse transform, in place in specA.
 static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, size_t stride, int L,
-                   cudaStream_t st, bool square, long long W = 1)
+                   cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr)
 {
     int pl[3];
     const int np = plan_passes(L, pl);
@@ -426,7 +470,8 @@ static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, s
         // the inverse output is scaled by exactly N^-1.
         const uint64_t p = prime_value(pi);
         const uint64_t ninv = h_inv(((uint64_t)1 << L) % p, p);
-        a.scale[k] = pi < 3 ? h_mont(h_mont(ninv, p), p) : (uint64_t)h_mont3(h_mont3(ninv));
+        // (normal-form q0: the pointwise product leaves no factor, so N^-1 itself)
+        a.scale[k] = pi < 3 ? h_mont(h_mont(ninv, p), p) : pi == 3 ? (uint64_t)h_mont3(h_mont3(ninv)) : ninv;
     }
     a.tw = tables(ps, 1);
     int log_ms[3];
@@ -441,9 +486,10 @@ static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, s
         const bool first = (i == np - 1);
         for (int k = 0; k < ps.n; k++) {
             const double nbw = word_bytes(ps.pi[k]) * (double)((size_t)1 << L) * (double)W;
-            rec_begin(st, first ? 2 : 3, pl[i], first ? (square ? 2.0 : 3.0) * nbw : 2.0 * nbw);
-            CK(launch_pass_any(ps.pi[k], pl[i], 1, first ? LD_PW : LD_U64, a, st));
-            rec_end(st);
+            cudaStream_t sk = (aux && k == 1) ? aux : st;
+            rec_begin(sk, first ? 2 : 3, pl[i], first ? (square ? 2.0 : 3.0) * nbw : 2.0 * nbw);
+            CK(launch_pass_any(ps.pi[k], pl[i], 1, first ? LD_PW : LD_U64, a, sk));
+            rec_end(sk);
         }
     }
     return GBNTT_OK;
@@ -503,13 +549,16 @@ static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t
     uint64_t *specA = g.d_spec;
     uint64_t *specB = g.d_spec + 3 * g.n_max;
     const PrimeSet &ps = coef32_set();
-    int rc = forward(ps, specA, g.n_max, d_a, na, L, st);
+    cudaStream_t aux = fork_aux(ps, st, g.stream2);
+    int rc = forward(ps, specA, g.n_max, d_a, na, L, st, false, 1, nullptr, nullptr, aux);
     if (rc) return rc;
     if (!square) {
-        rc = forward(ps, specB, g.n_max, d_b, nb, L, st);
+        rc = forward(ps, specB, g.n_max, d_b, nb, L, st, false, 1, nullptr, nullptr, aux);
         if (rc) return rc;
     }
-    rc = inverse(ps, specA, square ? specA : specB, g.n_max, L, st, square);
+    rc = inverse(ps, specA, square ? specA : specB, g.n_max, L, st, square, 1, aux);
+    if (rc) return rc;
+    rc = join_aux(st, aux);
     if (rc) return rc;
     return carry(ps, d_c, n_out, specA, g.n_max, L, st);
 }
@@ -590,7 +639,8 @@ struct BatchItem {
 };
 
 // One wave of W products, all of transform length 2^L, on stream st.
-static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, cudaStream_t st)
+static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, cudaStream_t st,
+                      cudaStream_t aux_stream = nullptr)
 {
     const int slot = *x.slot;
     CK(cudaEventSynchronize(x.btab_ev[slot]));
@@ -620,13 +670,16 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
     *x.slot = slot ^ 1;
     uint64_t *specA = x.spec, *specB = x.spec + 3 * x.cap;
     const PrimeSet &ps = coef32_set();
+    cudaStream_t aux = fork_aux(ps, st, aux_stream);
     int rc = forward(ps, specA, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab),
-                     (const long long *)(dtab + W));
+                     (const long long *)(dtab + W), aux);
     if (rc) return rc;
     rc = forward(ps, specB, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab + 2 * W),
-                 (const long long *)(dtab + 3 * W));
+                 (const long long *)(dtab + 3 * W), aux);
     if (rc) return rc;
-    rc = inverse(ps, specA, specB, x.cap, L, st, false, W);
+    rc = inverse(ps, specA, specB, x.cap, L, st, false, W, aux);
+    if (rc) return rc;
+    rc = join_aux(st, aux);
     if (rc) return rc;
     CarryArgs c;
     memset(&c, 0, sizeof c);
@@ -687,7 +740,7 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
                 const int i = order[w0 + k].second;
                 items.push_back({d_c[i], d_a[i], d_b[i], na[i], nb[i]});
             }
-            const int rc = batch_wave(x, items.data(), W, L, st);
+            const int rc = batch_wave(x, items.data(), W, L, st, g.stream2);
             if (rc) return rc;
         }
         pos = end;
@@ -1046,7 +1099,7 @@ int gbntt_set_plan(int log_n, int npasses, const int *passes)
 int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t n,
                        void *stream)
 {
-    if (prime < 0 || prime > 3 || op < 0 || op > 5) { set_err("gbntt_debug_modops: bad prime/op"); return GBNTT_ERR_ARG; }
+    if (prime < 0 || prime > 4 || op < 0 || op > 5) { set_err("gbntt_debug_modops: bad prime/op"); return GBNTT_ERR_ARG; }
     cudaStream_t st = stream ? (cudaStream_t)stream : (g.ready ? g.stream : (cudaStream_t)0);
     CK(launch_modops(prime, op, d_a, d_b, d_out, (long long)n, st));
     return GBNTT_OK;

@@ -43,6 +43,19 @@ __global__ void modops_kernel(int prime, int op, const uint64_t *a, const uint64
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t x = a[i], y = b[i];
+    if (prime == 4) {   // lazy normal-form q0 (operands any 64-bit words)
+        uint64_t r;
+        switch (op) {
+        case 0: r = gl_add(x, y); break;
+        case 1: r = gl_sub(x, y); break;
+        case 2: r = gl_mul(x, y); break;
+        case 3: r = gl_add_ref(x, y); break;
+        case 4: r = gl_sub_ref(x, y); break;
+        default: r = gl_mul_ref(x, y); break;
+        }
+        out[i] = r;
+        return;
+    }
     if (prime == 3) {   // the 32-bit prime (operands in the low words)
         const uint32_t u = (uint32_t)x, v = (uint32_t)y;
         uint32_t r;
@@ -134,7 +147,7 @@ __device__ __forceinline__ void garner_coef(const CarryArgs &a, long long j, uin
 
 typedef unsigned __int128 u128;
 
-// Two-prime form (q0 and the 32-bit p3): c_j = r0 + q0 a1 with
+// Two-prime form (lazy q0 and the 32-bit p3): c_j = r0 + q0 a1 with
 // a1 = (r1 - r0) q0^-1 mod p3, c_j < q0 p3 < 2^96. garner[0] = q0^-1 mod p3
 // and garner[1] = 2^64 mod p3, both as p3 Montgomery multipliers. A true
 // coefficient is below N 2^64 (N = the transform length, above the shorter
@@ -144,7 +157,7 @@ __device__ __forceinline__ void garner_coef2(const CarryArgs &a, long long j, ui
 {
     if (j < 0 || j >= a.n_coef) { w0 = w1 = w2 = 0; return; }
     constexpr uint64_t q0 = Prime<0>::P;
-    const uint64_t r0 = a.res[0][j];
+    const uint64_t r0 = gl_canon(a.res[0][j]);   // lazy residues reach [0, 2^64)
     const uint32_t r1 = ((const uint32_t *)a.res[1])[j];
     const uint32_t lo = (uint32_t)r0;
     const uint32_t r0m = p3_add(p3_mul((uint32_t)(r0 >> 32), (uint32_t)a.garner[1]), lo >= kP3 ? lo - kP3 : lo);

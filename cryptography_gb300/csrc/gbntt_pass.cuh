@@ -55,7 +55,11 @@ struct PassShape {
     static constexpr int T = kPassThreads;
     static constexpr int LOG_G = kLogPassThreads - LOG_B;
     static constexpr int G = 1 << LOG_G;          // columns per CTA
-    static constexpr int RS = L + A + 1;          // odd row stride in words
+    // row stride in words: odd for 8-byte words; for 4-byte words the pad
+    // that minimises bank conflicts over the load/store and both DFT steps
+    // (searched exhaustively per l; conflict-free at l = 10)
+    static constexpr int PAD4 = LOG_L == 5 ? 5 : LOG_L == 6 ? 2 : LOG_L == 7 ? 6 : LOG_L == 10 ? 8 : 4;
+    static constexpr int RS = L + A + (WORD == 4 ? PAD4 : 1);
     static constexpr size_t SMEM = (size_t)G * RS * WORD;
 };
 
@@ -165,8 +169,13 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
         const long long stepg = (long long)B * S;
         V *dst = sm + g * RS + m0;
+        if constexpr (sizeof(V) == 4) {   // all A loads in flight (registers allow it)
+#pragma unroll
+            for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
+        } else {
 #pragma unroll 8
-        for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
+            for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
+        }
     } else {
         const long long rows_left = a.ncols - col0;
         const long long base = col0 << LOG_L;

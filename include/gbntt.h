@@ -191,6 +191,8 @@ int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log
  * the plain C++ forms. a, b canonical (a may be any 64-bit value for op
  * 2 and 5). Prime index 3 is p3 = 3 * 2^30 + 1 on the low 32 bits of each
  * word, op 2 = a*b*2^-32 mod p3 (a may be any 32-bit value for op 2 and 5).
+ * Prime index 4 is q0 in lazy normal form: any 64-bit operands, op 2 =
+ * a*b mod q0, results in [0, 2^64) congruent mod q0 (canonical for 3..5).
  * Stream-ordered. */
 int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t n,
                        void *stream);

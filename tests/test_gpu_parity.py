@@ -274,6 +274,37 @@ def test_device_modops(engine, prime):
         buf.free()
 
 
+def test_device_modops_lazy_q0(engine):
+    # q0 in lazy normal form: operands are any 64-bit words (standing for
+    # their value mod q0), results lie in [0, 2^64) and must agree mod q0
+    p = oracle.PRIMES[0]
+    rng = np.random.default_rng(44)
+    corners = [0, 1, 2, p - 1, p, p + 1, (1 << 64) - 1, (1 << 64) - 2, (1 << 32) - 1, 1 << 32, 1 << 63,
+               (1 << 64) - (1 << 32)]
+    n = 1 << 16
+    a = rng.integers(0, 1 << 64, n, dtype=np.uint64)
+    b = rng.integers(0, 1 << 64, n, dtype=np.uint64)
+    k = len(corners)
+    a[:k * k] = np.repeat(np.array(corners, dtype=np.uint64), k)
+    b[:k * k] = np.tile(np.array(corners, dtype=np.uint64), k)
+    da, db, dout = (cudart.DeviceBuffer(8 * n) for _ in range(3))
+    da.upload(a)
+    db.upload(b)
+    A = [int(x) for x in a]
+    B = [int(y) for y in b]
+    want = {0: [(x + y) % p for x, y in zip(A, B)], 1: [(x - y) % p for x, y in zip(A, B)],
+            2: [x * y % p for x, y in zip(A, B)]}
+    for op in range(6):
+        assert engine.lib().gbntt_debug_modops(4, op, da.ptr, db.ptr, dout.ptr, n, None) == 0
+        cudart.stream_sync(engine.lib().gbntt_stream())
+        got = [int(v) for v in dout.download(np.uint64, n)]
+        assert [v % p for v in got] == want[op % 3], op
+        if op >= 3:
+            assert got == want[op % 3], op   # the plain forms return canonical values
+    for buf in (da, db, dout):
+        buf.free()
+
+
 def test_device_modops_p3(engine):
     # the 32-bit prime p3 = 3 * 2^30 + 1 (signed Montgomery, R = 2^32): PTX
     # and plain forms against Python integers, corners included
