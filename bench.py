@@ -558,7 +558,9 @@ def run_gpu(args, dist):
     tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if os.path.exists(tp):
         try:
-            traffic = json.load(open(tp)).get("ntt_pass_kernel_bytes_per_launch")
+            tj = json.load(open(tp))
+            traffic = tj.get("ntt_pass_kernel_bytes_per_launch" if g.prime_set() == 2 else
+                             "three_prime_64bit_bytes_per_launch")
         except (ValueError, OSError):
             traffic = None
     bm = bytes_model(lg)

@@ -329,6 +329,56 @@ __device__ __forceinline__ uint64_t gl_mul(uint64_t a, uint64_t b)
     return r;
 }
 
+// (v1:v0) + v2 EPS - v3 mod q0 (the value of v0 + v1 2^32 + v2 2^64 +
+// v3 2^96), canonical.
+__device__ __forceinline__ uint64_t gl_reduce4(uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3)
+{
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 x0, x1, bw, y0, y1, r0, r1, c, t0, t1, c2;\n\t"
+        "sub.cc.u32 x0, %1, %4;\n\t"
+        "subc.cc.u32 x1, %2, 0;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "mad.lo.cc.u32 x0, bw, 0xFFFFFFFF, x0;\n\t"
+        "madc.lo.u32 x1, bw, 1, x1;\n\t"
+        "sub.cc.u32 y0, 0, %3;\n\t"
+        "subc.u32 y1, %3, 0;\n\t"
+        "add.cc.u32 r0, x0, y0;\n\t"
+        "addc.cc.u32 r1, x1, y1;\n\t"
+        "addc.u32 c, 0, 0;\n\t"
+        "mad.lo.cc.u32 r0, c, 0xFFFFFFFF, r0;\n\t"
+        "addc.u32 r1, r1, 0;\n\t"
+        "add.cc.u32 t0, r0, 0xFFFFFFFF;\n\t"
+        "addc.cc.u32 t1, r1, 0;\n\t"
+        "addc.u32 c2, 0, 0;\n\t"
+        "mad.lo.cc.u32 r0, c2, 0xFFFFFFFF, r0;\n\t"
+        "addc.u32 r1, r1, 0;\n\t"
+        "mov.b64 %0, {r0, r1};\n\t"
+        "}"
+        : "=l"(r) : "r"(v0), "r"(v1), "r"(v2), "r"(v3));
+    return r;
+}
+
+// x * 2^e mod q0 for canonical x and 0 <= e < 96 (e folds to a constant
+// after unrolling, so the shifts and the branch on e / 32 vanish). In q0
+// every 64th root of unity is a power of two (2^96 == -1, 2^192 == 1), so
+// the register DFTs multiply by these instead of full products.
+__device__ __forceinline__ uint64_t gl_mul_pow2(uint64_t x, int e)
+{
+    if (e == 0) return x;
+    const uint32_t x0 = (uint32_t)x, x1 = (uint32_t)(x >> 32);
+    const int q = e >> 5, r = e & 31;
+    const uint32_t u0 = x0 << r;
+    const uint32_t u1 = r ? ((x1 << r) | (x0 >> (32 - r))) : x1;
+    const uint32_t u2 = r ? (x1 >> (32 - r)) : 0u;
+    if (q == 0) return gl_reduce4(u0, u1, u2, 0u);
+    if (q == 1) return gl_reduce4(0u, u0, u1, u2);
+    // q == 2: u0 2^64 + u1 2^96 + u2 2^128 == u0 EPS - (u2 2^32 + u1), the
+    // subtrahend below 2^63 < q0
+    const uint64_t y = ((uint64_t)u0 << 32) - (uint64_t)u0;   // u0 EPS < q0
+    return sub_mod<0>(y, ((uint64_t)u2 << 32) | u1);
+}
+
 // canonical representative in [0, q0)
 __host__ __device__ __forceinline__ uint64_t gl_canon(uint64_t x)
 {

@@ -317,6 +317,15 @@ static int init_impl(int max_log)
             for (int i = 0; i < 64; i++) { w64[pi][dir][i] = normal ? z : h_mont(z, p); z = h_mul(z, r64, p); }
         }
     }
+    // the q0 pass kernels multiply by w_64^k as the powers of two 2^(39k)
+    // (inverse 2^(153k)): the root must be the one those exponents assume
+    if (w64[0][0][1] != h_mont(h_pow(2, 39, prime_value(0)), prime_value(0)) ||
+        w64[0][1][1] != h_mont(h_pow(2, 153, prime_value(0)), prime_value(0))) {
+        free(h);
+        set_err("gbntt_init: q0 root of unity does not match the power-of-two DFT constants");
+        free_all();
+        return GBNTT_ERR_ARG;
+    }
     cudaError_t e = cudaMemcpy(g.d_tw, h, tw_words * sizeof(uint64_t), cudaMemcpyHostToDevice);
     free(h);
     if (e != cudaSuccess) { set_err("gbntt_init: twiddle upload failed: %s", cudaGetErrorString(e)); free_all(); return GBNTT_ERR_CUDA; }

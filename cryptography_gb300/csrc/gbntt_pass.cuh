@@ -81,7 +81,7 @@ __device__ __forceinline__ typename Field<PI>::T tw_exp(const typename Field<PI>
 // In-register radix-2 DIF DFT of 2^LOG_R points: natural order in,
 // bit-reversed order out (X[k] ends in x[bitrev(k)]). w64 = Montgomery forms
 // of the primitive 64th root's powers.
-template <int PI, int LOG_R>
+template <int PI, int LOG_R, int DIR>
 __device__ __forceinline__ void dft_reg(typename Field<PI>::T (&x)[1 << LOG_R], const uint64_t *w64)
 {
     using F = Field<PI>;
@@ -95,9 +95,19 @@ __device__ __forceinline__ void dft_reg(typename Field<PI>::T (&x)[1 << LOG_R], 
             for (int i = 0; i < s; i++) {
                 const T u = x[blk + i], v = x[blk + i + s];
                 x[blk + i] = F::add(u, v);
-                const T d = F::sub(u, v);
                 // w_{2s}^i = w_64^(i * 32 / s)
-                x[blk + i + s] = (i == 0) ? d : F::mul(d, (T)w64[i * (32 / s)]);
+                const int k = i * (32 / s);
+                if constexpr (PI == 0) {
+                    // q0's w_64 is 2^39 (inverse: 2^-39 = 2^153); 2^96 == -1,
+                    // so a power 2^e with e >= 96 is -2^(e-96): swap u and v
+                    const int e = (DIR == 0 ? 39 * k : 153 * k) % 192;
+                    if (k == 0) x[blk + i + s] = F::sub(u, v);
+                    else if (e < 96) x[blk + i + s] = gl_mul_pow2(F::sub(u, v), e);
+                    else x[blk + i + s] = gl_mul_pow2(F::sub(v, u), e - 96);
+                } else {
+                    const T d = F::sub(u, v);
+                    x[blk + i + s] = (k == 0) ? d : F::mul(d, (T)w64[k]);
+                }
             }
         }
     }
@@ -208,7 +218,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
                 if (i + 1 < A) base = F::mul(base, step);
             }
         }
-        dft_reg<PI, S_::LOG_A>(x, w64);
+        dft_reg<PI, S_::LOG_A, DIR>(x, w64);
 #pragma unroll
         for (int ka = 0; ka < A; ka++) {
             V v = x[bitrev(ka, S_::LOG_A)];
@@ -234,7 +244,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
             const int ka = q + r * B;
 #pragma unroll
             for (int i = 0; i < B; i++) y[r][i] = sm[g * RS + ka * (B + 1) + i];
-            dft_reg<PI, LOG_B>(y[r], w64);
+            dft_reg<PI, LOG_B, DIR>(y[r], w64);
             if (DIR == 0 && LAYOUT == LAYOUT_STRIDED && a.twiddle) {
                 // forward pass: output twiddle w_M^((ka + A kb) j)
                 const uint64_t j = j0 + (uint64_t)g;
