@@ -135,6 +135,23 @@ __device__ __forceinline__ uint64_t limb32_at(const PassArgs &a, long long addr)
     return addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
 }
 
+#ifndef GBNTT_PASS_CPASYNC
+#define GBNTT_PASS_CPASYNC 1   // plain residue loads go global -> shared through cp.async
+#endif
+
+// asynchronous global -> shared copy of one residue word (no register
+// staging, so every load of a thread can be in flight at once)
+template <int BYTES>
+__device__ __forceinline__ void cp_async_word(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;\n" ::: "memory");
+}
+
 // value of tile element at address addr for the load kind LD
 template <int PI, int LD>
 __device__ __forceinline__ typename Field<PI>::T load_elem(const PassArgs &a, const typename Field<PI>::T *data,
@@ -179,7 +196,11 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
         const long long stepg = (long long)B * S;
         V *dst = sm + g * RS + m0;
-        if constexpr (sizeof(V) == 4) {   // all A loads in flight (registers allow it)
+        if constexpr (LD == LD_U64 && GBNTT_PASS_CPASYNC) {
+#pragma unroll
+            for (int it = 0; it < A; it++) cp_async_word<sizeof(V)>(dst + it * (B + 1), data + base + it * stepg);
+            cp_async_wait_all();
+        } else if constexpr (sizeof(V) == 4) {   // all A loads in flight (registers allow it)
 #pragma unroll
             for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
         } else {
@@ -189,13 +210,25 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
     } else {
         const long long rows_left = a.ncols - col0;
         const long long base = col0 << LOG_L;
+        if constexpr (LD == LD_U64 && GBNTT_PASS_CPASYNC) {
+#pragma unroll
+            for (int it = 0; it < A; it++) {
+                const int e = t + it * T;
+                const int g = e >> LOG_L, m = e & (L - 1);
+                V *d = sm + g * RS + m + (m >> LOG_B);
+                if (g < rows_left) cp_async_word<sizeof(V)>(d, data + base + e);
+                else *d = 0;
+            }
+            cp_async_wait_all();
+        } else {
 #pragma unroll 8
-        for (int it = 0; it < A; it++) {
-            const int e = t + it * T;
-            const int g = e >> LOG_L, m = e & (L - 1);
-            V v = 0;
-            if (g < rows_left) v = load_elem<PI, LD>(a, data, other, base + e);
-            sm[g * RS + m + (m >> LOG_B)] = v;
+            for (int it = 0; it < A; it++) {
+                const int e = t + it * T;
+                const int g = e >> LOG_L, m = e & (L - 1);
+                V v = 0;
+                if (g < rows_left) v = load_elem<PI, LD>(a, data, other, base + e);
+                sm[g * RS + m + (m >> LOG_B)] = v;
+            }
         }
     }
     __syncthreads();
