@@ -71,6 +71,7 @@ struct Engine {
     int prime_set = 2;              // primes used for 32-bit coefficients: 2 or 3
     bool q0_lazy = false;           // two-prime set: q0 as prime 4 (lazy normal form) or 0 (Montgomery)
     bool overlap = true;            // two-prime set: second prime's passes on stream2
+    bool zero_copy = true;          // host-pointer calls: kernels read/write pinned host memory directly
     uint64_t garner2[2] = {0, 0};   // two-prime Garner constants (p3 Montgomery multipliers)
     unsigned *d_ctl = nullptr;      // [0] ticket, [1] error, [2..] tile status
     size_t n_status = 0;
@@ -381,6 +382,10 @@ static int init_impl(int max_log)
         g.q0_lazy = qf && qf[0] == 'l';
         const char *ov = getenv("GBNTT_OVERLAP");
         g.overlap = !(ov && ov[0] == '0');
+        // (measured at 2^28 limbs through ntt_bigint_mul: 105 ms against 110 ms
+        // through the staging buffer)
+        const char *zc = getenv("GBNTT_ZERO_COPY");
+        g.zero_copy = !(zc && zc[0] == '0');
     }
     g.ready = true;
     return GBNTT_OK;
@@ -414,7 +419,8 @@ static double word_bytes(int pi) { return pi == 3 ? 4.0 : 8.0; }
 // and inverse take the forked stream (nullptr: everything on st).
 static cudaStream_t fork_aux(const PrimeSet &ps, cudaStream_t st, cudaStream_t aux)
 {
-    if (!aux || ps.n != 2 || !g.overlap) return nullptr;
+    // per-launch event records (launch_log) need the launches serialised
+    if (!aux || ps.n != 2 || !g.overlap || g_rec_on) return nullptr;
     if (cudaEventRecord(g.ev_fork, st) != cudaSuccess || cudaStreamWaitEvent(aux, g.ev_fork, 0) != cudaSuccess)
         return nullptr;
     return aux;
@@ -896,6 +902,18 @@ static int read_errors(unsigned *flags)
 }
 
 // Host-pointer product through the staging buffer (a, b, c contiguous).
+// Device address of page-locked host memory (NVLink-C2C makes it directly
+// readable and writable by kernels), or nullptr for other memory.
+static void *pinned_device_ptr(const void *p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 static int mul_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b, size_t nb,
                     const uint32_t *dev_a, const uint32_t *dev_b)
 {
@@ -910,14 +928,19 @@ static int mul_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b
     uint32_t *da = g.d_io, *db = g.d_io + na, *dc = g.d_io + na + (square ? 0 : nb);
     double t0 = g.prof ? now_ms() : 0;
     const uint32_t *ua = dev_a, *ub = dev_b;
+    // zero copy: pinned operands are read by the first forward passes and a
+    // pinned result is written by the carry kernel, over NVLink-C2C
+    if (!ua && g.zero_copy) ua = (const uint32_t *)pinned_device_ptr(a);
+    if (!ub && !square && g.zero_copy) ub = (const uint32_t *)pinned_device_ptr(b);
+    uint32_t *uc = g.zero_copy ? (uint32_t *)pinned_device_ptr(c) : nullptr;
     if (!ua) { CK(cudaMemcpyAsync(da, a, na * 4, cudaMemcpyHostToDevice, g.stream)); ua = da; }
     if (square) ub = ua;
     else if (!ub) { CK(cudaMemcpyAsync(db, b, nb * 4, cudaMemcpyHostToDevice, g.stream)); ub = db; }
     if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[0] += t - t0; t0 = t; }
-    int rc = mul_dev(dc, ua, na, ub, nb, g.stream);
+    int rc = mul_dev(uc ? uc : dc, ua, na, ub, nb, g.stream);
     if (rc) return rc;
     if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[1] += t - t0; t0 = t; }
-    CK(cudaMemcpyAsync(c, dc, n_out * 4, cudaMemcpyDeviceToHost, g.stream));
+    if (!uc) CK(cudaMemcpyAsync(c, dc, n_out * 4, cudaMemcpyDeviceToHost, g.stream));
     unsigned flags = 0;
     rc = read_errors(&flags);
     if (rc) return rc;
@@ -946,14 +969,17 @@ static int mul_host64(uint64_t *c, const uint64_t *a, size_t na, const uint64_t 
     uint64_t *da = io, *db = io + na, *dc = io + na + (square ? 0 : nb);
     double t0 = g.prof ? now_ms() : 0;
     const uint64_t *ua = dev_a, *ub = dev_b;
+    if (!ua && g.zero_copy) ua = (const uint64_t *)pinned_device_ptr(a);
+    if (!ub && !square && g.zero_copy) ub = (const uint64_t *)pinned_device_ptr(b);
+    uint64_t *uc = g.zero_copy ? (uint64_t *)pinned_device_ptr(c) : nullptr;
     if (!ua) { CK(cudaMemcpyAsync(da, a, na * 8, cudaMemcpyHostToDevice, g.stream)); ua = da; }
     if (square) ub = ua;
     else if (!ub) { CK(cudaMemcpyAsync(db, b, nb * 8, cudaMemcpyHostToDevice, g.stream)); ub = db; }
     if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[0] += t - t0; t0 = t; }
-    int rc = mul_dev64(dc, ua, na, ub, nb, g.stream);
+    int rc = mul_dev64(uc ? uc : dc, ua, na, ub, nb, g.stream);
     if (rc) return rc;
     if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[1] += t - t0; t0 = t; }
-    CK(cudaMemcpyAsync(c, dc, n_out * 8, cudaMemcpyDeviceToHost, g.stream));
+    if (!uc) CK(cudaMemcpyAsync(c, dc, n_out * 8, cudaMemcpyDeviceToHost, g.stream));
     unsigned flags = 0;
     rc = read_errors(&flags);
     if (rc) return rc;
@@ -1346,6 +1372,41 @@ int gbntt_device_errors(unsigned int *flags)
 {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    return read_errors(flags);
+}
+
+int gbntt_debug_lookback_timeout(unsigned int *flags, double *seconds)
+{
+    // The carry kernel over 3 tiles with its ticket counter started at 1: no
+    // CTA takes tile 0, so tile 1's look-back waits on a status word nothing
+    // writes. The wait is bounded; it must end, set ERR_LOOKBACK_TIMEOUT and
+    // leave the context usable. Output goes to the staging buffer.
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    long long n_out = 1;
+    while (carry_tiles(n_out) < 3) n_out *= 2;   // smallest power of two spanning three carry tiles
+    if ((size_t)n_out > g.io_words || (long long)g.n_max < n_out) {
+        set_err("engine too small for the check");
+        return GBNTT_ERR_SIZE;
+    }
+    CK(cudaStreamSynchronize(g.stream));
+    CarryArgs c;
+    memset(&c, 0, sizeof c);
+    carry_setup(c, kSet3, g.d_spec, g.n_max);
+    c.out = g.d_io;
+    c.n_coef = n_out;
+    c.n_out = n_out;
+    c.ticket = g.d_ctl;
+    c.error = g.d_ctl + 1;
+    c.status = g.d_ctl + 2;
+    const unsigned start[2] = {1u, 0u};
+    CK(cudaMemsetAsync(g.d_ctl + 2, 0, 8 * sizeof(unsigned), g.stream));
+    CK(cudaMemcpyAsync(g.d_ctl, start, sizeof start, cudaMemcpyHostToDevice, g.stream));
+    CK(cudaStreamSynchronize(g.stream));
+    const double t0 = now_ms();
+    CK(launch_garner_carry(c, g.stream, nullptr));
+    CK(cudaStreamSynchronize(g.stream));
+    if (seconds) *seconds = (now_ms() - t0) * 1e-3;
     return read_errors(flags);
 }
 

@@ -46,7 +46,7 @@ EXPORTS = (
     "gbntt_server_stop",
     "gbntt_split_terms_needed", "gbntt_e_required_log", "gbntt_binary_split", "gbntt_newton_reciprocal_u32",
     "gbntt_div_newton_u32", "gbntt_pow10_u32", "gbntt_to_decimal_u32", "gbntt_compute_e",
-    "gbntt_set_prime_set", "gbntt_prime_set",
+    "gbntt_set_prime_set", "gbntt_prime_set", "gbntt_debug_lookback_timeout",
 )
 
 _lib = None
@@ -157,6 +157,8 @@ def lib():
     L.gbntt_set_prime_set.argtypes = [ctypes.c_int]
     L.gbntt_set_prime_set.restype = ctypes.c_int
     L.gbntt_prime_set.restype = ctypes.c_int
+    L.gbntt_debug_lookback_timeout.argtypes = [ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_double)]
+    L.gbntt_debug_lookback_timeout.restype = ctypes.c_int
     L.gbntt_last_error.restype = ctypes.c_char_p
     L.gbntt_stream.restype = _vp
     _lib = L

@@ -185,6 +185,15 @@ int gbntt_device_errors(unsigned int *flags);
  * tests. d_out needs 3 * 2^log_n entries. */
 int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log_n, void *stream);
 
+/* Self-test of the bounded waits (no reference counterpart): runs the
+ * Garner+carry kernel over a few tiles with its tile ticket started past
+ * tile 0, so one look-back waits on a status word that nothing writes; the
+ * wait gives up after its iteration limit, the kernel finishes and *flags
+ * receives the device error bits (bit 1: a look-back wait gave up).
+ * *seconds receives the kernel's wall time. Needs an engine of at least
+ * 2^13 coefficients. The context stays usable. */
+int gbntt_debug_lookback_timeout(unsigned int *flags, double *seconds);
+
 /* Element-wise modular arithmetic on device arrays for self-tests: for
  * prime index 0..2 (2^64 - 2^b + 1, b = 32, 34, 40) and op 0 = (a+b) mod p,
  * 1 = (a-b) mod p, 2 = a*b*2^-64 mod p (Montgomery), 3..5 = the same with

@@ -159,3 +159,38 @@ def test_checked_variant_returns_codes():
     assert r.returncode == 0, r.stderr
     rc, _ = json.loads(r.stdout.strip().splitlines()[-1])
     assert rc == 2   # GBNTT_ERR_SIZE
+
+
+@pytest.mark.parametrize("zero_copy", ["1", "0"])
+def test_bigint_mul_pinned_host_buffers(zero_copy):
+    # page-locked BigInts: with zero copy the kernels read the operands and
+    # write the product over NVLink-C2C; without it they go through the
+    # staging buffer. Both must give the exact product.
+    r = run("""
+        import numpy as np
+        from cryptography_gb300 import cudart
+        L.ntt_mul_init_impl(20)
+        rng = random.Random(11)
+        out = []
+        u64p = ctypes.POINTER(ctypes.c_uint64)
+        for na, nb in [(1, 1), (7, 5), (4096, 4093), ((1 << 18) + 3, (1 << 18) - 9)]:
+            x, y = rnd(rng, na), rnd(rng, nb)
+            pa, pb = cudart.PinnedBuffer(na, np.uint64), cudart.PinnedBuffer(nb, np.uint64)
+            pc = cudart.PinnedBuffer(na + nb + 8, np.uint64)
+            pa.array[:] = np.frombuffer(x.to_bytes(8 * na, "little"), dtype=np.uint64)
+            pb.array[:] = np.frombuffer(y.to_bytes(8 * nb, "little"), dtype=np.uint64)
+            pc.array[:] = 0xAAAAAAAAAAAAAAAA
+            a = g.BigInt(ctypes.cast(pa.ptr, u64p), na, na, 0)
+            b = g.BigInt(ctypes.cast(pb.ptr, u64p), nb, nb, 0)
+            c = g.BigInt(ctypes.cast(pc.ptr, u64p), 0, na + nb + 8, 0)
+            L.ntt_bigint_mul(B(c), B(a), B(b))
+            ok = int.from_bytes(pc.array[:c.n_limbs].tobytes(), "little") == x * y
+            out.append([na, nb, ok, int(c.limbs[0] == pc.array[0]), bool((pc.array[c.n_limbs:] == 0).all())])
+            for p in (pa, pb, pc):
+                p.free()
+        print(json.dumps(out))
+        L.ntt_mul_teardown_impl()
+    """, env={"GBNTT_ZERO_COPY": zero_copy})
+    assert r.returncode == 0, r.stderr
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    assert all(ok and same and zeros for _, _, ok, same, zeros in res), res
