@@ -592,7 +592,10 @@ def run_gpu(args, dist):
         t_e2e = dist.max(t_e2e)
         e2e = {"value": t_e2e / (args.e2e_steps * dist.world), "unit": UNIT, "h2d_bytes_per_step": 8 * n,
                "d2h_bytes_per_step": 8 * n, "api": "ntt_bigint_mul (pinned host BigInts)",
-               "steps": args.e2e_steps, "per_step_ms": [round(x, 2) for x in per]}
+               "steps": args.e2e_steps, "per_step_ms": [round(x, 2) for x in per],
+               "transfer": "zero copy: the first forward passes read the pinned operands and the carry kernel "
+                           "writes the pinned result over NVLink-C2C" if os.environ.get("GBNTT_ZERO_COPY", "1") != "0"
+                           else "cudaMemcpyAsync through the engine's staging buffer"}
         if C.cap != 2 * n64 + 8 or C.n_limbs != 2 * n64:
             e2e["warning"] = "unexpected output size"
         for p_ in (pa, pb, pc):
