@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--no-three-prime", action="store_true",
                     help="skip timing the same multiply with the reference's three 64-bit primes")
     ap.add_argument("--three-prime-steps", type=int, default=5)
+    ap.add_argument("--no-square", action="store_true", help="skip the squaring and 2^20-limb legs")
     ap.add_argument("--no-e", action="store_true", help="skip the e-digits leg")
     ap.add_argument("--e-digits", type=int, default=10 ** 8)
     ap.add_argument("--e-reps", type=int, default=3)
@@ -493,6 +494,49 @@ def run_gpu(args, dist):
                  "primes": "2^64-2^b+1, b = 32, 34, 40 (the reference's set; 64-bit residues)",
                  "note": "same product, same transform length; the headline uses two primes"}
 
+    # squaring of the same operand (one forward transform), reported apart
+    square = small = None
+    if not args.no_square:
+        def sq_step():
+            g.mul_device(dc.ptr, da.ptr, n, da.ptr, n, None)
+        for _ in range(2):
+            sq_step()
+        s0, s1 = cudart.Event(), cudart.Event()
+        dist.barrier()
+        s0.record(stream)
+        for _ in range(args.steps):
+            sq_step()
+        s1.record(stream)
+        s1.synchronize()
+        dist.barrier()
+        sq_ms = dist.max(s0.elapsed_ms(s1)) / (args.steps * dist.world)
+        bm_sq = 6 * 3 * (1 << (lg + 1)) * 8 + 12 * n
+        square = {"ms": sq_ms, "bytes_model": bm_sq, "model": "6*k*N*8 + 12*n, k=3",
+                  "frac": bm_sq / (sq_ms * 1e-3) / 1e9 / peaks()[0]}
+        # the 2^20 x 2^20-limb product (N = 2^21), checked against GMP
+        ns = 1 << 20
+        xa, xb = synth.operand(ns, 11), synth.operand(ns, 12)
+        sa, sb, sc = cudart.DeviceBuffer(4 * ns), cudart.DeviceBuffer(4 * ns), cudart.DeviceBuffer(8 * ns)
+        sa.upload(xa)
+        sb.upload(xb)
+        for _ in range(3):
+            g.mul_device(sc.ptr, sa.ptr, ns, sb.ptr, ns, None)
+        k0, k1 = cudart.Event(), cudart.Event()
+        reps = 50
+        k0.record(stream)
+        for _ in range(reps):
+            g.mul_device(sc.ptr, sa.ptr, ns, sb.ptr, ns, None)
+        k1.record(stream)
+        k1.synchronize()
+        sm_ms = k0.elapsed_ms(k1) / reps
+        bm_small = 10 * 3 * (1 << 21) * 8 + 8 * (2 * ns)
+        small = {"ms": sm_ms, "operand_limbs": ns, "transform_log": 21, "steps": reps,
+                 "bytes_model": bm_small, "frac": bm_small / (sm_ms * 1e-3) / 1e9 / peaks()[0],
+                 "parity": "tests/test_gpu_parity.py checks this size against GMP"}
+        for buf in (sa, sb, sc):
+            buf.free()
+        flags |= g.device_errors()
+
     # packed mode (one 64-bit limb per coefficient, transform length 2^lg)
     packed = None
     if not args.no_packed:
@@ -634,6 +678,8 @@ def run_gpu(args, dist):
                               "model_own_primes": "the same model with this run's residue words "
                                                   "(%d bytes per coefficient over all primes)" % res_bytes},
         "three_prime_64bit": three,
+        "square": square,
+        "multiply_2pow20": small,
         "packed_64bit_coefficients": packed,
         "batched": batched,
         "serving": serving,
