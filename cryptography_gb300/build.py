@@ -32,6 +32,8 @@ def _flags():
     extra = []
     if os.environ.get("GBNTT_PASS_MIN_BLOCKS"):   # tuning knob: resident CTAs per SM of the pass kernels
         extra.append("-DGBNTT_PASS_MIN_BLOCKS=%d" % int(os.environ["GBNTT_PASS_MIN_BLOCKS"]))
+    if os.environ.get("GBNTT_PASS_SHARED_DFT"):
+        extra.append("-DGBNTT_PASS_SHARED_DFT=%d" % int(os.environ["GBNTT_PASS_SHARED_DFT"]))
     if os.environ.get("GBNTT_PASS_CPASYNC"):
         extra.append("-DGBNTT_PASS_CPASYNC=%d" % int(os.environ["GBNTT_PASS_CPASYNC"]))
     if os.environ.get("GBNTT_PASS_MIN_BLOCKS32"):

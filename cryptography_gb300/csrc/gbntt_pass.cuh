@@ -135,6 +135,9 @@ __device__ __forceinline__ uint64_t limb32_at(const PassArgs &a, long long addr)
     return addr < a.n_limbs ? (uint64_t)__ldg(a.limbs + addr) : 0ull;
 }
 
+#ifndef GBNTT_PASS_SHARED_DFT
+#define GBNTT_PASS_SHARED_DFT 1   // even l: one loop body for both DFT steps
+#endif
 #ifndef GBNTT_PASS_CPASYNC
 #define GBNTT_PASS_CPASYNC 1   // plain residue loads go global -> shared through cp.async
 #endif
@@ -233,6 +236,56 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
     }
     __syncthreads();
 
+    if constexpr (S_::A == S_::B && GBNTT_PASS_SHARED_DFT) {
+        // Even l: both steps are A-point DFTs whose outputs go to
+        // sm[g RS + k (B + 1) + lane]; only the read differs (column, then
+        // row). One loop body keeps a single copy of the unrolled DFT code.
+        const int g = t >> LOG_B, lane = t & (B - 1);
+        const uint64_t jg = j0 + (uint64_t)(LAYOUT == LAYOUT_STRIDED ? g : 0);
+#pragma unroll 1
+        for (int phase = 0; phase < 2; phase++) {
+            V x[A];
+            const int rbase = g * RS + (phase == 0 ? lane : lane * (B + 1));
+            const int rstride = phase == 0 ? (B + 1) : 1;
+#pragma unroll
+            for (int i = 0; i < A; i++) x[i] = sm[rbase + i * rstride];
+            if (DIR == 1 && phase == 0 && (a.twiddle || a.use_scale)) {
+                // inverse pass: input twiddle w_M^-((iB + lane) j), times the scale
+                V base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)lane * jg) << sh));
+                const V step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * jg) << sh));
+                if (a.use_scale) base = F::mul(base, (V)a.scale[F::SLOT]);
+#pragma unroll
+                for (int i = 0; i < A; i++) {
+                    x[i] = F::mul(x[i], base);
+                    if (i + 1 < A) base = F::mul(base, step);
+                }
+            }
+            dft_reg<PI, S_::LOG_A, DIR>(x, w64);
+            if (phase == 0) {
+                if (lane > 0) {   // w_L^(lane ka)
+#pragma unroll
+                    for (int ka = 1; ka < A; ka++) {
+                        const int idx = bitrev(ka, S_::LOG_A);
+                        x[idx] = F::mul(x[idx], __ldg(twhi + ((lane * ka) << (kTwBits - LOG_L))));
+                    }
+                }
+            } else if (DIR == 0 && LAYOUT == LAYOUT_STRIDED && a.twiddle) {
+                // forward pass: output twiddle w_M^((lane + A kb) j)
+                const V step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)A * jg) << sh));
+                V base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)lane * jg) << sh));
+#pragma unroll
+                for (int kb = 0; kb < B; kb++) {
+                    const int idx = bitrev(kb, LOG_B);
+                    x[idx] = F::mul(x[idx], base);
+                    if (kb + 1 < B) base = F::mul(base, step);
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < A; k++) sm[g * RS + k * (B + 1) + lane] = x[bitrev(k, S_::LOG_A)];
+            __syncthreads();
+        }
+    } else {
     // ---- step 1: one A-point DFT per (g, b) over the high digit
     {
         const int g = t >> LOG_B, b = t & (B - 1);
@@ -302,6 +355,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         }
     }
     __syncthreads();
+    }
 
     // ---- store: same addressing as the load
     if (LAYOUT == LAYOUT_STRIDED) {
