@@ -269,16 +269,6 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
                         x[idx] = F::mul(x[idx], __ldg(twhi + ((lane * ka) << (kTwBits - LOG_L))));
                     }
                 }
-            } else if (DIR == 0 && LAYOUT == LAYOUT_STRIDED && a.twiddle) {
-                // forward pass: output twiddle w_M^((lane + A kb) j)
-                const V step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)A * jg) << sh));
-                V base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)lane * jg) << sh));
-#pragma unroll
-                for (int kb = 0; kb < B; kb++) {
-                    const int idx = bitrev(kb, LOG_B);
-                    x[idx] = F::mul(x[idx], base);
-                    if (kb + 1 < B) base = F::mul(base, step);
-                }
             }
             __syncthreads();
 #pragma unroll
@@ -320,28 +310,12 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         constexpr int R = A / B;
         const int g = t >> LOG_B, q = t & (B - 1);
         V y[R][B];
-        V step = 0;
-        if (DIR == 0 && LAYOUT == LAYOUT_STRIDED && a.twiddle) {
-            const uint64_t j = j0 + (uint64_t)g;
-            step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)A * j) << sh));
-        }
 #pragma unroll
         for (int r = 0; r < R; r++) {
             const int ka = q + r * B;
 #pragma unroll
             for (int i = 0; i < B; i++) y[r][i] = sm[g * RS + ka * (B + 1) + i];
             dft_reg<PI, LOG_B, DIR>(y[r], w64);
-            if (DIR == 0 && LAYOUT == LAYOUT_STRIDED && a.twiddle) {
-                // forward pass: output twiddle w_M^((ka + A kb) j)
-                const uint64_t j = j0 + (uint64_t)g;
-                V base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)ka * j) << sh));
-#pragma unroll
-                for (int kb = 0; kb < B; kb++) {
-                    const int idx = bitrev(kb, LOG_B);
-                    y[r][idx] = F::mul(y[r][idx], base);
-                    if (kb + 1 < B) base = F::mul(base, step);
-                }
-            }
         }
         __syncthreads();
 #pragma unroll
@@ -364,8 +338,22 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
         const long long stepg = (long long)B * S;
         const V *src = sm + g * RS + m0;
+        if (DIR == 0 && a.twiddle) {
+            // forward pass: output k = m0 + it B of column j gets w_M^(j k),
+            // applied here (a partly rolled loop) instead of in the
+            // unrolled register step
+            const uint64_t j = j0 + (uint64_t)g;
+            V tw = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)m0 * j) << sh));
+            const V step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * j) << sh));
+#pragma unroll 4
+            for (int it = 0; it < A; it++) {
+                data[base + it * stepg] = F::mul(src[it * (B + 1)], tw);
+                tw = F::mul(tw, step);
+            }
+        } else {
 #pragma unroll 8
-        for (int it = 0; it < A; it++) data[base + it * stepg] = src[it * (B + 1)];
+            for (int it = 0; it < A; it++) data[base + it * stepg] = src[it * (B + 1)];
+        }
     } else {
         const long long rows_left = a.ncols - col0;
         const long long base = col0 << LOG_L;
