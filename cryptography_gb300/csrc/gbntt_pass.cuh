@@ -234,6 +234,42 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
             }
         }
     }
+    if (DIR == 1 && (a.twiddle || a.use_scale)) {
+        // inverse pass: input row m of column j gets w_M^-(j m), times the
+        // scale in the last pass; each thread scales the words it loaded (a
+        // partly rolled loop instead of the unrolled register step)
+        if (LAYOUT == LAYOUT_STRIDED) {
+            const int g = t & (G - 1), m0 = t >> LOG_G;
+            const uint64_t j = j0 + (uint64_t)g;
+            V *dst = sm + g * RS + m0;
+            if (a.twiddle) {
+                V tw = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)m0 * j) << sh));
+                const V step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * j) << sh));
+                if (a.use_scale) tw = F::mul(tw, (V)a.scale[F::SLOT]);
+#pragma unroll 4
+                for (int it = 0; it < A; it++) {
+                    dst[it * (B + 1)] = F::mul(dst[it * (B + 1)], tw);
+                    tw = F::mul(tw, step);
+                }
+            } else {
+                const V sc = (V)a.scale[F::SLOT];
+#pragma unroll 4
+                for (int it = 0; it < A; it++) dst[it * (B + 1)] = F::mul(dst[it * (B + 1)], sc);
+            }
+        } else {   // contiguous: no twiddle (S = 1), only the scale
+            const long long rows_left = a.ncols - col0;
+            const V sc = (V)a.scale[F::SLOT];
+#pragma unroll 4
+            for (int it = 0; it < A; it++) {
+                const int e = t + it * T;
+                const int g = e >> LOG_L, m = e & (L - 1);
+                if (g < rows_left) {
+                    V *d = sm + g * RS + m + (m >> LOG_B);
+                    *d = F::mul(*d, sc);
+                }
+            }
+        }
+    }
     __syncthreads();
 
     if constexpr (S_::A == S_::B && GBNTT_PASS_SHARED_DFT) {
@@ -241,7 +277,6 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         // sm[g RS + k (B + 1) + lane]; only the read differs (column, then
         // row). One loop body keeps a single copy of the unrolled DFT code.
         const int g = t >> LOG_B, lane = t & (B - 1);
-        const uint64_t jg = j0 + (uint64_t)(LAYOUT == LAYOUT_STRIDED ? g : 0);
 #pragma unroll 1
         for (int phase = 0; phase < 2; phase++) {
             V x[A];
@@ -249,17 +284,6 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
             const int rstride = phase == 0 ? (B + 1) : 1;
 #pragma unroll
             for (int i = 0; i < A; i++) x[i] = sm[rbase + i * rstride];
-            if (DIR == 1 && phase == 0 && (a.twiddle || a.use_scale)) {
-                // inverse pass: input twiddle w_M^-((iB + lane) j), times the scale
-                V base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)lane * jg) << sh));
-                const V step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * jg) << sh));
-                if (a.use_scale) base = F::mul(base, (V)a.scale[F::SLOT]);
-#pragma unroll
-                for (int i = 0; i < A; i++) {
-                    x[i] = F::mul(x[i], base);
-                    if (i + 1 < A) base = F::mul(base, step);
-                }
-            }
             dft_reg<PI, S_::LOG_A, DIR>(x, w64);
             if (phase == 0) {
                 if (lane > 0) {   // w_L^(lane ka)
@@ -282,18 +306,6 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         V x[A];
 #pragma unroll
         for (int i = 0; i < A; i++) x[i] = sm[g * RS + i * (B + 1) + b];
-        if (DIR == 1 && (a.twiddle || a.use_scale)) {
-            // inverse pass: input twiddle w_M^-((iB + b) j), times the scale
-            const uint64_t j = j0 + (uint64_t)(LAYOUT == LAYOUT_STRIDED ? g : 0);
-            V base = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)b * j) << sh));
-            const V step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * j) << sh));
-            if (a.use_scale) base = F::mul(base, (V)a.scale[F::SLOT]);
-#pragma unroll
-            for (int i = 0; i < A; i++) {
-                x[i] = F::mul(x[i], base);
-                if (i + 1 < A) base = F::mul(base, step);
-            }
-        }
         dft_reg<PI, S_::LOG_A, DIR>(x, w64);
 #pragma unroll
         for (int ka = 0; ka < A; ka++) {
