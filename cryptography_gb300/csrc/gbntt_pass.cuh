@@ -321,22 +321,47 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
     {
         constexpr int R = A / B;
         const int g = t >> LOG_B, q = t & (B - 1);
-        V y[R][B];
+        if constexpr (R == 2 && GBNTT_PASS_SHARED_DFT) {
+            // odd l: the two B-point DFTs of a thread run through one loop
+            // body (one copy of the unrolled code); the first result waits
+            // in y0 until the barrier, the second stays in z
+            V y0[B], z[B];
+#pragma unroll 1
+            for (int r = 0; r < 2; r++) {
+                const int ka = q + r * B;
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int ka = q + r * B;
+                for (int i = 0; i < B; i++) z[i] = sm[g * RS + ka * (B + 1) + i];
+                dft_reg<PI, LOG_B, DIR>(z, w64);
+                if (r == 0) {
 #pragma unroll
-            for (int i = 0; i < B; i++) y[r][i] = sm[g * RS + ka * (B + 1) + i];
-            dft_reg<PI, LOG_B, DIR>(y[r], w64);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int ka = q + r * B;
+                    for (int i = 0; i < B; i++) y0[i] = z[i];
+                }
+            }
+            __syncthreads();
 #pragma unroll
             for (int kb = 0; kb < B; kb++) {
-                const int k = ka + A * kb;
-                sm[g * RS + k + (k >> LOG_B)] = y[r][bitrev(kb, LOG_B)];
+                const int k0 = q + A * kb, k1 = q + B + A * kb;
+                sm[g * RS + k0 + (k0 >> LOG_B)] = y0[bitrev(kb, LOG_B)];
+                sm[g * RS + k1 + (k1 >> LOG_B)] = z[bitrev(kb, LOG_B)];
+            }
+        } else {
+            V y[R][B];
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int ka = q + r * B;
+#pragma unroll
+                for (int i = 0; i < B; i++) y[r][i] = sm[g * RS + ka * (B + 1) + i];
+                dft_reg<PI, LOG_B, DIR>(y[r], w64);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int ka = q + r * B;
+#pragma unroll
+                for (int kb = 0; kb < B; kb++) {
+                    const int k = ka + A * kb;
+                    sm[g * RS + k + (k >> LOG_B)] = y[r][bitrev(kb, LOG_B)];
+                }
             }
         }
     }
