@@ -110,3 +110,43 @@ def test_synth_2pow22_both_sets(engine):
     c2, c3 = _both(engine, a, b)
     assert np.array_equal(c2, c3)
     assert np.array_equal(c2, _gmp(a, b))
+
+
+@pytest.mark.parametrize("knobs", [{"GBNTT_Q0_FORM": "lazy"}, {"GBNTT_OVERLAP": "0"},
+                                   {"GBNTT_Q0_FORM": "lazy", "GBNTT_OVERLAP": "0"}])
+def test_engine_knobs_give_identical_products(knobs):
+    # the tuning switches (lazy normal-form q0, no second-prime stream) change
+    # how the product is computed, never its value
+    import json
+    import os
+    import subprocess
+    import sys
+    import textwrap
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    body = textwrap.dedent("""
+        import json, sys
+        sys.path.insert(0, %r)
+        import numpy as np
+        import cryptography_gb300 as g
+        import oracle
+        g.init(22)
+        rng = np.random.default_rng(71)
+        ok = []
+        for na, nb in [(1, 1), (33, 17), (4096, 4095), (70000, 12345), ((1 << 20) + 1, (1 << 20) - 3)]:
+            a = rng.integers(0, 1 << 32, na, dtype=np.uint64).astype(np.uint32)
+            b = rng.integers(0, 1 << 32, nb, dtype=np.uint64).astype(np.uint32)
+            want = np.zeros(na + nb, dtype=np.uint32)
+            r = oracle.gmp_mul(a, b)
+            want[:len(r)] = r
+            ok.append(bool(np.array_equal(g.mul(a, b), want)))
+        full = np.full((1 << 20) - 1, 0xFFFFFFFF, dtype=np.uint32)
+        c = g.mul(full, full)
+        n = len(full)
+        ok.append(bool(c[0] == 1 and not c[1:n].any() and c[n] == 0xFFFFFFFE and (c[n + 1:] == 0xFFFFFFFF).all()))
+        print(json.dumps([ok, g.device_errors()]))
+    """ % root)
+    env = dict(os.environ, **knobs)
+    r = subprocess.run([sys.executable, "-c", body], capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    ok, errs = json.loads(r.stdout.strip().splitlines()[-1])
+    assert all(ok) and errs == 0, (knobs, ok)
