@@ -1,9 +1,9 @@
 """Full-size product (two 2^28-limb operands, transform length 2^29): too
 large for the oracle or GMP within a test budget, so it is checked through
 size-independent properties:
-  * the device Garner check (every coefficient's third mixed-radix digit
-    must be 0; a corrupted residue makes it nonzero with probability
-    ~1 - 2^-64) reports no error;
+  * the device Garner check reports no error (two primes: every
+    coefficient below N 2^64; three primes: the third mixed-radix digit
+    is 0);
   * the product agrees with the operands modulo several random 62-bit
     moduli (a checksum of the whole integer);
   * the low 2^20 limbs equal the low limbs of the GMP product of the low
