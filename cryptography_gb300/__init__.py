@@ -20,6 +20,7 @@ from .engine import (  # noqa: F401
     GBNTT_ERR_NOT_INIT,
     GBNTT_ERR_SIZE,
     GBNTT_OK,
+    autotune,
     batch_mul_device,
     bigint_alloc,
     bigint_free,
@@ -44,5 +45,6 @@ from .engine import (  # noqa: F401
     sqr,
     teardown,
     transform_log,
+    wave_graphs,
     workspace_bytes,
 )

@@ -9,7 +9,10 @@
 // twiddle tables are two-level (2 x 2^15 entries per prime and direction,
 // L2-resident) instead of O(N) host-built tables (ntt_mul.hip:189-308).
 #include <cuda_runtime.h>
+#include <array>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <vector>
 #include <algorithm>
 #include <atomic>
@@ -72,6 +75,7 @@ struct Engine {
     bool q0_lazy = false;           // two-prime set: q0 as prime 4 (lazy normal form) or 0 (Montgomery)
     bool overlap = true;            // two-prime set: second prime's passes on stream2
     bool zero_copy = true;          // host-pointer calls: kernels read/write pinned host memory directly
+    bool graphs = true;             // batched waves replayed as CUDA graphs
     uint64_t garner2[2] = {0, 0};   // two-prime Garner constants (p3 Montgomery multipliers)
     unsigned *d_ctl = nullptr;      // [0] ticket, [1] error, [2..] tile status
     size_t n_status = 0;
@@ -229,6 +233,8 @@ static size_t workspace_bytes(int max_log)
     return spec + tw + ctl + io;
 }
 
+static void invalidate_wave_graphs();
+
 static void free_all()
 {
     if (g.stream) cudaStreamSynchronize(g.stream);
@@ -245,6 +251,7 @@ static void free_all()
     if (g.ev_join) cudaEventDestroy(g.ev_join);
     if (g.stream2) cudaStreamDestroy(g.stream2);
     if (g.stream) cudaStreamDestroy(g.stream);
+    invalidate_wave_graphs();
     g = Engine();
 }
 
@@ -384,6 +391,8 @@ static int init_impl(int max_log)
         g.overlap = !(ov && ov[0] == '0');
         // (measured at 2^28 limbs through ntt_bigint_mul: 105 ms against 110 ms
         // through the staging buffer)
+        const char *gr = getenv("GBNTT_GRAPHS");
+        g.graphs = !(gr && gr[0] == '0');
         const char *zc = getenv("GBNTT_ZERO_COPY");
         g.zero_copy = !(zc && zc[0] == '0');
     }
@@ -417,10 +426,14 @@ static double word_bytes(int pi) { return pi == 3 ? 4.0 : 8.0; }
 // Garner+carry kernel, so the two primes' transforms share the SMs (q0's
 // kernels are bound by the integer pipes, p3's by memory latency). forward
 // and inverse take the forked stream (nullptr: everything on st).
-static cudaStream_t fork_aux(const PrimeSet &ps, cudaStream_t st, cudaStream_t aux)
+static bool aux_used(const PrimeSet &ps, cudaStream_t aux)
 {
     // per-launch event records (launch_log) need the launches serialised
-    if (!aux || ps.n != 2 || !g.overlap || g_rec_on) return nullptr;
+    return aux && ps.n == 2 && g.overlap && !g_rec_on;
+}
+static cudaStream_t fork_aux(const PrimeSet &ps, cudaStream_t st, cudaStream_t aux)
+{
+    if (!aux_used(ps, aux)) return nullptr;
     if (cudaEventRecord(g.ev_fork, st) != cudaSuccess || cudaStreamWaitEvent(aux, g.ev_fork, 0) != cudaSuccess)
         return nullptr;
     return aux;
@@ -653,6 +666,11 @@ struct BatchItem {
     size_t na, nb;
 };
 
+static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
+                         long long tiles);
+static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
+                      long long tiles);
+
 // One wave of W products, all of transform length 2^L, on stream st.
 static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, cudaStream_t st,
                       cudaStream_t aux_stream = nullptr)
@@ -683,6 +701,16 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
     CK(cudaMemcpyAsync(dtab, h, (7 * (size_t)W + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(x.btab_ev[slot], st));
     *x.slot = slot ^ 1;
+    if (g.graphs && !g_rec_on) return wave_graph(x, dtab, W, L, st, aux_stream, tiles);
+    return wave_launches(x, dtab, W, L, st, aux_stream, tiles);
+}
+
+// The launches of one wave after its table upload: both operands' forward
+// transforms, the fused pointwise product and inverse, the batched carry
+// kernel over `tiles` carry tiles.
+static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
+                         long long tiles)
+{
     uint64_t *specA = x.spec, *specB = x.spec + 3 * x.cap;
     const PrimeSet &ps = coef32_set();
     cudaStream_t aux = fork_aux(ps, st, aux_stream);
@@ -714,6 +742,89 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
     rec_begin(st, 4, 0, (rb * (double)((size_t)1 << L) + 4.0 * (double)(1 << L)) * (double)W);
     CK(launch_garner_carry_batch(c, tiles, st));
     rec_end(st);
+    return GBNTT_OK;
+}
+
+// CUDA-graph form of a wave: the launch sequence is captured the second time
+// a (context, table slot, transform length, wave size, prime set) key comes
+// up (the first run is launched directly, which also performs any one-time
+// kernel attribute setup outside a capture) and is replayed with one
+// cudaGraphLaunch from then on. Every argument of the captured launches is
+// fixed for the key: the tables live at the slot's device address and are
+// refreshed by the upload that precedes each replay, and the carry grid is
+// the key's upper bound on carry tiles, W ceil((2^L + 1) / 2048), whose
+// surplus CTAs take the highest tickets and exit at once. Anything that
+// changes the captured launches (plans, prime set, freed contexts) drops the
+// cache through invalidate_wave_graphs().
+struct WaveKey {
+    const uint64_t *spec;
+    const uint64_t *dtab;
+    const unsigned *ctl;
+    size_t cap;
+    int L;
+    long long W;
+    int primes;
+    bool operator<(const WaveKey &o) const
+    {
+        return std::tie(spec, dtab, ctl, cap, L, W, primes) < std::tie(o.spec, o.dtab, o.ctl, o.cap, o.L, o.W, o.primes);
+    }
+};
+struct WaveGraph {
+    cudaGraphExec_t exec = nullptr;
+    int runs = 0;
+};
+static std::map<WaveKey, WaveGraph> g_wave_graphs;
+static std::mutex g_wave_graphs_mu;
+constexpr size_t kMaxWaveGraphs = 512;
+
+static void invalidate_wave_graphs()
+{
+    std::lock_guard<std::mutex> lk(g_wave_graphs_mu);
+    for (auto &kv : g_wave_graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);   // in-flight replays finish first
+    g_wave_graphs.clear();
+}
+
+static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
+                      long long tiles)
+{
+    const PrimeSet &ps = coef32_set();
+    const long long ub = W * carry_tiles(((long long)1 << L) + 1);
+    if ((size_t)ub > x.n_status) return wave_launches(x, dtab, W, L, st, aux_stream, tiles);
+    const bool aux = aux_used(ps, aux_stream);
+    const WaveKey key{x.spec, dtab, x.ctl, x.cap, L, W, ps.n * 16 + ps.pi[0] * 4 + ps.pi[1] + (aux ? 256 : 0)};
+    cudaGraphExec_t exec = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_wave_graphs_mu);
+        WaveGraph &wg = g_wave_graphs[key];
+        exec = wg.exec;
+        if (!exec && wg.runs++ == 0) exec = (cudaGraphExec_t)-1;
+    }
+    if (exec == (cudaGraphExec_t)-1) return wave_launches(x, dtab, W, L, st, aux_stream, tiles);
+    if (!exec) {
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int rc = wave_launches(x, dtab, W, L, st, aux_stream, ub);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(st, &graph);
+        if (rc != GBNTT_OK || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            (void)cudaGetLastError();
+            if (rc != GBNTT_OK) return rc;
+            CK(e);
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CK(ei);
+        std::lock_guard<std::mutex> lk(g_wave_graphs_mu);
+        if (g_wave_graphs.size() >= kMaxWaveGraphs) {
+            for (auto &kv : g_wave_graphs)
+                if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+            g_wave_graphs.clear();
+        }
+        g_wave_graphs[key].exec = exec;
+        g_wave_graphs[key].runs = 2;
+    }
+    CK(cudaGraphLaunch(exec, st));
     return GBNTT_OK;
 }
 
@@ -876,6 +987,7 @@ void server_loop(Server *S)
 
 void server_free(Server *S)
 {
+    invalidate_wave_graphs();
     for (auto &sl : S->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         cudaFree(sl.spec);
@@ -1115,7 +1227,7 @@ int gbntt_set_plan(int log_n, int npasses, const int *passes)
 {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (log_n < kMinLog || log_n > kMaxLog) { set_err("gbntt_set_plan: log_n %d out of range", log_n); return GBNTT_ERR_ARG; }
-    if (npasses == 0) { g_plan_override[log_n][0] = 0; return GBNTT_OK; }
+    if (npasses == 0) { g_plan_override[log_n][0] = 0; invalidate_wave_graphs(); return GBNTT_OK; }
     if (npasses < 1 || npasses > 3 || !passes) { set_err("gbntt_set_plan: 1 to 3 passes"); return GBNTT_ERR_ARG; }
     int sum = 0;
     for (int i = 0; i < npasses; i++) {
@@ -1128,7 +1240,74 @@ int gbntt_set_plan(int log_n, int npasses, const int *passes)
     if (sum != log_n) { set_err("gbntt_set_plan: pass sizes sum to %d, not %d", sum, log_n); return GBNTT_ERR_ARG; }
     g_plan_override[log_n][0] = npasses;
     for (int i = 0; i < npasses; i++) g_plan_override[log_n][1 + i] = passes[i];
+    invalidate_wave_graphs();
     return GBNTT_OK;
+}
+
+// Autotuner: for each transform length 2^L in [log_lo, log_hi], time every
+// pass plan of 1 to 3 passes (each 2^5 .. 2^10 points) on a synthetic
+// 2^(L-1) x 2^(L-1)-limb product through the normal multiply path (CUDA
+// events on the engine stream, best of `reps` after a warm-up), and install
+// the fastest through the plan-override table. plans[4 i .. 4 i + 3]
+// receives (pass count, sizes...) and ms[i] its time for L = log_lo + i.
+int gbntt_autotune(int log_lo, int log_hi, int reps, int *plans, float *ms)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    if (log_lo < kMinLog || log_hi > g.max_log || log_lo > log_hi || reps < 1) {
+        set_err("gbntt_autotune: range [%d, %d] outside [%d, %d] or reps < 1", log_lo, log_hi, kMinLog, g.max_log);
+        return GBNTT_ERR_ARG;
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int rc = GBNTT_OK;
+    for (int L = log_lo; L <= log_hi && rc == GBNTT_OK; L++) {
+        const size_t half = (size_t)1 << (L - 1);
+        uint32_t *da = g.d_io, *db = da + half, *dc = db + half;
+        CK(launch_fill_splitmix(da, (long long)half, 0x5eed0000u + L, g.stream));
+        CK(launch_fill_splitmix(db, (long long)half, 0x5eed1000u + L, g.stream));
+        std::vector<std::array<int, 4>> cands;
+        for (int p0 = kMinLog; p0 <= kMaxPassLog; p0++) {
+            if (p0 == L) cands.push_back({1, p0, 0, 0});
+            for (int p1 = kMinLog; p1 <= kMaxPassLog; p1++) {
+                if (p0 + p1 == L) cands.push_back({2, p0, p1, 0});
+                const int p2 = L - p0 - p1;
+                if (p2 >= kMinLog && p2 <= kMaxPassLog) cands.push_back({3, p0, p1, p2});
+            }
+        }
+        float best = 1e30f;
+        std::array<int, 4> best_plan = {0, 0, 0, 0};
+        for (const auto &c : cands) {
+            g_plan_override[L][0] = c[0];
+            for (int i = 0; i < 3; i++) g_plan_override[L][1 + i] = c[1 + i];
+            if ((rc = mul_dev(dc, da, half, db, half, g.stream)) != GBNTT_OK) break;   // warm-up
+            float t_min = 1e30f;
+            for (int r = 0; r < reps && rc == GBNTT_OK; r++) {
+                CK(cudaEventRecord(e0, g.stream));
+                rc = mul_dev(dc, da, half, db, half, g.stream);
+                CK(cudaEventRecord(e1, g.stream));
+                CK(cudaEventSynchronize(e1));
+                float t = 0;
+                CK(cudaEventElapsedTime(&t, e0, e1));
+                t_min = std::min(t_min, t);
+            }
+            if (rc == GBNTT_OK && t_min < best) { best = t_min; best_plan = c; }
+        }
+        g_plan_override[L][0] = best_plan[0];
+        for (int i = 0; i < 3; i++) g_plan_override[L][1 + i] = best_plan[1 + i];
+        if (plans) for (int i = 0; i < 4; i++) plans[4 * (L - log_lo) + i] = best_plan[i];
+        if (ms) ms[L - log_lo] = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    invalidate_wave_graphs();
+    if (rc == GBNTT_OK) {
+        unsigned flags = 0;
+        rc = read_errors(&flags);
+        if (rc == GBNTT_OK && flags) { set_err("gbntt_autotune: device check failed (flags 0x%x)", flags); rc = GBNTT_ERR_DEVICE; }
+    }
+    return rc;
 }
 
 int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t n,
@@ -1213,10 +1392,19 @@ int gbntt_set_prime_set(int nprimes)
     if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
     cudaStreamSynchronize(g.stream);
     g.prime_set = nprimes;
+    invalidate_wave_graphs();
     return GBNTT_OK;
 }
 
 int gbntt_prime_set(void) { return g.ready ? g.prime_set : 0; }
+
+int gbntt_wave_graphs(void)
+{
+    std::lock_guard<std::mutex> lk(g_wave_graphs_mu);
+    int n = 0;
+    for (auto &kv : g_wave_graphs) n += kv.second.exec != nullptr;
+    return n;
+}
 
 int gbntt_set_coeff_bits(int bits)
 {

@@ -46,7 +46,8 @@ EXPORTS = (
     "gbntt_server_stop",
     "gbntt_split_terms_needed", "gbntt_e_required_log", "gbntt_binary_split", "gbntt_newton_reciprocal_u32",
     "gbntt_div_newton_u32", "gbntt_pow10_u32", "gbntt_to_decimal_u32", "gbntt_compute_e",
-    "gbntt_set_prime_set", "gbntt_prime_set", "gbntt_debug_lookback_timeout",
+    "gbntt_set_prime_set", "gbntt_prime_set", "gbntt_debug_lookback_timeout", "gbntt_autotune",
+    "gbntt_wave_graphs",
 )
 
 _lib = None
@@ -159,6 +160,10 @@ def lib():
     L.gbntt_prime_set.restype = ctypes.c_int
     L.gbntt_debug_lookback_timeout.argtypes = [ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_double)]
     L.gbntt_debug_lookback_timeout.restype = ctypes.c_int
+    L.gbntt_autotune.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                 ctypes.POINTER(ctypes.c_float)]
+    L.gbntt_autotune.restype = ctypes.c_int
+    L.gbntt_wave_graphs.restype = ctypes.c_int
     L.gbntt_last_error.restype = ctypes.c_char_p
     L.gbntt_stream.restype = _vp
     _lib = L
@@ -213,6 +218,21 @@ def launch_records(max_records=4096):
     if n < 0:
         _check(-n)
     return [(LAUNCH_KINDS[k[i]], l_[i], b[i], m[i]) for i in range(n)]
+
+
+def wave_graphs():
+    """Number of batched-wave CUDA graphs currently instantiated."""
+    return int(lib().gbntt_wave_graphs())
+
+
+def autotune(log_lo, log_hi, reps=3):
+    """Time every pass plan for transform lengths 2^log_lo .. 2^log_hi and
+    install the fastest; returns {L: (plan, ms)}."""
+    k = log_hi - log_lo + 1
+    plans = (ctypes.c_int * (4 * k))()
+    ms = (ctypes.c_float * k)()
+    _check(lib().gbntt_autotune(int(log_lo), int(log_hi), int(reps), plans, ms))
+    return {log_lo + i: ([plans[4 * i + 1 + j] for j in range(plans[4 * i])], float(ms[i])) for i in range(k)}
 
 
 def set_plan(log_n, passes):

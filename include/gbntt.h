@@ -118,6 +118,21 @@ int gbntt_plan(int log_n, int *passes);
  * npasses = 0 restores the default plan. Used by the autotuner. */
 int gbntt_set_plan(int log_n, int npasses, const int *passes);
 
+/* Autotuner (the reference picks its transform factorisation by hand): for
+ * each transform length 2^L, log_lo <= L <= log_hi <= the initialised
+ * maximum, times every pass plan of 1 to 3 passes of 2^5 .. 2^10 points on a
+ * synthetic product (best of `reps` runs after a warm-up, CUDA events) and
+ * installs the fastest as that length's plan (as gbntt_set_plan does).
+ * plans (may be NULL) receives 4 ints per length: pass count then sizes;
+ * ms (may be NULL) the winning time in milliseconds. Synchronous. */
+int gbntt_autotune(int log_lo, int log_hi, int reps, int *plans, float *ms);
+
+/* Batched waves run as CUDA graphs: a wave shape (context, table slot,
+ * transform length, wave size, prime set) seen a second time is captured
+ * and replayed from then on (environment GBNTT_GRAPHS=0 launches every
+ * wave directly). Returns the number of instantiated wave graphs held. */
+int gbntt_wave_graphs(void);
+
 /* d_c[0 .. na+nb) = d_a * d_b on the device, stream-ordered (returns after
  * enqueueing). d_b == d_a with nb == na squares. d_c must not overlap the
  * inputs. Device-side check failures are recorded and reported by
