@@ -71,6 +71,8 @@ struct Engine {
     uint64_t *d_spec = nullptr;     // 6 x n_max: spectra of operand A (3) then B (3)
     uint64_t *d_tw = nullptr;       // [prime 0..2, then normal-form q0][dir][hi|lo][2^15]
     uint32_t *d_tw3 = nullptr;      // p3: [dir][hi|lo][2^15]
+    uint64_t *d_st1 = nullptr;      // step-1 tables: [table slot 0..3][dir][kStep1Words]
+    uint32_t *d_st13 = nullptr;     // p3's: [dir][kStep1Words]
     int prime_set = 2;              // primes used for 32-bit coefficients: 2 or 3
     bool q0_lazy = false;           // two-prime set: q0 as prime 4 (lazy normal form) or 0 (Montgomery)
     bool overlap = true;            // two-prime set: second prime's passes on stream2
@@ -227,7 +229,8 @@ static size_t workspace_bytes(int max_log)
 {
     const size_t n = (size_t)1 << max_log;
     const size_t spec = 6 * n * sizeof(uint64_t);
-    const size_t tw = 4 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t) + 2 * 2 * (size_t)kTwSize * sizeof(uint32_t);
+    const size_t tw = 4 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t) + 2 * 2 * (size_t)kTwSize * sizeof(uint32_t) +
+                      4 * 2 * (size_t)kStep1Words * sizeof(uint64_t) + 2 * (size_t)kStep1Words * sizeof(uint32_t);
     const size_t ctl = (2 + status_words(n)) * sizeof(unsigned);
     const size_t io = (4 * n + 64) * sizeof(uint32_t);
     return spec + tw + ctl + io;
@@ -244,6 +247,8 @@ static void free_all()
     cudaFree(g.d_spec);
     cudaFree(g.d_tw);
     cudaFree(g.d_tw3);
+    cudaFree(g.d_st1);
+    cudaFree(g.d_st13);
     cudaFree(g.d_ctl);
     cudaFree(g.d_io);
     if (g.stream2) cudaStreamSynchronize(g.stream2);
@@ -272,7 +277,9 @@ static int init_impl(int max_log)
     CK(cudaEventCreateWithFlags(&g.ev_join, cudaEventDisableTiming));
     if (cudaMalloc(&g.d_spec, 6 * g.n_max * sizeof(uint64_t)) != cudaSuccess ||
         cudaMalloc(&g.d_tw, 4 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t)) != cudaSuccess ||
-        cudaMalloc(&g.d_tw3, 2 * 2 * (size_t)kTwSize * sizeof(uint32_t)) != cudaSuccess) {
+        cudaMalloc(&g.d_tw3, 2 * 2 * (size_t)kTwSize * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&g.d_st1, 4 * 2 * (size_t)kStep1Words * sizeof(uint64_t)) != cudaSuccess ||
+        cudaMalloc(&g.d_st13, 2 * (size_t)kStep1Words * sizeof(uint32_t)) != cudaSuccess) {
         set_err("gbntt_init: device allocation of %zu bytes failed", workspace_bytes(max_log));
         cudaGetLastError();
         free_all();
@@ -335,6 +342,12 @@ static int init_impl(int max_log)
         return GBNTT_ERR_ARG;
     }
     cudaError_t e = cudaMemcpy(g.d_tw, h, tw_words * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        std::vector<uint64_t> st(4 * 2 * (size_t)kStep1Words, 0);
+        for (int td = 0; td < 8; td++)
+            build_step1_tables(h + (size_t)td * 2 * kTwSize, st.data() + (size_t)td * kStep1Words);
+        e = cudaMemcpy(g.d_st1, st.data(), st.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    }
     free(h);
     if (e != cudaSuccess) { set_err("gbntt_init: twiddle upload failed: %s", cudaGetErrorString(e)); free_all(); return GBNTT_ERR_CUDA; }
     {
@@ -359,6 +372,12 @@ static int init_impl(int max_log)
             for (int i = 0; i < 64; i++) { w64[3][dir][i] = h_mont3(z); z = h_mul(z, r64, p); }
         }
         e = cudaMemcpy(g.d_tw3, h3.data(), h3.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) {
+            std::vector<uint32_t> st(2 * (size_t)kStep1Words, 0);
+            for (int dir = 0; dir < 2; dir++)
+                build_step1_tables(h3.data() + (size_t)dir * 2 * kTwSize, st.data() + (size_t)dir * kStep1Words);
+            e = cudaMemcpy(g.d_st13, st.data(), st.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+        }
         if (e != cudaSuccess) { set_err("gbntt_init: twiddle upload failed: %s", cudaGetErrorString(e)); free_all(); return GBNTT_ERR_CUDA; }
         // two-prime Garner: q0^-1 mod p3 and 2^64 mod p3 as p3 Montgomery multipliers
         const uint64_t q0 = prime_value(0);
@@ -410,9 +429,11 @@ static TwTables tables(const PrimeSet &ps, int dir)
             const int ts = pi == 4 ? 3 : pi;   // normal-form q0 tables sit in slot 3
             t.hi[k] = tw_ptr(ts, dir, 0);
             t.lo[k] = tw_ptr(ts, dir, 1);
+            t.st1[k] = g.d_st1 + ((size_t)ts * 2 + dir) * kStep1Words;
         } else {
             t.hi[k] = (const uint64_t *)(g.d_tw3 + ((size_t)dir * 2 + 0) * kTwSize);
             t.lo[k] = (const uint64_t *)(g.d_tw3 + ((size_t)dir * 2 + 1) * kTwSize);
+            t.st1[k] = (const uint64_t *)(g.d_st13 + (size_t)dir * kStep1Words);
         }
     }
     return t;

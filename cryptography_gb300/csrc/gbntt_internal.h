@@ -17,10 +17,33 @@ enum LoadKind { LD_U64 = 0, LD_U32 = 1, LD_PW = 2, LD_U64LIMB = 3 };
 // Twiddle tables of one direction for the three primes: Montgomery forms of
 // w^e, w the primitive 2^30-th root g^((p-1)/2^30) (or its inverse), with
 // hi[i] = w^(i*2^15) and lo[i] = w^i for i < 2^15.
+//
+// st1[k] points at the compact step-1 tables of the same prime and
+// direction: for each pass size 2^l (l = 5..10, A = 2^ceil(l/2),
+// B = 2^floor(l/2)) the A x B block at offset 2^l - 32 holds
+// w_L^(ka b) at [ka B + b]. The pass kernel's step-1 twiddles are
+// then one coalesced, L1-resident row per ka instead of a 32-line gather
+// from hi[] (whose w_L powers lie 2^(15 - l) entries apart).
 struct TwTables {
     const uint64_t *hi[3];
     const uint64_t *lo[3];
+    const uint64_t *st1[3];
 };
+
+constexpr int kStep1Words = 2048;   // sum of 2^l for l = 5..10 (2016), rounded up
+
+// Host: fill one (prime, direction) block of step-1 tables from that
+// prime's hi[] table (hi[i] = w^(i 2^15), so w_L^e = hi[e 2^(15 - l)]).
+template <typename W>
+inline void build_step1_tables(const W *hi, W *dst)
+{
+    for (int l = kMinLog; l <= kMaxPassLog; l++) {
+        const int L = 1 << l, A = 1 << ((l + 1) / 2), B = 1 << (l / 2);
+        W *blk = dst + (L - 32);
+        for (int ka = 0; ka < A; ka++)
+            for (int b = 0; b < B; b++) blk[ka * B + b] = hi[((ka * b) & (L - 1)) << (kTwBits - l)];
+    }
+}
 
 struct PassArgs {
     uint64_t *data[3];          // residues per prime, transformed in place

@@ -36,7 +36,8 @@ namespace {
 
 constexpr int kNoAllocMaxLog = 16;                       // products of up to 2^16 coefficients
 constexpr size_t kNoAllocMaxN = (size_t)1 << kNoAllocMaxLog;
-constexpr size_t kTwWords = 3 * 2 * 2 * (size_t)kTwSize; // [prime][dir][hi|lo][2^15]
+constexpr size_t kHiLoWords = 3 * 2 * 2 * (size_t)kTwSize;            // [prime][dir][hi|lo][2^15]
+constexpr size_t kTwWords = kHiLoWords + 3 * 2 * (size_t)kStep1Words;  // then [prime][dir] step-1 tables
 constexpr size_t kSpecWords = 6 * kNoAllocMaxN;          // 3 primes x (A, B)
 constexpr size_t kCtlWords = 64 + kNoAllocMaxN / 1024;   // ticket, error, tile status (32-bit each, rounded up)
 constexpr size_t kScratchWords = kTwWords + kSpecWords + kCtlWords;
@@ -94,6 +95,7 @@ void host_tables()
             const uint64_t r64 = na_pow(wd, (uint64_t)1 << (kMaxLog - 6), p);
             uint64_t z = 1;
             for (int i = 0; i < 64; i++) { g_na_w64[pi][dir][i] = na_mont(z, p); z = na_mul(z, r64, p); }
+            build_step1_tables(hi, g_na_tw_host + kHiLoWords + ((size_t)pi * 2 + dir) * kStep1Words);
         }
     }
     const uint64_t q0 = prime_value(0), q1 = prime_value(1), q2 = prime_value(2);
@@ -185,6 +187,7 @@ extern "C" int gbntt_mul_u32_noalloc(uint32_t *d_c, const uint32_t *d_a, size_t 
             a.data[pi] = spec + pi * stride;
             a.tw.hi[pi] = tw + (((size_t)pi * 2 + 0) * 2 + 0) * kTwSize;
             a.tw.lo[pi] = tw + (((size_t)pi * 2 + 0) * 2 + 1) * kTwSize;
+            a.tw.st1[pi] = tw + kHiLoWords + ((size_t)pi * 2 + 0) * kStep1Words;
         }
         a.limbs = op ? d_b : d_a;
         a.n_limbs = (long long)(op ? nb : na);
@@ -210,6 +213,7 @@ extern "C" int gbntt_mul_u32_noalloc(uint32_t *d_c, const uint32_t *d_a, size_t 
             a.other[pi] = (square ? specA : specB) + pi * stride;
             a.tw.hi[pi] = tw + (((size_t)pi * 2 + 1) * 2 + 0) * kTwSize;
             a.tw.lo[pi] = tw + (((size_t)pi * 2 + 1) * 2 + 1) * kTwSize;
+            a.tw.st1[pi] = tw + kHiLoWords + ((size_t)pi * 2 + 1) * kStep1Words;
             const uint64_t p = prime_value(pi);
             a.scale[pi] = na_mont(na_mont(na_inv(((uint64_t)1 << L) % p, p), p), p);
         }

@@ -228,6 +228,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
     const V *other = (const V *)a.other[F::SLOT];
     const V *twhi = (const V *)a.tw.hi[F::SLOT];
     const V *twlo = (const V *)a.tw.lo[F::SLOT];
+    const V *st1 = (const V *)a.tw.st1[F::SLOT] + (L - 32);   // w_L^(ka b) at [ka B + b]
     const int sh = kMaxLog - log_m;
     // column index within the sub-problem of the first column of this CTA
     const uint64_t j0 = LAYOUT == LAYOUT_STRIDED ? (uint64_t)(col0 & ((1LL << log_s) - 1)) : 0ull;
@@ -318,7 +319,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
 #pragma unroll
                     for (int ka = 1; ka < A; ka++) {
                         const int idx = bitrev(ka, S_::LOG_A);
-                        x[idx] = F::mul(x[idx], __ldg(twhi + ((lane * ka) << (kTwBits - LOG_L))));
+                        x[idx] = F::mul(x[idx], __ldg(st1 + ka * B + lane));
                     }
                 }
             }
@@ -339,7 +340,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         for (int ka = 0; ka < A; ka++) {
             V v = x[bitrev(ka, S_::LOG_A)];
             if (ka > 0 && b > 0)   // w_L^(b ka)
-                v = F::mul(v, __ldg(twhi + ((b * ka) << (kTwBits - LOG_L))));
+                v = F::mul(v, __ldg(st1 + ka * B + b));
             sm[g * RS + ka * (B + 1) + b] = v;
         }
     }
