@@ -180,8 +180,8 @@ static uint64_t *tw_ptr(int pi, int dir, int hi)
 }
 
 // Per-length plan overrides (set by gbntt_set_plan, e.g. from an autotuner):
-// [log_n][0] = pass count (0: default plan), [1..3] = pass sizes.
-static int g_plan_override[kMaxLog + 1][4];
+// [log_n][0] = pass count (0: default plan), [1..kMaxPasses] = pass sizes.
+static int g_plan_override[kMaxLog + 1][1 + kMaxPasses];
 
 int plan_passes(int log_n, int *p)
 {
@@ -191,15 +191,28 @@ int plan_passes(int log_n, int *p)
         return np;
     }
     if (log_n <= kMaxPassLog) { p[0] = log_n; return 1; }
-    if (log_n <= 2 * kMaxPassLog) { p[0] = (log_n + 1) / 2; p[1] = log_n / 2; return 2; }
-    // smallest pass first: the first forward pass reads 32-bit limbs down
-    // columns, and a 2^9-point pass moves 8 adjacent columns (32 bytes) per
-    // row instead of 4 (measured 2^29: [9, 10, 10] 95 ms, [10, 10, 9] 99 ms)
-    p[0] = log_n / 3;
-    const int rest = log_n - p[0];
-    p[1] = (rest + 1) / 2;
-    p[2] = rest / 2;
-    return 3;
+    // 2^18 .. 2^30: the plans gbntt_autotune measured fastest on GB300 for
+    // 2^(L-1) x 2^(L-1)-limb products (two-prime set). Passes of 2^7 and
+    // 2^8 points beat 2^9 and 2^10 even at the cost of a fourth pass: the
+    // 64-bit prime's 16-point register DFTs need 80 registers instead of 96
+    // (six resident CTAs instead of five) and a smaller loop body, and the
+    // extra sweep over HBM is cheap next to the integer work (2^29:
+    // [7, 7, 8, 7] 65.4 ms, [9, 10, 10] 71.7 ms).
+    constexpr int kTunedLo = 18;
+    static const signed char kTuned[kMaxLog + 1 - kTunedLo][1 + kMaxPasses] = {
+        {3, 6, 6, 6},    {3, 6, 8, 5},    {3, 8, 6, 6},    {3, 7, 8, 6},     // 2^18 .. 2^21
+        {3, 6, 8, 8},    {3, 7, 8, 8},    {3, 8, 8, 8},    {3, 7, 8, 10},    // 2^22 .. 2^25
+        {3, 8, 8, 10},   {4, 7, 7, 7, 6}, {4, 7, 7, 7, 7}, {4, 7, 7, 8, 7},  // 2^26 .. 2^29
+        {4, 7, 8, 8, 7},                                                    // 2^30
+    };
+    if (log_n >= kTunedLo && log_n <= kMaxLog) {
+        const signed char *t = kTuned[log_n - kTunedLo];
+        for (int i = 0; i < t[0]; i++) p[i] = t[1 + i];
+        return t[0];
+    }
+    p[0] = (log_n + 1) / 2;
+    p[1] = log_n / 2;
+    return 2;
 }
 
 static int choose_log(size_t na, size_t nb)
@@ -473,7 +486,7 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
                    cudaStream_t st, bool packed = false, long long W = 1, const uint32_t *const *limb_tab = nullptr,
                    const long long *len_tab = nullptr, cudaStream_t aux = nullptr)
 {
-    int pl[3];
+    int pl[kMaxPasses];
     const int np = plan_passes(L, pl);
     PassArgs a;
     memset(&a, 0, sizeof a);
@@ -507,7 +520,7 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
 static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, size_t stride, int L,
                    cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr)
 {
-    int pl[3];
+    int pl[kMaxPasses];
     const int np = plan_passes(L, pl);
     PassArgs a;
     memset(&a, 0, sizeof a);
@@ -523,7 +536,7 @@ static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, s
         a.scale[k] = pi < 3 ? h_mont(h_mont(ninv, p), p) : pi == 3 ? (uint64_t)h_mont3(h_mont3(ninv)) : ninv;
     }
     a.tw = tables(ps, 1);
-    int log_ms[3];
+    int log_ms[kMaxPasses];
     int log_m = L;
     for (int i = 0; i < np; i++) { log_ms[i] = log_m; log_m -= pl[i]; }
     for (int i = np - 1; i >= 0; i--) {
@@ -1249,7 +1262,10 @@ int gbntt_set_plan(int log_n, int npasses, const int *passes)
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (log_n < kMinLog || log_n > kMaxLog) { set_err("gbntt_set_plan: log_n %d out of range", log_n); return GBNTT_ERR_ARG; }
     if (npasses == 0) { g_plan_override[log_n][0] = 0; invalidate_wave_graphs(); return GBNTT_OK; }
-    if (npasses < 1 || npasses > 3 || !passes) { set_err("gbntt_set_plan: 1 to 3 passes"); return GBNTT_ERR_ARG; }
+    if (npasses < 1 || npasses > kMaxPasses || !passes) {
+        set_err("gbntt_set_plan: 1 to %d passes", kMaxPasses);
+        return GBNTT_ERR_ARG;
+    }
     int sum = 0;
     for (int i = 0; i < npasses; i++) {
         if (passes[i] < kMinLog || passes[i] > kMaxPassLog) {
@@ -1266,11 +1282,12 @@ int gbntt_set_plan(int log_n, int npasses, const int *passes)
 }
 
 // Autotuner: for each transform length 2^L in [log_lo, log_hi], time every
-// pass plan of 1 to 3 passes (each 2^5 .. 2^10 points) on a synthetic
-// 2^(L-1) x 2^(L-1)-limb product through the normal multiply path (CUDA
-// events on the engine stream, best of `reps` after a warm-up), and install
-// the fastest through the plan-override table. plans[4 i .. 4 i + 3]
-// receives (pass count, sizes...) and ms[i] its time for L = log_lo + i.
+// pass plan of 1 to kMaxPasses passes (each 2^5 .. 2^10 points) on a
+// synthetic 2^(L-1) x 2^(L-1)-limb product through the normal multiply path
+// (CUDA events on the engine stream, best of `reps` after a warm-up), and
+// install the fastest through the plan-override table.
+// plans[(1 + kMaxPasses) i ...] receives (pass count, sizes...) and ms[i]
+// its time for L = log_lo + i.
 int gbntt_autotune(int log_lo, int log_hi, int reps, int *plans, float *ms)
 {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
@@ -1288,20 +1305,30 @@ int gbntt_autotune(int log_lo, int log_hi, int reps, int *plans, float *ms)
         uint32_t *da = g.d_io, *db = da + half, *dc = db + half;
         CK(launch_fill_splitmix(da, (long long)half, 0x5eed0000u + L, g.stream));
         CK(launch_fill_splitmix(db, (long long)half, 0x5eed1000u + L, g.stream));
-        std::vector<std::array<int, 4>> cands;
-        for (int p0 = kMinLog; p0 <= kMaxPassLog; p0++) {
-            if (p0 == L) cands.push_back({1, p0, 0, 0});
-            for (int p1 = kMinLog; p1 <= kMaxPassLog; p1++) {
-                if (p0 + p1 == L) cands.push_back({2, p0, p1, 0});
-                const int p2 = L - p0 - p1;
-                if (p2 >= kMinLog && p2 <= kMaxPassLog) cands.push_back({3, p0, p1, p2});
+        // every composition of L into 1..kMaxPasses parts of 5..10
+        typedef std::array<int, 1 + kMaxPasses> Plan;
+        std::vector<Plan> cands;
+        Plan cur{};
+        auto extend = [&](auto &&self, int depth, int left) -> void {
+            if (left == 0 && depth > 0) {
+                Plan c{};
+                c[0] = depth;
+                for (int i = 0; i < depth; i++) c[1 + i] = cur[1 + i];
+                cands.push_back(c);
+                return;
             }
-        }
+            if (depth == kMaxPasses) return;
+            for (int p = kMinLog; p <= kMaxPassLog && p <= left; p++) {
+                cur[1 + depth] = p;
+                self(self, depth + 1, left - p);
+            }
+        };
+        extend(extend, 0, L);
         float best = 1e30f;
-        std::array<int, 4> best_plan = {0, 0, 0, 0};
+        Plan best_plan{};
         for (const auto &c : cands) {
             g_plan_override[L][0] = c[0];
-            for (int i = 0; i < 3; i++) g_plan_override[L][1 + i] = c[1 + i];
+            for (int i = 0; i < kMaxPasses; i++) g_plan_override[L][1 + i] = c[1 + i];
             if ((rc = mul_dev(dc, da, half, db, half, g.stream)) != GBNTT_OK) break;   // warm-up
             float t_min = 1e30f;
             for (int r = 0; r < reps && rc == GBNTT_OK; r++) {
@@ -1316,8 +1343,9 @@ int gbntt_autotune(int log_lo, int log_hi, int reps, int *plans, float *ms)
             if (rc == GBNTT_OK && t_min < best) { best = t_min; best_plan = c; }
         }
         g_plan_override[L][0] = best_plan[0];
-        for (int i = 0; i < 3; i++) g_plan_override[L][1 + i] = best_plan[1 + i];
-        if (plans) for (int i = 0; i < 4; i++) plans[4 * (L - log_lo) + i] = best_plan[i];
+        for (int i = 0; i < kMaxPasses; i++) g_plan_override[L][1 + i] = best_plan[1 + i];
+        if (plans)
+            for (int i = 0; i <= kMaxPasses; i++) plans[(1 + kMaxPasses) * (L - log_lo) + i] = best_plan[i];
         if (ms) ms[L - log_lo] = best;
     }
     cudaEventDestroy(e0);

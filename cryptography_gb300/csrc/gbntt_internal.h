@@ -11,6 +11,7 @@ constexpr int kTwBits = 15;        // two-level twiddle split: e = hi*2^15 + lo
 constexpr int kTwSize = 1 << kTwBits;
 constexpr int kMinLog = 5;         // smallest transform length used (32)
 constexpr int kMaxPassLog = 10;    // largest sub-DFT staged in one CTA
+constexpr int kMaxPasses = 4;      // passes per transform plan
 
 enum LoadKind { LD_U64 = 0, LD_U32 = 1, LD_PW = 2, LD_U64LIMB = 3 };
 

@@ -177,7 +177,7 @@ extern "C" int gbntt_mul_u32_noalloc(uint32_t *d_c, const uint32_t *d_a, size_t 
 
     PassArgs a;
     memset(&a, 0, sizeof a);
-    int pl[3];
+    int pl[kMaxPasses];
     const int np = plan_passes(L, pl);
     const bool square = (d_a == d_b && na == nb);
     // forward transforms of both operands

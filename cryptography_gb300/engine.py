@@ -195,8 +195,11 @@ def transform_log(na, nb):
     return int(lib().gbntt_transform_log(na, nb))
 
 
+MAX_PASSES = 4
+
+
 def plan(log_n):
-    p = (ctypes.c_int * 3)()
+    p = (ctypes.c_int * MAX_PASSES)()
     n = lib().gbntt_plan(int(log_n), p)
     return [p[i] for i in range(n)]
 
@@ -229,15 +232,16 @@ def autotune(log_lo, log_hi, reps=3):
     """Time every pass plan for transform lengths 2^log_lo .. 2^log_hi and
     install the fastest; returns {L: (plan, ms)}."""
     k = log_hi - log_lo + 1
-    plans = (ctypes.c_int * (4 * k))()
+    w = 1 + MAX_PASSES
+    plans = (ctypes.c_int * (w * k))()
     ms = (ctypes.c_float * k)()
     _check(lib().gbntt_autotune(int(log_lo), int(log_hi), int(reps), plans, ms))
-    return {log_lo + i: ([plans[4 * i + 1 + j] for j in range(plans[4 * i])], float(ms[i])) for i in range(k)}
+    return {log_lo + i: ([plans[w * i + 1 + j] for j in range(plans[w * i])], float(ms[i])) for i in range(k)}
 
 
 def set_plan(log_n, passes):
     """Override the pass plan for 2^log_n-point transforms ([] restores)."""
-    arr = (ctypes.c_int * 3)(*(list(passes) + [0, 0, 0])[:3])
+    arr = (ctypes.c_int * MAX_PASSES)(*(list(passes) + [0] * MAX_PASSES)[:MAX_PASSES])
     _check(lib().gbntt_set_plan(int(log_n), len(passes), arr))
 
 

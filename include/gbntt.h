@@ -110,20 +110,23 @@ size_t gbntt_workspace_bytes(int max_log32);
 int gbntt_transform_log(size_t na, size_t nb);
 
 /* Pass plan for a transform of 2^log_n points: writes the pass sizes
- * (log2, outermost first) to passes[0..2] and returns the pass count. */
+ * (log2, outermost first) to passes[0..3] (room for GBNTT_MAX_PASSES ints)
+ * and returns the pass count. */
+#define GBNTT_MAX_PASSES 4
 int gbntt_plan(int log_n, int *passes);
 
-/* Override the pass plan of transforms of 2^log_n points (1 to 3 passes,
+/* Override the pass plan of transforms of 2^log_n points (1 to 4 passes,
  * each of 2^5 .. 2^10 points, sizes summing to log_n, outermost first);
  * npasses = 0 restores the default plan. Used by the autotuner. */
 int gbntt_set_plan(int log_n, int npasses, const int *passes);
 
 /* Autotuner (the reference picks its transform factorisation by hand): for
  * each transform length 2^L, log_lo <= L <= log_hi <= the initialised
- * maximum, times every pass plan of 1 to 3 passes of 2^5 .. 2^10 points on a
+ * maximum, times every pass plan of 1 to 4 passes of 2^5 .. 2^10 points on a
  * synthetic product (best of `reps` runs after a warm-up, CUDA events) and
  * installs the fastest as that length's plan (as gbntt_set_plan does).
- * plans (may be NULL) receives 4 ints per length: pass count then sizes;
+ * plans (may be NULL) receives 1 + GBNTT_MAX_PASSES ints per length: pass
+ * count, then the sizes (unused entries 0);
  * ms (may be NULL) the winning time in milliseconds. Synchronous. */
 int gbntt_autotune(int log_lo, int log_hi, int reps, int *plans, float *ms);
 

@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 from cryptography_gb300 import engine
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "gbntt.h")
@@ -40,9 +42,9 @@ def test_library_is_native_sm103a(built_lib):
 
 def test_pure_host_queries(built_lib):
     # no device needed: planning and sizing are host logic
-    assert engine.plan(29) == [9, 10, 10]
-    assert engine.plan(30) == [10, 10, 10]
-    assert engine.plan(21) == [7, 7, 7]
+    assert engine.plan(29) == [7, 7, 8, 7]
+    assert engine.plan(30) == [7, 8, 8, 7]
+    assert engine.plan(21) == [7, 8, 6]
     assert engine.plan(12) == [6, 6]
     assert engine.plan(5) == [5]
     assert engine.transform_log(1 << 28, 1 << 28) == 29
@@ -52,3 +54,19 @@ def test_pure_host_queries(built_lib):
     assert not engine.is_ready()
     rc = built_lib.gbntt_mul_u32(ctypes.c_void_p(8), ctypes.c_void_p(8), 1, ctypes.c_void_p(8), 1, None)
     assert rc == engine.GBNTT_ERR_NOT_INIT
+
+
+def test_plan_overrides_host_logic(built_lib):
+    # plan overrides are host state: up to four passes of 2^5 .. 2^10 points
+    # summing to the transform log; anything else is rejected
+    default = engine.plan(29)
+    try:
+        engine.set_plan(29, [8, 7, 7, 7])
+        assert engine.plan(29) == [8, 7, 7, 7]
+        for bad in ([5, 6, 6, 6, 6], [10, 10, 8], [4, 10, 10, 5], [11, 9, 9]):
+            with pytest.raises(engine.EngineError):
+                engine.set_plan(29, bad)
+        assert engine.plan(29) == [8, 7, 7, 7]
+    finally:
+        engine.set_plan(29, [])
+    assert engine.plan(29) == default

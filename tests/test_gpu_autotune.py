@@ -15,7 +15,7 @@ def test_autotune_installs_valid_plans_and_keeps_products_exact(engine):
         res = engine.autotune(lo, hi, reps=2)
         assert sorted(res) == list(range(lo, hi + 1))
         for L, (plan, ms) in res.items():
-            assert 1 <= len(plan) <= 3 and sum(plan) == L, (L, plan)
+            assert 1 <= len(plan) <= 4 and sum(plan) == L, (L, plan)
             assert all(5 <= p <= 10 for p in plan), (L, plan)
             assert ms > 0
             assert engine.plan(L) == plan
