@@ -637,9 +637,7 @@ def run_gpu(args, dist):
         e2e = {"value": t_e2e / (args.e2e_steps * dist.world), "unit": UNIT, "h2d_bytes_per_step": 8 * n,
                "d2h_bytes_per_step": 8 * n, "api": "ntt_bigint_mul (pinned host BigInts)",
                "steps": args.e2e_steps, "per_step_ms": [round(x, 2) for x in per],
-               "transfer": "zero copy: the first forward passes read the pinned operands and the carry kernel "
-                           "writes the pinned result over NVLink-C2C" if os.environ.get("GBNTT_ZERO_COPY", "1") != "0"
-                           else "cudaMemcpyAsync through the engine's staging buffer"}
+               "transfer": _transfer_mode()}
         if C.cap != 2 * n64 + 8 or C.n_limbs != 2 * n64:
             e2e["warning"] = "unexpected output size"
         for p_ in (pa, pb, pc):
@@ -697,6 +695,17 @@ def run_gpu(args, dist):
         buf.free()
     g.teardown()
     return 0 if flags == 0 else 3
+
+
+def _transfer_mode():
+    if os.environ.get("GBNTT_ZERO_COPY", "1") == "0":
+        return "cudaMemcpyAsync through the engine's staging buffer"
+    if os.environ.get("GBNTT_STAGE_INPUTS", "1") == "0":
+        return ("zero copy: the first forward passes of both primes read the pinned operands and the carry "
+                "kernel writes the pinned result over NVLink-C2C")
+    return ("operand A read over NVLink-C2C once by its first q0 pass (which leaves a copy in HBM for p3), "
+            "operand B pulled into HBM by a copy kernel on a second stream while A is transformed, product "
+            "written to pinned memory by the carry kernel (zero copy)")
 
 
 def main():

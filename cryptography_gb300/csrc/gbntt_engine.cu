@@ -77,6 +77,7 @@ struct Engine {
     bool q0_lazy = false;           // two-prime set: q0 as prime 4 (lazy normal form) or 0 (Montgomery)
     bool overlap = true;            // two-prime set: second prime's passes on stream2
     bool zero_copy = true;          // host-pointer calls: kernels read/write pinned host memory directly
+    bool stage_inputs = true;       // ... except the operands, copied once to HBM (B's copy overlaps A's transform)
     bool graphs = true;             // batched waves replayed as CUDA graphs
     uint64_t garner2[2] = {0, 0};   // two-prime Garner constants (p3 Montgomery multipliers)
     unsigned *d_ctl = nullptr;      // [0] ticket, [1] error, [2..] tile status
@@ -86,6 +87,9 @@ struct Engine {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;      // second prime's passes run here, overlapping the first's
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t cstream = nullptr;      // host -> device operand copies overlapping the transforms
+    int sms = 152;                       // multiprocessors of the device (copy-kernel grids)
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_stage = nullptr;
     uint64_t garner[4] = {0, 0, 0, 0};
     uint64_t q01_lo = 0, q01_hi = 0;   // q0 * q1
     int bigint_coeff_bits = 32;        // coefficient width used by the BigInt entry points
@@ -267,6 +271,11 @@ static void free_all()
     if (g.stream2) cudaStreamSynchronize(g.stream2);
     if (g.ev_fork) cudaEventDestroy(g.ev_fork);
     if (g.ev_join) cudaEventDestroy(g.ev_join);
+    if (g.cstream) cudaStreamSynchronize(g.cstream);
+    if (g.ev_a) cudaEventDestroy(g.ev_a);
+    if (g.ev_b) cudaEventDestroy(g.ev_b);
+    if (g.ev_stage) cudaEventDestroy(g.ev_stage);
+    if (g.cstream) cudaStreamDestroy(g.cstream);
     if (g.stream2) cudaStreamDestroy(g.stream2);
     if (g.stream) cudaStreamDestroy(g.stream);
     invalidate_wave_graphs();
@@ -288,6 +297,16 @@ static int init_impl(int max_log)
     CK(cudaStreamCreateWithFlags(&g.stream2, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&g.ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&g.ev_join, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithFlags(&g.cstream, cudaStreamNonBlocking));
+    {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+            g.sms = sms;
+    }
+    CK(cudaEventCreateWithFlags(&g.ev_a, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&g.ev_b, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&g.ev_stage, cudaEventDisableTiming));
     if (cudaMalloc(&g.d_spec, 6 * g.n_max * sizeof(uint64_t)) != cudaSuccess ||
         cudaMalloc(&g.d_tw, 4 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t)) != cudaSuccess ||
         cudaMalloc(&g.d_tw3, 2 * 2 * (size_t)kTwSize * sizeof(uint32_t)) != cudaSuccess ||
@@ -425,6 +444,8 @@ static int init_impl(int max_log)
         // through the staging buffer)
         const char *gr = getenv("GBNTT_GRAPHS");
         g.graphs = !(gr && gr[0] == '0');
+        const char *si = getenv("GBNTT_STAGE_INPUTS");
+        g.stage_inputs = !(si && si[0] == '0');
         const char *zc = getenv("GBNTT_ZERO_COPY");
         g.zero_copy = !(zc && zc[0] == '0');
     }
@@ -482,9 +503,13 @@ static int join_aux(cudaStream_t st, cudaStream_t aux)
 
 // Forward transform of one operand: limbs -> one spectrum per prime of the
 // set at spec[k * stride] (k = slot; p3's 32-bit words fill half a slot).
+// stage (optional, single 32-bit-limb operands): the first prime's first
+// pass also copies the limbs it reads into stage[0 .. n), and the other
+// primes' first passes read that copy, so limbs in host memory cross
+// NVLink-C2C once.
 static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void *limbs, size_t n, int L,
                    cudaStream_t st, bool packed = false, long long W = 1, const uint32_t *const *limb_tab = nullptr,
-                   const long long *len_tab = nullptr, cudaStream_t aux = nullptr)
+                   const long long *len_tab = nullptr, cudaStream_t aux = nullptr, uint32_t *stage = nullptr)
 {
     int pl[kMaxPasses];
     const int np = plan_passes(L, pl);
@@ -507,10 +532,22 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
         for (int k = 0; k < ps.n; k++) {
             const double nbw = word_bytes(ps.pi[k]) * (double)((size_t)1 << L) * (double)W;
             cudaStream_t sk = (aux && k == 1) ? aux : st;
+            const bool staged = stage && i == 0 && !packed && W == 1;
+            if (staged && k > 0) {
+                a.limbs = stage;
+                a.stage_out = nullptr;
+                if (sk != st) {   // wait for the first prime's pass to fill the copy
+                    CK(cudaEventRecord(g.ev_stage, st));
+                    CK(cudaStreamWaitEvent(sk, g.ev_stage, 0));
+                }
+            } else {
+                a.stage_out = staged ? stage : nullptr;
+            }
             rec_begin(sk, i == 0 ? 0 : 1, pl[i], i == 0 ? (packed ? 8.0 : 4.0) * (double)n + nbw : 2.0 * nbw);
             CK(launch_pass_any(ps.pi[k], pl[i], 0, i == 0 ? (packed ? LD_U64LIMB : LD_U32) : LD_U64, a, sk));
             rec_end(sk);
         }
+        a.stage_out = nullptr;
         log_m -= pl[i];
     }
     return GBNTT_OK;
@@ -593,7 +630,11 @@ static int carry(const PrimeSet &ps, uint32_t *d_c, size_t n_out, const uint64_t
     return GBNTT_OK;
 }
 
-static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb, cudaStream_t st)
+// b_ready (optional): an event the second operand's transform waits for
+// (its host -> device copy on another stream).
+// stage_a (optional): HBM copy of A made by its first pass (see forward).
+static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb, cudaStream_t st,
+                   cudaEvent_t b_ready = nullptr, uint32_t *stage_a = nullptr)
 {
     if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
     if (!st) st = g.stream;
@@ -612,9 +653,13 @@ static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t
     uint64_t *specB = g.d_spec + 3 * g.n_max;
     const PrimeSet &ps = coef32_set();
     cudaStream_t aux = fork_aux(ps, st, g.stream2);
-    int rc = forward(ps, specA, g.n_max, d_a, na, L, st, false, 1, nullptr, nullptr, aux);
+    int rc = forward(ps, specA, g.n_max, d_a, na, L, st, false, 1, nullptr, nullptr, aux, stage_a);
     if (rc) return rc;
     if (!square) {
+        if (b_ready) {
+            CK(cudaStreamWaitEvent(st, b_ready, 0));
+            if (aux) CK(cudaStreamWaitEvent(aux, b_ready, 0));
+        }
         rc = forward(ps, specB, g.n_max, d_b, nb, L, st, false, 1, nullptr, nullptr, aux);
         if (rc) return rc;
     }
@@ -1074,16 +1119,47 @@ static int mul_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b
     uint32_t *da = g.d_io, *db = g.d_io + na, *dc = g.d_io + na + (square ? 0 : nb);
     double t0 = g.prof ? now_ms() : 0;
     const uint32_t *ua = dev_a, *ub = dev_b;
-    // zero copy: pinned operands are read by the first forward passes and a
-    // pinned result is written by the carry kernel, over NVLink-C2C
-    if (!ua && g.zero_copy) ua = (const uint32_t *)pinned_device_ptr(a);
-    if (!ub && !square && g.zero_copy) ub = (const uint32_t *)pinned_device_ptr(b);
+    // Zero copy: a pinned result is written by the carry kernel over
+    // NVLink-C2C. Pinned operands: without stage_inputs the first forward
+    // passes of both primes read them in place (twice over C2C). With it
+    // (default) A's first q0 pass reads A over C2C once and leaves a copy in
+    // HBM for p3's first pass, and B is pulled into HBM by a copy kernel on
+    // the copy stream while A is being transformed. Pageable operands go
+    // through cudaMemcpyAsync.
+    if (!ua && g.zero_copy && !g.stage_inputs) ua = (const uint32_t *)pinned_device_ptr(a);
+    if (!ub && !square && g.zero_copy && !g.stage_inputs) ub = (const uint32_t *)pinned_device_ptr(b);
     uint32_t *uc = g.zero_copy ? (uint32_t *)pinned_device_ptr(c) : nullptr;
-    if (!ua) { CK(cudaMemcpyAsync(da, a, na * 4, cudaMemcpyHostToDevice, g.stream)); ua = da; }
+    auto stage = [&](uint32_t *dst, const uint32_t *src, size_t n, int grid, cudaStream_t s) -> int {
+        const uint32_t *mapped = g.zero_copy ? (const uint32_t *)pinned_device_ptr(src) : nullptr;
+        if (mapped) CK(launch_copy_words(dst, mapped, (long long)n, grid, s));
+        else CK(cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyHostToDevice, s));
+        return GBNTT_OK;
+    };
+    int rs;
+    uint32_t *stage_a = nullptr;
+    if (!ua && g.zero_copy && g.stage_inputs && (ua = (const uint32_t *)pinned_device_ptr(a)) != nullptr) {
+        stage_a = da;   // A's first pass reads it over C2C once and leaves a copy in HBM for the other prime
+    } else if (!ua) {
+        if ((rs = stage(da, a, na, g.sms * 4, g.stream)) != GBNTT_OK) return rs;
+        ua = da;
+    }
+    cudaEvent_t b_ready = nullptr;
     if (square) ub = ua;
-    else if (!ub) { CK(cudaMemcpyAsync(db, b, nb * 4, cudaMemcpyHostToDevice, g.stream)); ub = db; }
-    if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[0] += t - t0; t0 = t; }
-    int rc = mul_dev(uc ? uc : dc, ua, na, ub, nb, g.stream);
+    else if (!ub) {
+        // B's copy overlaps A's forward transform with a small grid
+        CK(cudaEventRecord(g.ev_a, g.stream));
+        CK(cudaStreamWaitEvent(g.cstream, g.ev_a, 0));
+        if ((rs = stage(db, b, nb, g.sms / 2, g.cstream)) != GBNTT_OK) return rs;
+        CK(cudaEventRecord(g.ev_b, g.cstream));
+        b_ready = g.ev_b;
+        ub = db;
+    }
+    if (g.prof) {
+        CK(cudaStreamSynchronize(g.stream));
+        CK(cudaStreamSynchronize(g.cstream));
+        double t = now_ms(); g.prof_ms[0] += t - t0; t0 = t;
+    }
+    int rc = mul_dev(uc ? uc : dc, ua, na, ub, nb, g.stream, b_ready, stage_a);
     if (rc) return rc;
     if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[1] += t - t0; t0 = t; }
     if (!uc) CK(cudaMemcpyAsync(c, dc, n_out * 4, cudaMemcpyDeviceToHost, g.stream));

@@ -57,6 +57,7 @@ struct PassArgs {
     const long long *len_tab;
     int log_n_prod;
     long long n_limbs;          // limbs beyond this index read as zero
+    uint32_t *stage_out;        // first pass: also store each limb read here (a copy in HBM), or null
     TwTables tw;
     uint64_t scale[3];          // Montgomery constant folded into inverse twiddles
     long long ncols;            // N / L columns per prime
@@ -104,6 +105,7 @@ cudaError_t launch_garner_carry_batch(const CarryArgs &args, long long grid_tile
 long long carry_tiles(long long n_out);
 long long carry_tiles64(long long n_out);
 cudaError_t launch_fill_splitmix(uint32_t *d, long long n, uint64_t seed, cudaStream_t st);
+cudaError_t launch_copy_words(uint32_t *dst, const uint32_t *src, long long n, int grid, cudaStream_t st);
 cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *b, uint64_t *out, long long n,
                           cudaStream_t stream);
 

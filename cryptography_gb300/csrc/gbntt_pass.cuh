@@ -254,6 +254,17 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
 #pragma unroll 8
             for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
         }
+        if constexpr (LD == LD_U32 && sizeof(V) == 8) {
+            // staged first pass (64-bit prime, whose residue of a limb is
+            // the limb): copy the limbs just read to stage_out in HBM
+            if (a.stage_out) {
+#pragma unroll 4
+                for (int it = 0; it < A; it++) {
+                    const long long addr = base + it * stepg;
+                    if (addr < a.n_limbs) a.stage_out[addr] = (uint32_t)dst[it * (B + 1)];
+                }
+            }
+        }
     } else if constexpr (LD == LD_PW && GBNTT_PASS_PW_ASYNC) {
         // pointwise product: this spectrum's words go to the tile through
         // cp.async while the other spectrum's words are loaded into
@@ -293,6 +304,16 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
             V v = 0;
             if (g < rows_left) v = load_elem<PI, LD>(a, data, other, base + e);
             sm[g * RS + m + (m >> LOG_B)] = v;
+        }
+        if constexpr (LD == LD_U32 && sizeof(V) == 8) {
+            if (a.stage_out) {   // staged first pass, as in the strided layout
+#pragma unroll 4
+                for (int it = 0; it < A; it++) {
+                    const int e = t + it * T;
+                    const int g = e >> LOG_L, m = e & (L - 1);
+                    if (g < rows_left && base + e < a.n_limbs) a.stage_out[base + e] = (uint32_t)sm[g * RS + m + (m >> LOG_B)];
+                }
+            }
         }
     }
     if (DIR == 1 && (a.twiddle || a.use_scale)) {

@@ -161,11 +161,13 @@ def test_checked_variant_returns_codes():
     assert rc == 2   # GBNTT_ERR_SIZE
 
 
-@pytest.mark.parametrize("zero_copy", ["1", "0"])
-def test_bigint_mul_pinned_host_buffers(zero_copy):
-    # page-locked BigInts: with zero copy the kernels read the operands and
-    # write the product over NVLink-C2C; without it they go through the
-    # staging buffer. Both must give the exact product.
+@pytest.mark.parametrize("zero_copy,stage", [("1", "1"), ("1", "0"), ("0", "1")])
+def test_bigint_mul_pinned_host_buffers(zero_copy, stage):
+    # page-locked BigInts: with zero copy the carry kernel writes the product
+    # over NVLink-C2C and the operands are either read in place by the first
+    # passes (stage 0) or staged in HBM (A by its first q0 pass, B by a copy
+    # kernel on a second stream); without zero copy everything goes through
+    # the staging buffer. All must give the exact product, squares included.
     r = run("""
         import numpy as np
         from cryptography_gb300 import cudart
@@ -176,21 +178,26 @@ def test_bigint_mul_pinned_host_buffers(zero_copy):
         for na, nb in [(1, 1), (7, 5), (4096, 4093), ((1 << 18) + 3, (1 << 18) - 9)]:
             x, y = rnd(rng, na), rnd(rng, nb)
             pa, pb = cudart.PinnedBuffer(na, np.uint64), cudart.PinnedBuffer(nb, np.uint64)
-            pc = cudart.PinnedBuffer(na + nb + 8, np.uint64)
+            cap = max(na + nb, 2 * na) + 8   # room for the square too: no realloc of pinned memory
+            pc = cudart.PinnedBuffer(cap, np.uint64)
             pa.array[:] = np.frombuffer(x.to_bytes(8 * na, "little"), dtype=np.uint64)
             pb.array[:] = np.frombuffer(y.to_bytes(8 * nb, "little"), dtype=np.uint64)
             pc.array[:] = 0xAAAAAAAAAAAAAAAA
             a = g.BigInt(ctypes.cast(pa.ptr, u64p), na, na, 0)
             b = g.BigInt(ctypes.cast(pb.ptr, u64p), nb, nb, 0)
-            c = g.BigInt(ctypes.cast(pc.ptr, u64p), 0, na + nb + 8, 0)
+            c = g.BigInt(ctypes.cast(pc.ptr, u64p), 0, cap, 0)
             L.ntt_bigint_mul(B(c), B(a), B(b))
             ok = int.from_bytes(pc.array[:c.n_limbs].tobytes(), "little") == x * y
             out.append([na, nb, ok, int(c.limbs[0] == pc.array[0]), bool((pc.array[c.n_limbs:] == 0).all())])
+            pc.array[:] = 0
+            L.ntt_bigint_mul(B(c), B(a), B(a))
+            ok = int.from_bytes(pc.array[:c.n_limbs].tobytes(), "little") == x * x
+            out.append([na, na, ok, int(c.limbs[0] == pc.array[0]), c.cap == cap])
             for p in (pa, pb, pc):
                 p.free()
         print(json.dumps(out))
         L.ntt_mul_teardown_impl()
-    """, env={"GBNTT_ZERO_COPY": zero_copy})
+    """, env={"GBNTT_ZERO_COPY": zero_copy, "GBNTT_STAGE_INPUTS": stage})
     assert r.returncode == 0, r.stderr
     res = json.loads(r.stdout.strip().splitlines()[-1])
     assert all(ok and same and zeros for _, _, ok, same, zeros in res), res
