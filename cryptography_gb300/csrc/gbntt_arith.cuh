@@ -126,6 +126,126 @@ __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b)
     return r;
 }
 
+// q0 = 2^64 - 2^32 + 1 specialisations with the corrections on the ALU pipe.
+// With small passes the q0 kernels saturate the FMA-heavy pipe (IMAD) and
+// leave the ALU pipe about a fifth idle, so for q0 the +-p corrections are
+// borrow-chain subtractions of EPS = 2^32 - 1 (adding q0 mod 2^64 is
+// subtracting EPS) or selects, and the Montgomery reduction needs no
+// multiply at all: with m = T_lo (1 + 2^32) = (m1 : m0), m0 = t0,
+// m1 = t1 + t0, the high half of m q0 is m - m1 - [m1 < m0], so
+//   u = T_hi - m + m1 + [m1 < m0]   in (-q0, q0), minus EPS when negative.
+#ifndef GBNTT_Q0_ALU
+// bit 0: add/sub corrections (measured slower: the ALU pipe fills up),
+// bit 1: multiply-free Montgomery reduction, bit 2: power-of-two reduction;
+// 2^29 transform pairs: 65.4 ms with none, 61.6 ms with bits 1 and 2.
+// bit 3: the 64 x 64 product as 32-bit multiply-add carry chains instead of
+// wide multiplies with zero-extended addends (61.6 -> 60.9 ms).
+#define GBNTT_Q0_ALU 14
+#endif
+#if GBNTT_Q0_ALU & 1
+template <>
+__device__ __forceinline__ uint64_t add_mod<0>(uint64_t a, uint64_t b)
+{
+    // s = a + b; x = s + EPS; x when a + b >= 2^64 or s >= q0, else s
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 a0, a1, b0, b1, s0, s1, c, x0, x1, c2, r0, r1;\n\t"
+        ".reg .pred p;\n\t"
+        "mov.b64 {a0, a1}, %1;\n\t"
+        "mov.b64 {b0, b1}, %2;\n\t"
+        "add.cc.u32 s0, a0, b0;\n\t"
+        "addc.cc.u32 s1, a1, b1;\n\t"
+        "addc.u32 c, 0, 0;\n\t"
+        "add.cc.u32 x0, s0, 0xFFFFFFFF;\n\t"
+        "addc.cc.u32 x1, s1, 0;\n\t"
+        "addc.u32 c2, c, 0;\n\t"
+        "setp.ne.u32 p, c2, 0;\n\t"
+        "selp.u32 r0, x0, s0, p;\n\t"
+        "selp.u32 r1, x1, s1, p;\n\t"
+        "mov.b64 %0, {r0, r1};\n\t"
+        "}"
+        : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+template <>
+__device__ __forceinline__ uint64_t sub_mod<0>(uint64_t a, uint64_t b)
+{
+    // d = a - b; on borrow (bw = 0xFFFFFFFF) subtract EPS = bw
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 a0, a1, b0, b1, d0, d1, bw, r0, r1;\n\t"
+        "mov.b64 {a0, a1}, %1;\n\t"
+        "mov.b64 {b0, b1}, %2;\n\t"
+        "sub.cc.u32 d0, a0, b0;\n\t"
+        "subc.cc.u32 d1, a1, b1;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "sub.cc.u32 r0, d0, bw;\n\t"
+        "subc.u32 r1, d1, 0;\n\t"
+        "mov.b64 %0, {r0, r1};\n\t"
+        "}"
+        : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+#endif
+
+#if GBNTT_Q0_ALU & 2
+template <>
+__device__ __forceinline__ uint64_t mont_mul<0>(uint64_t a, uint64_t b)
+{
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 a0, a1, b0, b1, z, l00, h00, l01, h01, l10, h10, t2, t3, m1, s, v0, v1, bw, w0, w1, cy, r0, r1;\n\t"
+        ".reg .u64 p00, p01, p10, p11, w;\n\t"
+        ".reg .pred lt;\n\t"
+        "mov.b64 {a0, a1}, %1;\n\t"
+        "mov.b64 {b0, b1}, %2;\n\t"
+#if GBNTT_Q0_ALU & 8
+        // T = (t3 : t2 : l10 : l00) through 32-bit carry chains
+        "mul.lo.u32 l00, a0, b0;\n\t"
+        "mul.hi.u32 l10, a0, b0;\n\t"
+        "mad.lo.cc.u32 l10, a0, b1, l10;\n\t"
+        "madc.hi.u32 t2, a0, b1, 0;\n\t"
+        "mad.lo.cc.u32 l10, a1, b0, l10;\n\t"
+        "madc.hi.cc.u32 t2, a1, b0, t2;\n\t"
+        "addc.u32 t3, 0, 0;\n\t"
+        "mad.lo.cc.u32 t2, a1, b1, t2;\n\t"
+        "madc.hi.u32 t3, a1, b1, t3;\n\t"
+#else
+        "mov.u32 z, 0;\n\t"
+        "mul.wide.u32 p00, a0, b0;\n\t"
+        "mov.b64 {l00, h00}, p00;\n\t"
+        "mov.b64 w, {h00, z};\n\t"
+        "mad.wide.u32 p01, a0, b1, w;\n\t"
+        "mov.b64 {l01, h01}, p01;\n\t"
+        "mov.b64 w, {l01, z};\n\t"
+        "mad.wide.u32 p10, a1, b0, w;\n\t"
+        "mov.b64 {l10, h10}, p10;\n\t"
+        "mov.b64 w, {h01, z};\n\t"
+        "mad.wide.u32 p11, a1, b1, w;\n\t"
+        "mov.b64 {t2, t3}, p11;\n\t"
+        "add.cc.u32 t2, t2, h10;\n\t"           // T_hi = (t3 : t2)
+        "addc.u32 t3, t3, 0;\n\t"
+#endif
+        "add.u32 m1, l10, l00;\n\t"              // m = (m1 : l00)
+        "setp.lt.u32 lt, m1, l00;\n\t"
+        "selp.u32 s, 1, 0, lt;\n\t"
+        "add.u32 s, s, m1;\n\t"                  // s = m1 + [m1 < m0] < 2^32
+        "sub.cc.u32 v0, t2, l00;\n\t"            // v = T_hi - m
+        "subc.cc.u32 v1, t3, m1;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "add.cc.u32 w0, v0, s;\n\t"              // w = v + s
+        "addc.cc.u32 w1, v1, 0;\n\t"
+        "addc.u32 cy, bw, 0;\n\t"               // 0xFFFFFFFF: u < 0
+        "sub.cc.u32 r0, w0, cy;\n\t"             // u + q0 = w - EPS
+        "subc.u32 r1, w1, 0;\n\t"
+        "mov.b64 %0, {r0, r1};\n\t"
+        "}"
+        : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+#endif
+
 // Reference forms of the same three operations in plain C++ (64-bit compares
 // and selects); kept for the device self-test that pins the PTX forms.
 template <int PI>
@@ -174,6 +294,58 @@ constexpr uint32_t kP3 = 0xC0000001u;          // 3 * 2^30 + 1
 constexpr uint32_t kP3Inv = 0x40000001u;       // p3^-1 mod 2^32
 constexpr uint32_t kP3Neg = 0x3FFFFFFFu;       // -p3 mod 2^32
 
+#ifndef GBNTT_P3_ALU
+#define GBNTT_P3_ALU 0   // p3 corrections as and + add (ALU pipe) instead of IMAD (measured +0.6 ms at 2^29)
+#endif
+#if GBNTT_P3_ALU
+__device__ __forceinline__ uint32_t p3_add(uint32_t a, uint32_t b)
+{
+    uint32_t r;
+    asm("{\n\t"
+        ".reg .u32 nb, d, bw, k;\n\t"
+        "sub.u32 nb, %3, %2;\n\t"
+        "sub.cc.u32 d, %1, nb;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "and.b32 k, bw, %3;\n\t"
+        "add.u32 %0, d, k;\n\t"
+        "}"
+        : "=r"(r) : "r"(a), "r"(b), "n"(kP3));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t p3_sub(uint32_t a, uint32_t b)
+{
+    uint32_t r;
+    asm("{\n\t"
+        ".reg .u32 d, bw, k;\n\t"
+        "sub.cc.u32 d, %1, %2;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "and.b32 k, bw, %3;\n\t"
+        "add.u32 %0, d, k;\n\t"
+        "}"
+        : "=r"(r) : "r"(a), "r"(b), "n"(kP3));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t p3_mul(uint32_t a, uint32_t b)
+{
+    uint32_t r;
+    asm("{\n\t"
+        ".reg .u32 t0, t1, m, h, d, bw, k;\n\t"
+        ".reg .u64 t;\n\t"
+        "mul.wide.u32 t, %1, %2;\n\t"
+        "mov.b64 {t0, t1}, t;\n\t"
+        "mul.lo.u32 m, t0, %3;\n\t"
+        "mul.hi.u32 h, m, %4;\n\t"
+        "sub.cc.u32 d, t1, h;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "and.b32 k, bw, %4;\n\t"
+        "add.u32 %0, d, k;\n\t"
+        "}"
+        : "=r"(r) : "r"(a), "r"(b), "n"(kP3Inv), "n"(kP3));
+    return r;
+}
+#else
 __device__ __forceinline__ uint32_t p3_add(uint32_t a, uint32_t b)
 {
     uint32_t r;
@@ -219,6 +391,7 @@ __device__ __forceinline__ uint32_t p3_mul(uint32_t a, uint32_t b)
         : "=r"(r) : "r"(a), "r"(b), "n"(kP3Inv), "n"(kP3), "n"(kP3Neg));
     return r;
 }
+#endif
 
 // plain C++ forms for the device self-test
 __device__ __forceinline__ uint32_t p3_add_ref(uint32_t a, uint32_t b)
@@ -331,6 +504,39 @@ __device__ __forceinline__ uint64_t gl_mul(uint64_t a, uint64_t b)
 
 // (v1:v0) + v2 EPS - v3 mod q0 (the value of v0 + v1 2^32 + v2 2^64 +
 // v3 2^96), canonical.
+#if GBNTT_Q0_ALU & 4
+// corrections as borrow chains and selects (ALU pipe)
+__device__ __forceinline__ uint64_t gl_reduce4(uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3)
+{
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 x0, x1, bw, y0, y1, r0, r1, c, m, t0, t1, c2;\n\t"
+        ".reg .pred p;\n\t"
+        "sub.cc.u32 x0, %1, %4;\n\t"            // x = (v1:v0) - v3, + q0 (= - EPS) on borrow
+        "subc.cc.u32 x1, %2, 0;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "sub.cc.u32 x0, x0, bw;\n\t"
+        "subc.u32 x1, x1, 0;\n\t"
+        "sub.cc.u32 y0, 0, %3;\n\t"             // y = v2 EPS = (v2 << 32) - v2
+        "subc.u32 y1, %3, 0;\n\t"
+        "add.cc.u32 r0, x0, y0;\n\t"            // r = x + y, + EPS on carry
+        "addc.cc.u32 r1, x1, y1;\n\t"
+        "addc.u32 c, 0, 0;\n\t"
+        "neg.s32 m, c;\n\t"
+        "add.cc.u32 r0, r0, m;\n\t"
+        "addc.u32 r1, r1, 0;\n\t"
+        "add.cc.u32 t0, r0, 0xFFFFFFFF;\n\t"     // canonical: r - q0 = r + EPS when r >= q0
+        "addc.cc.u32 t1, r1, 0;\n\t"
+        "addc.u32 c2, 0, 0;\n\t"
+        "setp.ne.u32 p, c2, 0;\n\t"
+        "selp.u32 r0, t0, r0, p;\n\t"
+        "selp.u32 r1, t1, r1, p;\n\t"
+        "mov.b64 %0, {r0, r1};\n\t"
+        "}"
+        : "=l"(r) : "r"(v0), "r"(v1), "r"(v2), "r"(v3));
+    return r;
+}
+#else
 __device__ __forceinline__ uint64_t gl_reduce4(uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3)
 {
     uint64_t r;
@@ -358,6 +564,7 @@ __device__ __forceinline__ uint64_t gl_reduce4(uint32_t v0, uint32_t v1, uint32_
         : "=l"(r) : "r"(v0), "r"(v1), "r"(v2), "r"(v3));
     return r;
 }
+#endif
 
 // x * 2^e mod q0 for canonical x and 0 <= e < 96 (e folds to a constant
 // after unrolling, so the shifts and the branch on e / 32 vanish). In q0
