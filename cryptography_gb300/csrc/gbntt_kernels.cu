@@ -195,6 +195,28 @@ __device__ __forceinline__ void garner_coef2(const CarryArgs &a, long long j, ui
     if (top >= (uint64_t)a.n_coef) err |= ERR_GARNER_DIGIT;
 }
 
+// The two-prime Garner step on residues already loaded (r0 of q0, r1 of p3;
+// (0, 0) gives 0). c = r0 + a1 q0 = r0 + a1 + a1 2^64 - a1 2^32 through add
+// and borrow chains instead of a 128-bit multiply.
+__device__ __forceinline__ void garner2_vals(const CarryArgs &a, uint64_t r0, uint32_t r1, uint32_t &w0,
+                                             uint32_t &w1, uint32_t &w2, unsigned &err)
+{
+    r0 = gl_canon(r0);   // lazy residues reach [0, 2^64)
+    const uint32_t lo = (uint32_t)r0;
+    const uint32_t r0m = p3_add(p3_mul((uint32_t)(r0 >> 32), (uint32_t)a.garner[1]), lo >= kP3 ? lo - kP3 : lo);
+    const uint32_t a1 = p3_mul(p3_sub(r1, r0m), (uint32_t)a.garner[0]);
+    const uint64_t x = r0 + (uint64_t)a1;
+    const uint32_t ca = x < r0 ? 1u : 0u;
+    const uint64_t sh = (uint64_t)a1 << 32;
+    const uint64_t y = x - sh;
+    const uint32_t bb = x < sh ? 1u : 0u;
+    const uint32_t top = a1 + ca - bb;
+    w0 = (uint32_t)y;
+    w1 = (uint32_t)(y >> 32);
+    w2 = top;
+    if ((long long)top >= a.n_coef) err |= ERR_GARNER_DIGIT;
+}
+
 template <bool MIXED>
 __device__ __forceinline__ void garner_any(const CarryArgs &a, long long j, uint32_t &w0, uint32_t &w1, uint32_t &w2,
                                            unsigned &err)
@@ -203,8 +225,11 @@ __device__ __forceinline__ void garner_any(const CarryArgs &a, long long j, uint
     else garner_coef(a, j, w0, w1, w2, err);
 }
 
+#ifndef GBNTT_CARRY_MIN_BLOCKS
+#define GBNTT_CARRY_MIN_BLOCKS 6   // resident carry CTAs per SM the register budget targets (2^29: 5 -> 2.39 ms, 6 -> 2.21, 8 -> 2.34)
+#endif
 template <bool BATCH, bool MIXED>
-__global__ void __launch_bounds__(kCarryThreads) garner_carry_kernel_t(CarryArgs a)
+__global__ void __launch_bounds__(kCarryThreads, GBNTT_CARRY_MIN_BLOCKS) garner_carry_kernel_t(CarryArgs a)
 {
     constexpr int T = kCarryThreads, K = kCarryPerThread, TILE = kCarryTile;
     constexpr int SW = TILE + 2 + (TILE + 2) / 32 + 1;
@@ -248,12 +273,35 @@ __global__ void __launch_bounds__(kCarryThreads) garner_carry_kernel_t(CarryArgs
     unsigned err = 0;
 
     // phase 1: coefficients of positions base-2 .. base+TILE-1 (slot q+2)
+    if constexpr (MIXED) {
+        // all of this thread's residue loads first (beyond the transform:
+        // zero), then the arithmetic
+        const uint64_t *res0 = a.res[0];
+        const uint32_t *res1 = (const uint32_t *)a.res[1];
+        uint64_t v0[K];
+        uint32_t v1[K];
 #pragma unroll
-    for (int r = 0; r < K; r++) {
-        const int q = r * T + tid;
-        uint32_t w0, w1, w2;
-        garner_any<MIXED>(a, base + q, w0, w1, w2, err);
-        W0[spad(q + 2)] = w0; W1[spad(q + 2)] = w1; W2[spad(q + 2)] = w2;
+        for (int r = 0; r < K; r++) {
+            const long long j = base + r * T + tid;
+            const bool in = j < a.n_coef;
+            v0[r] = in ? __ldcs(res0 + j) : 0ull;
+            v1[r] = in ? __ldcs(res1 + j) : 0u;
+        }
+#pragma unroll
+        for (int r = 0; r < K; r++) {
+            const int q = r * T + tid;
+            uint32_t w0, w1, w2;
+            garner2_vals(a, v0[r], v1[r], w0, w1, w2, err);
+            W0[spad(q + 2)] = w0; W1[spad(q + 2)] = w1; W2[spad(q + 2)] = w2;
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < K; r++) {
+            const int q = r * T + tid;
+            uint32_t w0, w1, w2;
+            garner_any<MIXED>(a, base + q, w0, w1, w2, err);
+            W0[spad(q + 2)] = w0; W1[spad(q + 2)] = w1; W2[spad(q + 2)] = w2;
+        }
     }
     if (tid < 2) {
         uint32_t w0, w1, w2;
@@ -473,8 +521,23 @@ cudaError_t launch_garner_carry64(const CarryArgs &args, cudaStream_t stream, lo
     return cudaGetLastError();
 }
 
+// the carry kernels' tiles live in shared memory: ask for the largest
+// shared-memory carveout so that shared memory does not cap their residency
+static void carry_carveout()
+{
+    static bool done = false;
+    if (done) return;
+    done = true;
+    cudaFuncSetAttribute(garner_carry_kernel_t<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(garner_carry_kernel_t<false, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(garner_carry_kernel_t<true, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(garner_carry_kernel_t<true, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    (void)cudaGetLastError();
+}
+
 cudaError_t launch_garner_carry(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out)
 {
+    carry_carveout();
     const long long nt = carry_tiles(args.n_out);
     if (ntiles_out) *ntiles_out = nt;
     if (nt == 0) return cudaSuccess;
@@ -485,6 +548,7 @@ cudaError_t launch_garner_carry(const CarryArgs &args, cudaStream_t stream, long
 
 cudaError_t launch_garner_carry_batch(const CarryArgs &args, long long grid_tiles, cudaStream_t stream)
 {
+    carry_carveout();
     if (grid_tiles <= 0) return cudaSuccess;
     if (args.mixed) garner_carry_kernel_t<true, true><<<(unsigned)grid_tiles, kCarryThreads, 0, stream>>>(args);
     else garner_carry_kernel_t<true, false><<<(unsigned)grid_tiles, kCarryThreads, 0, stream>>>(args);
