@@ -553,13 +553,16 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
 }
 
 // Pointwise product of the spectra and inverse transform, in place in specA.
+// shared_b: specB holds one spectrum (2^L points) that every product of
+// the wave multiplies by.
 static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, size_t stride, int L,
-                   cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr)
+                   cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr, bool shared_b = false)
 {
     int pl[kMaxPasses];
     const int np = plan_passes(L, pl);
     PassArgs a;
     memset(&a, 0, sizeof a);
+    a.other_log = shared_b ? L : 0;
     for (int k = 0; k < ps.n; k++) {
         const int pi = ps.pi[k];
         a.data[k] = specA + k * stride;
@@ -745,9 +748,9 @@ struct BatchItem {
 };
 
 static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                         long long tiles);
+                         long long tiles, bool shared_b);
 static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                      long long tiles);
+                      long long tiles, bool shared_b);
 
 // One wave of W products, all of transform length 2^L, on stream st.
 static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, cudaStream_t st,
@@ -760,8 +763,12 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
     uint64_t *hA = h, *hLA = h + W, *hB = h + 2 * W, *hLB = h + 3 * W, *hC = h + 4 * W, *hNC = h + 5 * W,
              *hTS = h + 6 * W;
     long long tiles = 0;
+    // every product multiplying by the same right operand (a division by a
+    // shared divisor or reciprocal): its transform is computed once
+    bool shared_b = W > 1;
     for (long long k = 0; k < W; k++) {
         const BatchItem &it = items[k];
+        if (it.b != items[0].b || it.nb != items[0].nb || it.a == it.b) shared_b = false;
         hA[k] = (uint64_t)(uintptr_t)it.a;
         hLA[k] = (uint64_t)it.na;
         hB[k] = (uint64_t)(uintptr_t)it.b;
@@ -779,15 +786,15 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
     CK(cudaMemcpyAsync(dtab, h, (7 * (size_t)W + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(x.btab_ev[slot], st));
     *x.slot = slot ^ 1;
-    if (g.graphs && !g_rec_on) return wave_graph(x, dtab, W, L, st, aux_stream, tiles);
-    return wave_launches(x, dtab, W, L, st, aux_stream, tiles);
+    if (g.graphs && !g_rec_on) return wave_graph(x, dtab, W, L, st, aux_stream, tiles, shared_b);
+    return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b);
 }
 
 // The launches of one wave after its table upload: both operands' forward
 // transforms, the fused pointwise product and inverse, the batched carry
 // kernel over `tiles` carry tiles.
 static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                         long long tiles)
+                         long long tiles, bool shared_b)
 {
     uint64_t *specA = x.spec, *specB = x.spec + 3 * x.cap;
     const PrimeSet &ps = coef32_set();
@@ -795,10 +802,12 @@ static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaSt
     int rc = forward(ps, specA, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab),
                      (const long long *)(dtab + W), aux);
     if (rc) return rc;
-    rc = forward(ps, specB, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab + 2 * W),
+    // shared right operand: one transform (table entry 0), read by every
+    // product's pointwise pass
+    rc = forward(ps, specB, x.cap, nullptr, 0, L, st, false, shared_b ? 1 : W, (const uint32_t *const *)(dtab + 2 * W),
                  (const long long *)(dtab + 3 * W), aux);
     if (rc) return rc;
-    rc = inverse(ps, specA, specB, x.cap, L, st, false, W, aux);
+    rc = inverse(ps, specA, specB, x.cap, L, st, false, W, aux, shared_b);
     if (rc) return rc;
     rc = join_aux(st, aux);
     if (rc) return rc;
@@ -864,13 +873,14 @@ static void invalidate_wave_graphs()
 }
 
 static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                      long long tiles)
+                      long long tiles, bool shared_b)
 {
     const PrimeSet &ps = coef32_set();
     const long long ub = W * carry_tiles(((long long)1 << L) + 1);
-    if ((size_t)ub > x.n_status) return wave_launches(x, dtab, W, L, st, aux_stream, tiles);
+    if ((size_t)ub > x.n_status) return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b);
     const bool aux = aux_used(ps, aux_stream);
-    const WaveKey key{x.spec, dtab, x.ctl, x.cap, L, W, ps.n * 16 + ps.pi[0] * 4 + ps.pi[1] + (aux ? 256 : 0)};
+    const WaveKey key{x.spec, dtab, x.ctl, x.cap, L, W,
+                      ps.n * 16 + ps.pi[0] * 4 + ps.pi[1] + (aux ? 256 : 0) + (shared_b ? 512 : 0)};
     cudaGraphExec_t exec = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_wave_graphs_mu);
@@ -878,10 +888,10 @@ static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStrea
         exec = wg.exec;
         if (!exec && wg.runs++ == 0) exec = (cudaGraphExec_t)-1;
     }
-    if (exec == (cudaGraphExec_t)-1) return wave_launches(x, dtab, W, L, st, aux_stream, tiles);
+    if (exec == (cudaGraphExec_t)-1) return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b);
     if (!exec) {
         CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        const int rc = wave_launches(x, dtab, W, L, st, aux_stream, ub);
+        const int rc = wave_launches(x, dtab, W, L, st, aux_stream, ub, shared_b);
         cudaGraph_t graph = nullptr;
         const cudaError_t e = cudaStreamEndCapture(st, &graph);
         if (rc != GBNTT_OK || e != cudaSuccess) {

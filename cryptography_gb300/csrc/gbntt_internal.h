@@ -49,6 +49,7 @@ inline void build_step1_tables(const W *hi, W *dst)
 struct PassArgs {
     uint64_t *data[3];          // residues per prime, transformed in place
     const uint64_t *other[3];   // second spectrum for the fused pointwise product
+    int other_log;              // nonzero: one shared second spectrum of 2^other_log points for every product
     const uint32_t *limbs;      // 32-bit limbs for the fused decomposition
     const uint64_t *limbs64;    // 64-bit limbs (one per coefficient) for the packed mode
     // batched first pass: product b's limbs are limb_tab[b][0 .. len_tab[b]),

@@ -171,7 +171,8 @@ __device__ __forceinline__ typename Field<PI>::T load_elem(const PassArgs &a, co
         if constexpr (sizeof(typename F::T) == 8) return limb64_residue<PI>(a, addr);
         else return 0;
     } else if constexpr (LD == LD_PW) {
-        return F::mul(data[addr], other[addr]);
+        const long long oaddr = a.other_log ? (addr & ((1LL << a.other_log) - 1)) : addr;
+        return F::mul(data[addr], other[oaddr]);
     } else {
         return data[addr];
     }
@@ -272,6 +273,9 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         // words it copied (visible to it after the wait)
         const long long rows_left = a.ncols - col0;
         const long long base = col0 << LOG_L;
+        // a shared second spectrum (one operand common to the whole batch)
+        // is read at the position within its product
+        const long long omask = a.other_log ? ((1LL << a.other_log) - 1) : -1LL;
         V o[A];
 #pragma unroll
         for (int it = 0; it < A; it++) {
@@ -280,7 +284,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
             V *d = sm + g * RS + m + (m >> LOG_B);
             if (g < rows_left) {
                 cp_async_word<sizeof(V)>(d, data + base + e);
-                o[it] = __ldg(other + base + e);
+                o[it] = __ldg(other + ((base + e) & omask));
             } else {
                 *d = 0;
                 o[it] = 0;

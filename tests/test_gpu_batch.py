@@ -118,3 +118,34 @@ def test_batch_many_tiny_products_on_a_small_engine():
     r = subprocess.run([sys.executable, "-c", body], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     assert json.loads(r.stdout.strip().splitlines()[-1]) == [True, 0]
+
+
+def test_batch_shared_right_operand(engine):
+    # every product of the batch multiplies by the same device operand (the
+    # e pipeline's divisions by a shared reciprocal or divisor): its
+    # transform is computed once per wave; results must equal single
+    # products. Two rounds so the second replays the wave graphs.
+    rng = np.random.default_rng(31)
+    for nb in (1, 700, 5000):
+        b = rng.integers(0, 1 << 32, nb, dtype=np.uint64).astype(np.uint32)
+        db = _upload([b])[0]
+        for _ in range(2):
+            A = [rng.integers(0, 1 << 32, int(n), dtype=np.uint64).astype(np.uint32)
+                 for n in rng.integers(1, 6000, 40)]
+            da = _upload(A)
+            dc = [cudart.DeviceBuffer(max(4, 4 * (len(a) + nb))) for a in A]
+            engine.batch_mul_device([c.ptr for c in dc], [x.ptr for x in da], [len(a) for a in A],
+                                    [db.ptr] * len(A), [nb] * len(A))
+            cudart.synchronize()
+            got = [c.download(np.uint32, len(a) + nb) for c, a in zip(dc, A)]
+            for i, (a, c) in enumerate(zip(A, got)):
+                assert np.array_equal(c, engine.mul(a, b)), (nb, i)
+            for i in range(0, len(A), 13):
+                want = np.zeros(len(A[i]) + nb, dtype=np.uint32)
+                r = oracle.mul(A[i], b)
+                want[:len(r)] = r
+                assert np.array_equal(got[i], want), (nb, i)
+            for x in da + dc:
+                x.free()
+        db.free()
+    assert engine.device_errors() == 0
