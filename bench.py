@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--batch-reps", type=int, default=2)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-products leg")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-negacyclic", action="store_true", help="skip the negacyclic polynomial-product leg")
+    ap.add_argument("--nega-log", type=int, default=24, help="negacyclic leg: N = 2^k coefficients")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--serve-saturation", type=int, default=3000)
     ap.add_argument("--serve-slots", type=int, default=4)
@@ -561,6 +563,11 @@ def run_gpu(args, dist):
                   "note": "same integers as 2^%d 64-bit limbs, one coefficient per limb (reference granularity); "
                           "not the headline configuration" % (lg - 1)}
 
+    negacyclic = None
+    if not args.no_negacyclic and dist.rank == 0:
+        negacyclic = run_negacyclic_leg(g, cudart, args, stream)
+        flags |= g.device_errors()
+
     batched = None
     if not args.no_batched and dist.rank == 0:
         batched = run_batched_leg(g, cudart, args, stream)
@@ -679,6 +686,7 @@ def run_gpu(args, dist):
         "square": square,
         "multiply_2pow20": small,
         "packed_64bit_coefficients": packed,
+        "negacyclic": negacyclic,
         "batched": batched,
         "serving": serving,
         "e_digits": e_leg,
@@ -695,6 +703,41 @@ def run_gpu(args, dist):
         buf.free()
     g.teardown()
     return 0 if flags == 0 else 3
+
+
+def run_negacyclic_leg(g, cudart, args, stream):
+    """Negacyclic polynomial product mod X^N + 1 (the reference's crt_ntt
+    negacyclic pipeline): N seeded 64-bit coefficients per operand, device
+    resident, three 64-bit primes, signed 256-bit outputs."""
+    L = args.nega_log
+    n = 1 << L
+    df, dgb, do = cudart.DeviceBuffer(8 * n), cudart.DeviceBuffer(8 * n), cudart.DeviceBuffer(32 * n)
+    # 64-bit coefficients from two 32-bit splitmix streams each
+    g.lib().gbntt_fill_operand(ctypes.c_void_p(df.ptr), 2 * n, 0x6E6100 + L, ctypes.c_void_p(stream))
+    g.lib().gbntt_fill_operand(ctypes.c_void_p(dgb.ptr), 2 * n, 0x6E6200 + L, ctypes.c_void_p(stream))
+
+    def step():
+        g.negacyclic_mul_device(do.ptr, df.ptr, dgb.ptr, L, stream)
+    for _ in range(max(1, args.warmup)):
+        step()
+    cudart.stream_sync(stream)
+    e0, e1 = cudart.Event(), cudart.Event()
+    steps = max(1, min(args.steps, 10))
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_ms(e1) / steps
+    for b in (df, dgb, do):
+        b.free()
+    # bytes: coefficients in (16 N), three primes x (twist write, 2-pass
+    # forward per operand, pointwise + inverse, finish read) and 32 N out
+    bm = 16 * n + 3 * 8 * n * (2 + 2 * 2 * 2 + 3 + 2 + 1) + 32 * n
+    return {"ms": ms, "log_n": L, "coefficients": n, "primes": 3,
+            "bytes_model": bm, "bytes_model_GBps": bm / (ms * 1e-3) / 1e9,
+            "output": "signed 256-bit coefficients (4 uint64 words each)",
+            "api": "gbntt_negacyclic_mul_u64 (device pointers)"}
 
 
 def _transfer_mode():

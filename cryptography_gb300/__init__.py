@@ -37,6 +37,8 @@ from .engine import (  # noqa: F401
     mul,
     mul_device,
     mul64,
+    negacyclic_mul,
+    negacyclic_mul_device,
     set_coeff_bits,
     set_prime_set,
     prime_set,

@@ -17,7 +17,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbntt.so")
 
 SOURCES = ["gbntt_pass_p0.cu", "gbntt_pass_p1.cu", "gbntt_pass_p2.cu", "gbntt_pass_p3.cu", "gbntt_pass_p4.cu", "gbntt_kernels.cu", "gbntt_engine.cu", "gbntt_noalloc.cu",
-           "gbntt_e.cu"]
+           "gbntt_e.cu", "gbntt_negacyclic.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 

@@ -508,8 +508,10 @@ static int join_aux(cudaStream_t st, cudaStream_t aux)
 // NVLink-C2C once.
 static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void *limbs, size_t n, int L,
                    cudaStream_t st, bool packed = false, long long W = 1, const uint32_t *const *limb_tab = nullptr,
-                   const long long *len_tab = nullptr, cudaStream_t aux = nullptr, uint32_t *stage = nullptr)
+                   const long long *len_tab = nullptr, cudaStream_t aux = nullptr, uint32_t *stage = nullptr,
+                   bool preloaded = false)
 {
+    // preloaded: spec already holds the residues (the first pass reads them)
     int pl[kMaxPasses];
     const int np = plan_passes(L, pl);
     PassArgs a;
@@ -543,7 +545,8 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
                 a.stage_out = staged ? stage : nullptr;
             }
             rec_begin(sk, i == 0 ? 0 : 1, pl[i], i == 0 ? (packed ? 8.0 : 4.0) * (double)n + nbw : 2.0 * nbw);
-            CK(launch_pass_any(ps.pi[k], pl[i], 0, i == 0 ? (packed ? LD_U64LIMB : LD_U32) : LD_U64, a, sk));
+            const int ld0 = preloaded ? LD_U64 : (packed ? LD_U64LIMB : LD_U32);
+            CK(launch_pass_any(ps.pi[k], pl[i], 0, i == 0 ? ld0 : LD_U64, a, sk));
             rec_end(sk);
         }
         a.stage_out = nullptr;
@@ -1104,6 +1107,68 @@ static int read_errors(unsigned *flags)
 // Host-pointer product through the staging buffer (a, b, c contiguous).
 // Device address of page-locked host memory (NVLink-C2C makes it directly
 // readable and writable by kernels), or nullptr for other memory.
+// Negacyclic product modulo X^N + 1 (N = 2^L) of two N-coefficient
+// polynomials with 64-bit coefficients, over the three 64-bit primes:
+// twist, the cyclic pass chain, the fused pointwise product and inverse,
+// then untwist + Garner to signed 256-bit coefficients (reference
+// pipeline_negacyclic, ntt/lib/main.hip:557-684).
+static int negacyclic_dev(uint64_t *d_out, const uint64_t *d_f, const uint64_t *d_g, int L, cudaStream_t st)
+{
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    if (!st) st = g.stream;
+    if (L < kMinLog || L > kMaxLog - 1 || L > g.max_log) {
+        set_err("gbntt_negacyclic_mul_u64: log_n %d outside [%d, %d]", L, kMinLog, std::min(kMaxLog - 1, g.max_log));
+        return GBNTT_ERR_ARG;
+    }
+    if (!d_out || !d_f || !d_g) { set_err("gbntt_negacyclic_mul_u64: null pointer"); return GBNTT_ERR_ARG; }
+    const PrimeSet &ps = kSet3;
+    const long long N = 1LL << L;
+    uint64_t *specA = g.d_spec, *specB = g.d_spec + 3 * g.n_max;
+    const bool square = d_f == d_g;
+    NegaArgs na;
+    memset(&na, 0, sizeof na);
+    na.n = N;
+    na.shift = (kMaxLog - 1) - L;   // psi = w^(2^(29 - L)): a primitive 2^(L+1)-th root
+    const TwTables tf = tables(ps, 0), ti = tables(ps, 1);
+    for (int k = 0; k < 3; k++) { na.hi[k] = tf.hi[k]; na.lo[k] = tf.lo[k]; }
+    for (int op = 0; op < (square ? 1 : 2); op++) {
+        uint64_t *spec = op ? specB : specA;
+        for (int k = 0; k < 3; k++) na.spec[k] = spec + k * g.n_max;
+        na.coef = op ? d_g : d_f;
+        CK(launch_nega_twist(na, st));
+        const int rc = forward(ps, spec, g.n_max, nullptr, (size_t)N, L, st, false, 1, nullptr, nullptr, nullptr,
+                               nullptr, true);
+        if (rc) return rc;
+    }
+    int rc = inverse(ps, specA, square ? specA : specB, g.n_max, L, st, square);
+    if (rc) return rc;
+    for (int k = 0; k < 3; k++) {
+        na.spec[k] = specA + k * g.n_max;
+        na.hi[k] = ti.hi[k];
+        na.lo[k] = ti.lo[k];
+        na.garner[k] = g.garner[k];
+    }
+    na.out = d_out;
+    na.q01_lo = g.q01_lo;
+    na.q01_hi = g.q01_hi;
+    {
+        typedef unsigned __int128 u128;
+        const u128 q01 = ((u128)g.q01_hi << 64) | g.q01_lo;
+        const uint64_t q2 = prime_value(2);
+        const u128 lo = (u128)(uint64_t)q01 * q2, hi = (u128)(uint64_t)(q01 >> 64) * q2;
+        const u128 mid = (lo >> 64) + (uint64_t)hi;
+        na.m[0] = (uint64_t)lo;
+        na.m[1] = (uint64_t)mid;
+        na.m[2] = (uint64_t)(hi >> 64) + (uint64_t)(mid >> 64);
+        // (M - 1) / 2: M is odd
+        na.half[0] = (na.m[0] >> 1) | (na.m[1] << 63);
+        na.half[1] = (na.m[1] >> 1) | (na.m[2] << 63);
+        na.half[2] = na.m[2] >> 1;
+    }
+    CK(launch_nega_finish(na, st));
+    return GBNTT_OK;
+}
+
 static void *pinned_device_ptr(const void *p)
 {
     cudaPointerAttributes at;
@@ -1550,6 +1615,12 @@ int gbntt_set_coeff_bits(int bits)
 }
 
 int gbntt_coeff_bits(void) { return g.bigint_coeff_bits; }
+
+int gbntt_negacyclic_mul_u64(uint64_t *d_out, const uint64_t *d_f, const uint64_t *d_g, int log_n, void *stream)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    return negacyclic_dev(d_out, d_f, d_g, log_n, (cudaStream_t)stream);
+}
 
 int gbntt_batch_mul_u32(uint32_t *const *d_c, const uint32_t *const *d_a, const size_t *na,
                         const uint32_t *const *d_b, const size_t *nb, int count, void *stream)

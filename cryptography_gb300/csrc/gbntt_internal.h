@@ -107,6 +107,25 @@ long long carry_tiles(long long n_out);
 long long carry_tiles64(long long n_out);
 cudaError_t launch_fill_splitmix(uint32_t *d, long long n, uint64_t seed, cudaStream_t st);
 cudaError_t launch_copy_words(uint32_t *dst, const uint32_t *src, long long n, int grid, cudaStream_t st);
+
+// Negacyclic products (gbntt_negacyclic.cu): the twist writes psi^i-scaled
+// residues of coef into spec[0..2]; the finish untwists spec, reconstructs
+// each coefficient modulo M = q0 q1 q2 and writes it to out as a signed
+// 256-bit integer (4 words, least significant first).
+struct NegaArgs {
+    uint64_t *spec[3];            // residues per prime
+    const uint64_t *coef;         // twist: N input coefficients
+    const uint64_t *hi[3], *lo[3];// twiddle tables (forward for the twist, inverse for the finish)
+    int shift;                    // psi^i = w^(i << shift)
+    long long n;                  // N
+    uint64_t *out;                // finish: 4 N words
+    uint64_t garner[3];           // Montgomery Garner constants (three-prime set)
+    uint64_t q01_lo, q01_hi;      // q0 q1
+    uint64_t m[3];                // M = q0 q1 q2
+    uint64_t half[3];             // (M - 1) / 2
+};
+cudaError_t launch_nega_twist(const NegaArgs &a, cudaStream_t st);
+cudaError_t launch_nega_finish(const NegaArgs &a, cudaStream_t st);
 cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *b, uint64_t *out, long long n,
                           cudaStream_t stream);
 

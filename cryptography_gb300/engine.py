@@ -47,7 +47,7 @@ EXPORTS = (
     "gbntt_split_terms_needed", "gbntt_e_required_log", "gbntt_binary_split", "gbntt_newton_reciprocal_u32",
     "gbntt_div_newton_u32", "gbntt_pow10_u32", "gbntt_to_decimal_u32", "gbntt_compute_e",
     "gbntt_set_prime_set", "gbntt_prime_set", "gbntt_debug_lookback_timeout", "gbntt_autotune",
-    "gbntt_wave_graphs",
+    "gbntt_wave_graphs", "gbntt_negacyclic_mul_u64",
 )
 
 _lib = None
@@ -164,6 +164,8 @@ def lib():
                                  ctypes.POINTER(ctypes.c_float)]
     L.gbntt_autotune.restype = ctypes.c_int
     L.gbntt_wave_graphs.restype = ctypes.c_int
+    L.gbntt_negacyclic_mul_u64.argtypes = [_vp, _vp, _vp, ctypes.c_int, _vp]
+    L.gbntt_negacyclic_mul_u64.restype = ctypes.c_int
     L.gbntt_last_error.restype = ctypes.c_char_p
     L.gbntt_stream.restype = _vp
     _lib = L
@@ -277,6 +279,43 @@ def mul64(a, b):
     _check(lib().gbntt_mul_u64_host(c.ctypes.data_as(_u64p), a.ctypes.data_as(_u64p), len(a),
                                     b.ctypes.data_as(_u64p), len(b)))
     return c
+
+
+def negacyclic_mul_device(out_ptr, f_ptr, g_ptr, log_n, stream=None):
+    """Negacyclic product mod X^N + 1 (N = 2^log_n) of device uint64
+    coefficient arrays; out receives 4 N words (signed 256-bit values)."""
+    _check(lib().gbntt_negacyclic_mul_u64(out_ptr, f_ptr, g_ptr, int(log_n), stream))
+
+
+def negacyclic_mul(f, g):
+    """Host convenience around negacyclic_mul_device: f, g uint64 arrays of
+    the same power-of-two length N; returns N Python ints (signed)."""
+    from . import cudart
+    f = _u64(f)
+    same = g is f
+    g = f if same else _u64(g)
+    n = len(f)
+    if n == 0 or n & (n - 1) or len(g) != n:
+        raise ValueError("f and g need the same power-of-two length")
+    log_n = n.bit_length() - 1
+    df = cudart.DeviceBuffer(8 * n)
+    dg = df if same else cudart.DeviceBuffer(8 * n)
+    do = cudart.DeviceBuffer(32 * n)
+    try:
+        df.upload(f)
+        if not same:
+            dg.upload(g)
+        negacyclic_mul_device(do.ptr, df.ptr, dg.ptr, log_n, lib().gbntt_stream())
+        cudart.stream_sync(lib().gbntt_stream())
+        words = do.download(np.uint64, 4 * n).reshape(n, 4)
+    finally:
+        for b in {id(df): df, id(dg): dg, id(do): do}.values():
+            b.free()
+    out = []
+    for w in words:
+        v = int(w[0]) | (int(w[1]) << 64) | (int(w[2]) << 128) | (int(w[3]) << 192)
+        out.append(v - (1 << 256) if v >> 255 else v)
+    return out
 
 
 def batch_mul_device(c_ptrs, a_ptrs, na, b_ptrs, nb, stream=None):

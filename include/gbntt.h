@@ -144,6 +144,18 @@ int gbntt_mul_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t 
                   void *stream);
 int gbntt_sqr_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, void *stream);
 
+/* Negacyclic polynomial product (the reference's crt_ntt negacyclic
+ * pipeline, ntt/lib/main.hip:557-684, twist / NTT / pointwise / inverse NTT /
+ * untwist / Garner): for N = 2^log_n and f, g of N 64-bit coefficients,
+ *   out[k] = sum_{i+j=k} f_i g_j - sum_{i+j=k+N} f_i g_j   (mod X^N + 1),
+ * exact, as signed 256-bit two's complement integers (4 uint64 words per
+ * coefficient, least significant first; |out[k]| < N 2^128). Device
+ * pointers, stream-ordered; d_g == d_f squares. Three 64-bit primes
+ * (modulus ~2^192). 5 <= log_n <= min(29, the initialised maximum). The
+ * reference writes the unsigned residue modulo its four-prime modulus
+ * (U256); here the value itself is written. */
+int gbntt_negacyclic_mul_u64(uint64_t *d_out, const uint64_t *d_f, const uint64_t *d_g, int log_n, void *stream);
+
 /* Batched products (no reference counterpart; the reference runs one
  * product at a time): d_c[i][0 .. na[i]+nb[i]) = d_a[i] * d_b[i] for
  * i < count. The arrays are host arrays of device pointers and sizes. The

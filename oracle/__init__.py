@@ -177,3 +177,32 @@ def from_int(v, n=None):
 
 def num_threads():
     return int(lib().oracle_num_threads())
+
+
+def negacyclic_mul(f, g):
+    """Negacyclic convolution mod X^N + 1 of two length-N sequences of
+    unsigned 64-bit coefficients, as exact Python ints (signed):
+    c_k = sum_{i+j=k} f_i g_j - sum_{i+j=k+N} f_i g_j. This is the product
+    the reference's crt_ntt negacyclic pipeline computes
+    (ntt/lib/main.hip:557-684), stated by its definition; evaluated here by
+    Kronecker substitution (one big-integer product of the two sequences
+    packed into byte-aligned slots wide enough for every full-product
+    coefficient, < N 2^128)."""
+    f = np.ascontiguousarray(f, dtype=np.uint64)
+    g = np.ascontiguousarray(g, dtype=np.uint64)
+    n = len(f)
+    if len(g) != n:
+        raise ValueError("f and g need the same length")
+    if n == 0:
+        return []
+    slot = (128 + n.bit_length() + 8) // 8   # bytes per slot
+
+    def pack(x):
+        buf = np.zeros((n, slot), dtype=np.uint8)
+        buf[:, :8] = x.view(np.uint8).reshape(n, 8)
+        return int.from_bytes(buf.tobytes(), "little")
+
+    prod = pack(f) * pack(g)
+    raw = np.frombuffer(prod.to_bytes(2 * n * slot, "little"), dtype=np.uint8).reshape(2 * n, slot)
+    d = [int.from_bytes(raw[k].tobytes(), "little") for k in range(2 * n)]
+    return [d[k] - d[k + n] for k in range(n)]
