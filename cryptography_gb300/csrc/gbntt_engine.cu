@@ -509,8 +509,10 @@ static int join_aux(cudaStream_t st, cudaStream_t aux)
 static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void *limbs, size_t n, int L,
                    cudaStream_t st, bool packed = false, long long W = 1, const uint32_t *const *limb_tab = nullptr,
                    const long long *len_tab = nullptr, cudaStream_t aux = nullptr, uint32_t *stage = nullptr,
-                   bool preloaded = false)
+                   bool preloaded = false, cudaEvent_t after_first = nullptr)
 {
+    // after_first (optional): recorded on st once the first pass of the
+    // first prime is enqueued (the operand's limbs have then been read)
     // preloaded: spec already holds the residues (the first pass reads them)
     int pl[kMaxPasses];
     const int np = plan_passes(L, pl);
@@ -549,6 +551,7 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
             CK(launch_pass_any(ps.pi[k], pl[i], 0, i == 0 ? ld0 : LD_U64, a, sk));
             rec_end(sk);
         }
+        if (i == 0 && after_first) CK(cudaEventRecord(after_first, st));
         a.stage_out = nullptr;
         log_m -= pl[i];
     }
@@ -637,9 +640,20 @@ static int carry(const PrimeSet &ps, uint32_t *d_c, size_t n_out, const uint64_t
 
 // b_ready (optional): an event the second operand's transform waits for
 // (its host -> device copy on another stream).
+// Host -> device copy of the second operand, issued by mul_dev once the
+// first operand's first pass has read its limbs (both share the host link).
+struct StageJob {
+    uint32_t *dst = nullptr;
+    const uint32_t *src = nullptr;   // device-mapped pinned memory, or a host pointer
+    size_t n = 0;
+    bool mapped = false;
+};
+
 // stage_a (optional): HBM copy of A made by its first pass (see forward).
+// stage_b (optional): copy of B into d_b, run on the copy stream while A is
+// transformed.
 static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb, cudaStream_t st,
-                   cudaEvent_t b_ready = nullptr, uint32_t *stage_a = nullptr)
+                   const StageJob *stage_b = nullptr, uint32_t *stage_a = nullptr)
 {
     if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
     if (!st) st = g.stream;
@@ -658,12 +672,17 @@ static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t
     uint64_t *specB = g.d_spec + 3 * g.n_max;
     const PrimeSet &ps = coef32_set();
     cudaStream_t aux = fork_aux(ps, st, g.stream2);
-    int rc = forward(ps, specA, g.n_max, d_a, na, L, st, false, 1, nullptr, nullptr, aux, stage_a);
+    int rc = forward(ps, specA, g.n_max, d_a, na, L, st, false, 1, nullptr, nullptr, aux, stage_a, false,
+                     stage_b ? g.ev_a : nullptr);
     if (rc) return rc;
     if (!square) {
-        if (b_ready) {
-            CK(cudaStreamWaitEvent(st, b_ready, 0));
-            if (aux) CK(cudaStreamWaitEvent(aux, b_ready, 0));
+        if (stage_b) {
+            CK(cudaStreamWaitEvent(g.cstream, g.ev_a, 0));
+            if (stage_b->mapped) CK(launch_copy_words(stage_b->dst, stage_b->src, (long long)stage_b->n, g.sms / 2, g.cstream));
+            else CK(cudaMemcpyAsync(stage_b->dst, stage_b->src, stage_b->n * 4, cudaMemcpyHostToDevice, g.cstream));
+            CK(cudaEventRecord(g.ev_b, g.cstream));
+            CK(cudaStreamWaitEvent(st, g.ev_b, 0));
+            if (aux) CK(cudaStreamWaitEvent(aux, g.ev_b, 0));
         }
         rc = forward(ps, specB, g.n_max, d_b, nb, L, st, false, 1, nullptr, nullptr, aux);
         if (rc) return rc;
@@ -1217,15 +1236,19 @@ static int mul_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b
         if ((rs = stage(da, a, na, g.sms * 4, g.stream)) != GBNTT_OK) return rs;
         ua = da;
     }
-    cudaEvent_t b_ready = nullptr;
+    StageJob jb;
+    const StageJob *stage_b = nullptr;
     if (square) ub = ua;
     else if (!ub) {
-        // B's copy overlaps A's forward transform with a small grid
-        CK(cudaEventRecord(g.ev_a, g.stream));
-        CK(cudaStreamWaitEvent(g.cstream, g.ev_a, 0));
-        if ((rs = stage(db, b, nb, g.sms / 2, g.cstream)) != GBNTT_OK) return rs;
-        CK(cudaEventRecord(g.ev_b, g.cstream));
-        b_ready = g.ev_b;
+        // B is copied by mul_dev on the copy stream (a small-grid copy
+        // kernel for pinned memory) after A's first pass: it then overlaps
+        // A's remaining passes instead of sharing the host link with them
+        const uint32_t *mapped = g.zero_copy ? (const uint32_t *)pinned_device_ptr(b) : nullptr;
+        jb.dst = db;
+        jb.src = mapped ? mapped : b;
+        jb.n = nb;
+        jb.mapped = mapped != nullptr;
+        stage_b = &jb;
         ub = db;
     }
     if (g.prof) {
@@ -1233,7 +1256,7 @@ static int mul_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b
         CK(cudaStreamSynchronize(g.cstream));
         double t = now_ms(); g.prof_ms[0] += t - t0; t0 = t;
     }
-    int rc = mul_dev(uc ? uc : dc, ua, na, ub, nb, g.stream, b_ready, stage_a);
+    int rc = mul_dev(uc ? uc : dc, ua, na, ub, nb, g.stream, stage_b, stage_a);
     if (rc) return rc;
     if (g.prof) { CK(cudaStreamSynchronize(g.stream)); double t = now_ms(); g.prof_ms[1] += t - t0; t0 = t; }
     if (!uc) CK(cudaMemcpyAsync(c, dc, n_out * 4, cudaMemcpyDeviceToHost, g.stream));
