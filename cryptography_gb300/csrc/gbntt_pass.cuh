@@ -36,14 +36,19 @@ namespace gbntt {
 enum PassLayout { LAYOUT_STRIDED = 0, LAYOUT_CONTIG = 1 };
 
 #ifndef GBNTT_PASS_MIN_BLOCKS
-#define GBNTT_PASS_MIN_BLOCKS 5   // resident CTAs per SM the register budget targets (measured best of 3..6)
+#define GBNTT_PASS_MIN_BLOCKS 5   // resident CTAs per SM the register budget targets, 2^9/2^10-point passes (measured best of 3..6)
+#endif
+#ifndef GBNTT_PASS_MIN_BLOCKS_SMALL
+#define GBNTT_PASS_MIN_BLOCKS_SMALL 7   // the same for passes of up to 2^8 points (2^29: 5 -> 59.9 ms, 7 -> 59.4 ms)
 #endif
 #ifndef GBNTT_PASS_MIN_BLOCKS32
 #define GBNTT_PASS_MIN_BLOCKS32 8  // the same for the 32-bit prime (measured 5..10 at 2^29: 8 within 1%, no spills of note)
 #endif
-template <int PI>
+template <int PI, int LOG_L>
 struct PassMinBlocks {
-    static constexpr int value = sizeof(typename Field<PI>::T) == 4 ? GBNTT_PASS_MIN_BLOCKS32 : GBNTT_PASS_MIN_BLOCKS;
+    static constexpr int value = sizeof(typename Field<PI>::T) == 4
+                                     ? GBNTT_PASS_MIN_BLOCKS32
+                                     : (LOG_L <= 8 ? GBNTT_PASS_MIN_BLOCKS_SMALL : GBNTT_PASS_MIN_BLOCKS);
 };
 constexpr int kPassThreads = 128;
 constexpr int kLogPassThreads = 7;
@@ -490,7 +495,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
 }
 
 template <int PI, int LOG_L, int DIR, int LD, int LAYOUT>
-__global__ void __launch_bounds__(kPassThreads, PassMinBlocks<PI>::value) ntt_pass_kernel(PassArgs a)
+__global__ void __launch_bounds__(kPassThreads, PassMinBlocks<PI, LOG_L>::value) ntt_pass_kernel(PassArgs a)
 {
     extern __shared__ uint64_t sm[];
     using S_ = PassShape<LOG_L, sizeof(typename Field<PI>::T)>;
@@ -504,7 +509,7 @@ __global__ void __launch_bounds__(kPassThreads, PassMinBlocks<PI>::value) ntt_pa
 // tile is transformed and stored, so global-load latency is hidden behind
 // the DFTs instead of being waited out by every CTA.
 template <int PI, int LOG_L, int DIR, int LAYOUT>
-__global__ void __launch_bounds__(kPassThreads, PassMinBlocks<PI>::value) ntt_pass_kernel_pipe(PassArgs a)
+__global__ void __launch_bounds__(kPassThreads, PassMinBlocks<PI, LOG_L>::value) ntt_pass_kernel_pipe(PassArgs a)
 {
     extern __shared__ uint64_t smraw[];
     using V = typename Field<PI>::T;
