@@ -273,6 +273,42 @@ __global__ void dec_leaf_kernel(const uint32_t *pieces, int stride, long long fi
     }
 }
 
+// Batched limb additions for the engine's split products (gbntt_engine.cu):
+// out_i = x_i + y_i over n_i limbs each, on stream st; the sums fit in n_i
+// limbs (no carry leaves the top). Item table and tile status come from the
+// stream-ordered pool. Look-back wait failures set bits in *err.
+int batch_add_limbs(const uint32_t *const *x, const uint32_t *const *y, uint32_t *const *out, const long long *n,
+                    int count, cudaStream_t st, unsigned *err)
+{
+    std::vector<AddItem> run;
+    run.reserve((size_t)count);
+    long long tiles = 0;
+    for (int i = 0; i < count; i++) {
+        if (n[i] <= 0) continue;
+        run.push_back({x[i], y[i], out[i], nullptr, n[i], n[i], n[i], tiles});
+        tiles += (n[i] + kAddTile - 1) / kAddTile;
+    }
+    if (run.empty()) return GBNTT_OK;
+    if (tiles > 0x7FFFFFFFLL) return GBNTT_ERR_SIZE;
+    void *d = nullptr, *ctl = nullptr;
+    if (cudaMallocAsync(&d, run.size() * sizeof(AddItem), st) != cudaSuccess ||
+        cudaMallocAsync(&ctl, ((size_t)tiles + 1) * sizeof(unsigned), st) != cudaSuccess) {
+        if (d) cudaFreeAsync(d, st);
+        (void)cudaGetLastError();
+        return GBNTT_ERR_ALLOC;
+    }
+    cudaError_t e = cudaMemcpyAsync(d, run.data(), run.size() * sizeof(AddItem), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctl, 0, ((size_t)tiles + 1) * sizeof(unsigned), st);
+    if (e == cudaSuccess) {
+        addsub_kernel<<<(unsigned)tiles, kAddThreads, 0, st>>>((const AddItem *)d, (int)run.size(), 0, (unsigned *)ctl,
+                                                               (unsigned *)ctl + 1, err);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(d, st);
+    cudaFreeAsync(ctl, st);
+    return e == cudaSuccess ? GBNTT_OK : GBNTT_ERR_CUDA;
+}
+
 // ---------------------------------------------------------------------------
 // Host orchestration
 // ---------------------------------------------------------------------------

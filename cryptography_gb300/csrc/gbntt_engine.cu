@@ -79,6 +79,8 @@ struct Engine {
     bool zero_copy = true;          // host-pointer calls: kernels read/write pinned host memory directly
     bool stage_inputs = true;       // ... except the operands, copied once to HBM (B's copy overlaps A's transform)
     bool graphs = true;             // batched waves replayed as CUDA graphs
+    bool batch_split = true;        // uneven batch products split into chunk products
+    int split_ratio_log = 3;        // ... when the longer operand is >= 2^this x the shorter
     uint64_t garner2[2] = {0, 0};   // two-prime Garner constants (p3 Montgomery multipliers)
     unsigned *d_ctl = nullptr;      // [0] ticket, [1] error, [2..] tile status
     size_t n_status = 0;
@@ -441,6 +443,10 @@ static int init_impl(int max_log)
         g.overlap = !(ov && ov[0] == '0');
         // (measured at 2^28 limbs through ntt_bigint_mul: 105 ms against 110 ms
         // through the staging buffer)
+        const char *bs = getenv("GBNTT_BATCH_SPLIT");
+        g.batch_split = !(bs && bs[0] == '0');
+        const char *sr = getenv("GBNTT_SPLIT_RATIO_LOG");
+        g.split_ratio_log = sr ? std::max(1, atoi(sr)) : 3;
         const char *gr = getenv("GBNTT_GRAPHS");
         g.graphs = !(gr && gr[0] == '0');
         const char *si = getenv("GBNTT_STAGE_INPUTS");
@@ -940,15 +946,40 @@ static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStrea
 
 static int g_batch_slot = 0;
 
+// Uneven products in a batch: a product whose longer operand (nB limbs) is
+// at least 2^split_ratio_log times its shorter one (nS limbs, at least
+// kSplitMinShort) and whose transform would be longer than the chunks' is
+// split into chunk products: the longer operand in
+// chunks of 2^ls - nS + 1 limbs (2^ls = 4 x the power of two >= nS), each
+// multiplied by the shorter operand at transform length 2^ls, so a
+// 2^21 x 2^13 product becomes 86 products of 2^15 points (the shorter
+// operand, common to all chunks of a wave, is transformed once) instead of
+// three transforms of 2^22 points. Even-numbered chunk products land
+// side by side in one buffer E and odd-numbered ones in O (consecutive
+// chunk products overlap by nS limbs, every second one does not), and the
+// product is E + O by one batched carry-propagating addition.
+constexpr size_t kSplitMinShort = 64;
+
 static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const size_t *na,
                      const uint32_t *const *d_b, const size_t *nb, int count, cudaStream_t st)
 {
     if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
     if (count < 0 || (count > 0 && (!d_c || !d_a || !na || !d_b || !nb))) { set_err("bad batch arguments"); return GBNTT_ERR_ARG; }
     if (!st) st = g.stream;
-    std::vector<std::pair<int, int>> order;   // (log N, index)
-    order.reserve(count);
-    for (int i = 0; i < count; i++) {
+    struct Keyed {
+        int L;
+        long long group;   // items of one split stay together (shared operand per wave)
+        BatchItem item;
+    };
+    struct Split {
+        uint32_t *E, *O, *c;
+        long long n;
+    };
+    std::vector<Keyed> all;
+    std::vector<Split> splits;
+    all.reserve(count);
+    int rc = GBNTT_OK;
+    for (int i = 0; i < count && rc == GBNTT_OK; i++) {
         if (na[i] == 0 || nb[i] == 0) {
             if (na[i] + nb[i]) CK(cudaMemsetAsync(d_c[i], 0, (na[i] + nb[i]) * sizeof(uint32_t), st));
             continue;
@@ -956,32 +987,79 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
         const int L = choose_log(na[i], nb[i]);
         if (L > g.max_log) {
             set_err("batch product %d needs 2^%d coefficients; engine initialised for 2^%d", i, L, g.max_log);
-            return GBNTT_ERR_SIZE;
+            rc = GBNTT_ERR_SIZE;
+            break;
         }
-        order.push_back({L, i});
-    }
-    std::stable_sort(order.begin(), order.end());
-    BatchCtx x{g.d_spec, g.n_max, g.d_ctl, g.n_status, g.d_btab, g.h_btab, g.btab_ev, &g_batch_slot};
-    std::vector<BatchItem> items;
-    size_t pos = 0;
-    while (pos < order.size()) {
-        const int L = order[pos].first;
-        size_t end = pos;
-        while (end < order.size() && order[end].first == L) end++;
-        const long long wmax = std::min<long long>(kMaxBatch, (long long)(g.n_max >> L));
-        for (size_t w0 = pos; w0 < end; w0 += (size_t)wmax) {
-            const long long W = std::min<long long>(wmax, (long long)(end - w0));
-            items.clear();
-            for (long long k = 0; k < W; k++) {
-                const int i = order[w0 + k].second;
-                items.push_back({d_c[i], d_a[i], d_b[i], na[i], nb[i]});
+        const bool a_short = na[i] <= nb[i];
+        const size_t nS = a_short ? na[i] : nb[i], nB = a_short ? nb[i] : na[i];
+        const uint32_t *S = a_short ? d_a[i] : d_b[i], *Bp = a_short ? d_b[i] : d_a[i];
+        int ls = kMinLog;
+        while (((size_t)1 << ls) < 4 * nS) ls++;
+        if (g.batch_split && nS >= kSplitMinShort && L > ls && nB >= (nS << g.split_ratio_log)) {
+            const size_t chunk = ((size_t)1 << ls) - nS + 1;
+            const size_t n_out = nB + nS;
+            void *E = nullptr, *O = nullptr;
+            if (cudaMallocAsync(&E, n_out * sizeof(uint32_t), st) != cudaSuccess ||
+                cudaMallocAsync(&O, n_out * sizeof(uint32_t), st) != cudaSuccess) {
+                if (E) cudaFreeAsync(E, st);
+                (void)cudaGetLastError();
+                set_err("batch split: stream-ordered allocation of %zu limbs failed", 2 * n_out);
+                rc = GBNTT_ERR_ALLOC;
+                break;
             }
-            const int rc = batch_wave(x, items.data(), W, L, st, g.stream2);
-            if (rc) return rc;
+            splits.push_back({(uint32_t *)E, (uint32_t *)O, d_c[i], (long long)n_out});
+            CK(cudaMemsetAsync(E, 0, n_out * sizeof(uint32_t), st));
+            CK(cudaMemsetAsync(O, 0, n_out * sizeof(uint32_t), st));
+            for (size_t j = 0, off = 0; off < nB; j++, off += chunk) {
+                const size_t len = std::min(chunk, nB - off);
+                uint32_t *dst = ((j & 1) ? (uint32_t *)O : (uint32_t *)E) + off;
+                all.push_back({choose_log(len, nS), (long long)i, {dst, Bp + off, S, len, nS}});
+            }
+            continue;
         }
-        pos = end;
+        all.push_back({L, (long long)i, {d_c[i], d_a[i], d_b[i], na[i], nb[i]}});
     }
-    return GBNTT_OK;
+    if (rc == GBNTT_OK) {
+        std::stable_sort(all.begin(), all.end(), [](const Keyed &x, const Keyed &y) {
+            return x.L != y.L ? x.L < y.L : x.group < y.group;
+        });
+        BatchCtx x{g.d_spec, g.n_max, g.d_ctl, g.n_status, g.d_btab, g.h_btab, g.btab_ev, &g_batch_slot};
+        std::vector<BatchItem> items;
+        size_t pos = 0;
+        while (pos < all.size() && rc == GBNTT_OK) {
+            const int L = all[pos].L;
+            size_t end = pos;
+            while (end < all.size() && all[end].L == L) end++;
+            const long long wmax = std::min<long long>(kMaxBatch, (long long)(g.n_max >> L));
+            for (size_t w0 = pos; w0 < end && rc == GBNTT_OK; w0 += (size_t)wmax) {
+                const long long W = std::min<long long>(wmax, (long long)(end - w0));
+                items.clear();
+                for (long long k = 0; k < W; k++) items.push_back(all[w0 + k].item);
+                rc = batch_wave(x, items.data(), W, L, st, g.stream2);
+            }
+            pos = end;
+        }
+    }
+    if (!splits.empty()) {
+        if (rc == GBNTT_OK) {
+            std::vector<const uint32_t *> ex(splits.size()), ey(splits.size());
+            std::vector<uint32_t *> eo(splits.size());
+            std::vector<long long> en(splits.size());
+            for (size_t k = 0; k < splits.size(); k++) {
+                ex[k] = splits[k].E;
+                ey[k] = splits[k].O;
+                eo[k] = splits[k].c;
+                en[k] = splits[k].n;
+            }
+            rc = batch_add_limbs(ex.data(), ey.data(), eo.data(), en.data(), (int)splits.size(), st, g.d_ctl + 1);
+            if (rc) set_err("batch split: the chunk-product addition failed");
+        }
+        for (auto &sp : splits) {
+            cudaFreeAsync(sp.E, st);
+            cudaFreeAsync(sp.O, st);
+        }
+    }
+    return rc;
 }
 
 // ---------------------------------------------------------------------------

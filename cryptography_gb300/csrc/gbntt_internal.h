@@ -126,6 +126,10 @@ struct NegaArgs {
 };
 cudaError_t launch_nega_twist(const NegaArgs &a, cudaStream_t st);
 cudaError_t launch_nega_finish(const NegaArgs &a, cudaStream_t st);
+
+// Batched limb additions out_i = x_i + y_i over n_i limbs (gbntt_e.cu).
+int batch_add_limbs(const uint32_t *const *x, const uint32_t *const *y, uint32_t *const *out, const long long *n,
+                    int count, cudaStream_t st, unsigned *err);
 cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *b, uint64_t *out, long long n,
                           cudaStream_t stream);
 

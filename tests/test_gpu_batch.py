@@ -149,3 +149,31 @@ def test_batch_shared_right_operand(engine):
                 x.free()
         db.free()
     assert engine.device_errors() == 0
+
+
+def test_batch_uneven_products_split(engine):
+    # lopsided pairs (longer operand >= 8x the shorter, shorter >= 64 limbs)
+    # run as chunk products of the shorter operand's size plus one addition;
+    # both operand orders, the size thresholds, thousands of chunks, and a
+    # mix with balanced products: every result must equal the single
+    # product (which runs one full-length transform) and GMP
+    rng = np.random.default_rng(808)
+    shapes = [(100000, 64), (64, 100000), ((1 << 18) + 5, 3000), (5000, (1 << 17) - 3),
+              (70000, 63), (4096, 512), (4095, 512), ((1 << 20) + 11, 100), (3000, 2900),
+              (1 << 16, 1 << 16), (200, 1 << 15), (1 << 19, 1 << 12)]
+    A, B = [], []
+    for na, nb in shapes:
+        A.append(rng.integers(0, 1 << 32, na, dtype=np.uint64).astype(np.uint32))
+        B.append(rng.integers(0, 1 << 32, nb, dtype=np.uint64).astype(np.uint32))
+    A.append(np.full(1 << 17, 0xFFFFFFFF, dtype=np.uint32))   # all-ones: longest carries
+    B.append(np.full(700, 0xFFFFFFFF, dtype=np.uint32))
+    for _ in range(2):   # the second round replays the wave graphs
+        got = _run_batch(engine, A, B)
+        for i, (a, b, c) in enumerate(zip(A, B, got)):
+            want = np.zeros(len(a) + len(b), dtype=np.uint32)
+            r = oracle.gmp_mul(a, b)
+            want[:len(r)] = r
+            assert np.array_equal(c, want), (i, len(a), len(b))
+            if i % 3 == 0:
+                assert np.array_equal(c, engine.mul(a, b)), i
+    assert engine.device_errors() == 0
