@@ -202,12 +202,12 @@ int plan_passes(int log_n, int *p)
     // points beat 2^9 and 2^10 even at the cost of a fourth pass: their
     // register DFTs are shorter (fewer registers, a smaller loop body), and
     // the extra sweep over HBM is cheap next to the integer work (2^29:
-    // [6, 8, 8, 7] 60.6 ms, [9, 10, 10] about 67 ms).
+    // [7, 7, 8, 7] 58.8 ms, [9, 10, 10] about 67 ms).
     constexpr int kTunedLo = 18;
     static const signed char kTuned[kMaxLog + 1 - kTunedLo][1 + kMaxPasses] = {
         {3, 6, 6, 6},    {3, 6, 7, 6},    {3, 6, 6, 8},    {3, 5, 8, 8},     // 2^18 .. 2^21
-        {3, 6, 8, 8},    {3, 8, 8, 7},    {3, 8, 8, 8},    {3, 9, 8, 8},     // 2^22 .. 2^25
-        {3, 9, 9, 8},    {4, 6, 7, 7, 7}, {4, 6, 7, 8, 7}, {4, 6, 8, 8, 7},  // 2^26 .. 2^29
+        {3, 6, 8, 8},    {3, 8, 8, 7},    {3, 8, 8, 8},    {3, 8, 8, 9},     // 2^22 .. 2^25
+        {3, 8, 8, 10},   {4, 6, 7, 7, 7}, {4, 7, 7, 7, 7}, {4, 7, 7, 8, 7},  // 2^26 .. 2^29
         {4, 7, 8, 8, 7},                                                    // 2^30
     };
     if (log_n >= kTunedLo && log_n <= kMaxLog) {
