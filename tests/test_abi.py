@@ -70,3 +70,14 @@ def test_plan_overrides_host_logic(built_lib):
     finally:
         engine.set_plan(29, [])
     assert engine.plan(29) == default
+
+
+def test_default_plans_are_valid_factorisations(built_lib):
+    # every transform length the engine accepts has a default plan of 1-4
+    # passes of 2^5..2^10 points summing to it, smallest lengths in one pass
+    for log_n in range(5, 31):
+        p = engine.plan(log_n)
+        assert 1 <= len(p) <= 4 and sum(p) == log_n, (log_n, p)
+        assert all(5 <= x <= 10 for x in p), (log_n, p)
+        if log_n <= 10:
+            assert p == [log_n]
