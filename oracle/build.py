@@ -5,7 +5,7 @@
 * ``build_ref()`` compiles the reference's own host sources, by path from the
   reference checkout, together with ``ref_shim.cpp`` into
   ``oracle/_ref/libref.so``. Nothing from the reference is copied; when the
-  checkout is absent (the GPU machine) it is skipped and the tests that need it
+  checkout is absent (machines without it) it is skipped and the tests that need it
   skip too.
 """
 import os

@@ -39,7 +39,7 @@
 
 typedef unsigned __int128 u128;
 
-/* Prime index 0,1,2 of this build = reference P0, P2, P3. */
+/* Prime index 0,1,2 of this engine = reference P0, P2, P3. */
 static const uint64_t ORC_P[3] = {
     UINT64_C(0xffffffff00000001),   /* 2^64 - 2^32 + 1 */
     UINT64_C(0xfffffffc00000001),   /* 2^64 - 2^34 + 1 */

@@ -7,7 +7,7 @@ Run here, where the reference checkout exists:
 It compiles the reference's primes.h / shoup.h / garner.hip / bigint.c by
 path (oracle/build.py -> oracle/_ref/libref.so) and records their outputs on
 seeded inputs, plus GMP products. The committed JSON then pins the oracle on
-machines without the reference (the GPU machine).
+machines without the reference checkout.
 
 Sections:
   modops   reduce_p*/mulmod/addmod/submod/shoup_mul of the reference
@@ -31,7 +31,7 @@ import oracle  # noqa: E402
 from cryptography_gb300 import synth  # noqa: E402
 
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.json")
-REF_PIDX = (0, 2, 3)   # reference prime index of this build's primes 0, 1, 2
+REF_PIDX = (0, 2, 3)   # reference prime index of this engine's primes 0, 1, 2
 M64 = (1 << 64) - 1
 
 

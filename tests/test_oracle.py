@@ -38,7 +38,7 @@ def test_modops_match_reference(golden, section):
 
 
 def test_shoup_equals_mulmod(golden):
-    # the reference's Shoup twiddle multiply and this build's multiply agree
+    # the reference's Shoup twiddle multiply and this engine's multiply agree
     for i, m in enumerate(golden["modops"]):
         for t, w, want in m["shoup_mul"]:
             assert oracle.lib().oracle_mulmod(i, t, w) == want
