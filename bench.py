@@ -2,12 +2,14 @@
 """Benchmark of the CRT-NTT big-integer multiply on one GB300.
 
 Workload (default): one multiply of two seeded uniform-random operands of
-2^28 32-bit limbs (1 GiB each), transform length N = 2^29 per prime over the
-three primes 2^64 - 2^b + 1 (b = 32, 34, 40), uint64 residues. A step is one
-full multiply (decomposition, 2 x 3 forward transforms, pointwise product,
-3 inverse transforms, Garner + carry). Inputs (2 x 1 GiB) and the 24 GiB of
-spectra are far larger than the 129 MB L2, so no L2 flush is needed between
-steps.
+2^28 32-bit limbs (1 GiB each), transform length N = 2^29 per prime over two
+primes: q0 = 2^64 - 2^32 + 1 (uint64 residues) and p3 = 3 * 2^30 + 1
+(uint32 residues), whose product exceeds every coefficient of the product
+(the reference's three 64-bit primes 2^64 - 2^b + 1, b = 32, 34, 40, are
+timed beside it). A step is one full multiply (decomposition, 2 x 2 forward
+transforms, pointwise product, 2 inverse transforms, Garner + carry).
+Inputs (2 x 1 GiB) and the 12 GiB of spectra are far larger than the 129 MB
+L2, so no L2 flush is needed between steps.
 
 Prints one JSON line. ``value`` is milliseconds per multiply with the
 operands already resident in HBM (CUDA events on the engine stream); ``e2e``
@@ -49,6 +51,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-log-limbs", type=int, default=22, help="CPU baseline sample size 2^k limbs")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-full", type=int, default=1,
+                    help="also time one full-size product by the CPU port (all cores but one) and GMP (one core)")
     ap.add_argument("--plan", default="", help="comma-separated pass sizes overriding the default plan")
     ap.add_argument("--no-packed", action="store_true", help="skip the packed (64-bit coefficient) measurement")
     ap.add_argument("--batch-pairs", type=int, default=4096)
@@ -204,13 +208,69 @@ def cpu_baseline(log_limbs_sample, log_limbs_target, reps=1, with_gmp=True):
     return out
 
 
+def _host_mem_available():
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+
+
+def cpu_full_size(log_limbs):
+    """One full-size multiply (2^k x 2^k limbs, the headline workload's own
+    operands) by the oracle CRT-NTT port on all host cores but one, timed
+    while GMP mpz_mul multiplies the same operands on the remaining core;
+    both products are compared. Skipped (with the reason) when the host has
+    too little free memory for both (about 30 GiB for the port at 2^28
+    limbs plus GMP's working space)."""
+    import threading
+    import oracle
+    from cryptography_gb300 import synth
+    n = 1 << log_limbs
+    need = 160 * n
+    avail = _host_mem_available()
+    if avail < need:
+        return {"skipped": "host has %.1f GiB free, the two full-size CPU products need about %.1f GiB"
+                           % (avail / 2 ** 30, need / 2 ** 30)}
+    a = synth.operand(n, 1)
+    b = synth.operand(n, 2)
+    threads = max(1, (os.cpu_count() or 2) - 1)
+    res = {}
+
+    def run_gmp():
+        t0 = time.perf_counter()
+        res["gmp"] = oracle.gmp_mul(a, b)
+        res["gmp_s"] = time.perf_counter() - t0
+
+    out = {"operands": "2^%d x 2^%d limbs, seeds 1 and 2 (the headline operands)" % (log_limbs, log_limbs)}
+    th = None
+    if oracle.gmp_available():
+        th = threading.Thread(target=run_gmp)
+        th.start()
+    prev = oracle.num_threads()
+    oracle.set_threads(threads)
+    try:
+        t0 = time.perf_counter()
+        c = oracle.mul(a, b)
+        out["port_s"] = time.perf_counter() - t0
+        out["port_threads"] = threads
+    finally:
+        oracle.set_threads(prev)
+    if th is not None:
+        th.join()
+        out["gmp_s"] = res["gmp_s"]
+        out["gmp_threads"] = 1
+        out["port_equals_gmp"] = bool(np.array_equal(c, res["gmp"]))
+    return out
+
+
 def batched_sizes(pairs, seed, lo=10, hi=22):
     """Operand sizes log-uniform in 2^lo .. 2^hi limbs (independent per
     operand), seeded."""
-    rng = np.random.default_rng(seed)
-    na = np.floor(2.0 ** rng.uniform(lo, hi, pairs)).astype(np.int64)
-    nb = np.floor(2.0 ** rng.uniform(lo, hi, pairs)).astype(np.int64)
-    return na, nb
+    from cryptography_gb300 import synth
+    return synth.batched_sizes(pairs, seed, lo, hi)
 
 
 def run_batched_leg(g, cudart, args, stream):
@@ -420,6 +480,15 @@ def run_reference(args, dist):
             res = r
     v = float(np.median(times))
     res["value"] = v
+    res["value_kind"] = "sample scaled by N log N"
+    if args.cpu_full and not args.no_cpu:
+        # one full-size product measured on the same cores: the scaled
+        # samples are reported next to it, with their error
+        full = cpu_full_size(args.log_limbs)
+        res["measured_full"] = full
+        if "port_s" in full:
+            res["measured_full_s"] = {"port": full["port_s"], "gmp_1thread": full.get("gmp_s")}
+            res["extrapolation_error"] = v / (full["port_s"] * 1e3) - 1.0
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded splitmix64 limbs)",
@@ -654,6 +723,12 @@ def run_gpu(args, dist):
     if dist.rank == 0 and not args.no_cpu:
         try:
             cpu = cpu_baseline(args.cpu_log_limbs, lg)
+            if args.cpu_full:
+                full = cpu_full_size(lg)
+                cpu["measured_full"] = full
+                if "port_s" in full:
+                    cpu["measured_full_s"] = {"port": full["port_s"], "gmp_1thread": full.get("gmp_s")}
+                    cpu["extrapolation_error"] = cpu["value"] / (full["port_s"] * 1e3) - 1.0
         except Exception as ex:   # the baseline is reported, never required
             cpu = {"error": str(ex)}
 

@@ -566,6 +566,68 @@ __device__ __forceinline__ uint64_t gl_reduce4(uint32_t v0, uint32_t v1, uint32_
 }
 #endif
 
+#ifndef GBNTT_Q0_POW2
+#define GBNTT_Q0_POW2 1   // 1: the shorter per-range forms below; 0: the general fold gl_reduce4
+#endif
+
+// Canonical form of w = (w1:w0) < 2^64: w >= q0 exactly when w1 is all ones
+// and w0 is nonzero, and then w - q0 = (0 : w0 - 1).
+#define GBNTT_GL_CANON_W                                  \
+    "setp.eq.u32 p, w1, 0xFFFFFFFF;\n\t"                  \
+    "setp.ne.and.u32 p, w0, 0, p;\n\t"                   \
+    "@p sub.u32 w0, w0, 1;\n\t"                          \
+    "@p mov.u32 w1, 0;\n\t"
+
+// x 2^r for r < 32 as u = (u2 : u1 : u0), u2 < 2^r: (u1:u0) + u2 EPS
+// = (u1:u0) - u2 + (u2 << 32) is below 2^64 + 2^63 (carry c in {0, 1}),
+// folded once by c EPS (no second carry), then made canonical.
+__device__ __forceinline__ uint64_t gl_pow2_q0(uint32_t u0, uint32_t u1, uint32_t u2)
+{
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 s0, s1, b, c, w0, w1;\n\t"
+        ".reg .pred p;\n\t"
+        "sub.cc.u32 s0, %1, %3;\n\t"
+        "subc.cc.u32 s1, %2, 0;\n\t"
+        "subc.u32 b, 0, 0;\n\t"
+        "add.cc.u32 s1, s1, %3;\n\t"
+        "addc.u32 c, b, 0;\n\t"
+        "mad.lo.cc.u32 w0, c, 0xFFFFFFFF, s0;\n\t"
+        "addc.u32 w1, s1, 0;\n\t"
+        GBNTT_GL_CANON_W
+        "mov.b64 %0, {w0, w1};\n\t"
+        "}"
+        : "=l"(r) : "r"(u0), "r"(u1), "r"(u2));
+    return r;
+}
+
+// x 2^(32 + r) for r < 32, u as above: u0 2^32 + u1 2^64 + u2 2^96
+// == (u0 + u1) 2^32 - (u1 + u2) = v2 2^64 + (v1:v0) with v2 in {-1, 0, 1};
+// folding v2 EPS leaves a canonical value unless v2 = 0, so one check.
+__device__ __forceinline__ uint64_t gl_pow2_q1(uint32_t u0, uint32_t u1, uint32_t u2)
+{
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 h, hc, s, sc, v0, v1, v2, n, sg, w0, w1;\n\t"
+        ".reg .pred p;\n\t"
+        "add.cc.u32 h, %1, %2;\n\t"
+        "addc.u32 hc, 0, 0;\n\t"
+        "add.cc.u32 s, %2, %3;\n\t"
+        "addc.u32 sc, 0, 0;\n\t"
+        "sub.cc.u32 v0, 0, s;\n\t"
+        "subc.cc.u32 v1, h, sc;\n\t"
+        "subc.u32 v2, hc, 0;\n\t"
+        "neg.s32 n, v2;\n\t"
+        "shr.s32 sg, v2, 31;\n\t"
+        "add.cc.u32 w0, v0, n;\n\t"
+        "addc.u32 w1, v1, sg;\n\t"
+        GBNTT_GL_CANON_W
+        "mov.b64 %0, {w0, w1};\n\t"
+        "}"
+        : "=l"(r) : "r"(u0), "r"(u1), "r"(u2));
+    return r;
+}
+
 // x * 2^e mod q0 for canonical x and 0 <= e < 96 (e folds to a constant
 // after unrolling, so the shifts and the branch on e / 32 vanish). In q0
 // every 64th root of unity is a power of two (2^96 == -1, 2^192 == 1), so
@@ -578,8 +640,13 @@ __device__ __forceinline__ uint64_t gl_mul_pow2(uint64_t x, int e)
     const uint32_t u0 = x0 << r;
     const uint32_t u1 = r ? ((x1 << r) | (x0 >> (32 - r))) : x1;
     const uint32_t u2 = r ? (x1 >> (32 - r)) : 0u;
+#if GBNTT_Q0_POW2
+    if (q == 0) return gl_pow2_q0(u0, u1, u2);
+    if (q == 1) return gl_pow2_q1(u0, u1, u2);
+#else
     if (q == 0) return gl_reduce4(u0, u1, u2, 0u);
     if (q == 1) return gl_reduce4(0u, u0, u1, u2);
+#endif
     // q == 2: u0 2^64 + u1 2^96 + u2 2^128 == u0 EPS - (u2 2^32 + u1), the
     // subtrahend below 2^63 < q0
     const uint64_t y = ((uint64_t)u0 << 32) - (uint64_t)u0;   // u0 EPS < q0

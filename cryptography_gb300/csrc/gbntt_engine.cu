@@ -79,6 +79,8 @@ struct Engine {
     bool zero_copy = true;          // host-pointer calls: kernels read/write pinned host memory directly
     bool stage_inputs = true;       // ... except the operands, copied once to HBM (B's copy overlaps A's transform)
     bool graphs = true;             // batched waves replayed as CUDA graphs
+    bool pass_tables = true;        // strided passes read their twiddles from pass tables (PassArgs::ptw)
+    size_t ptw_budget = 0;          // ... up to this many bytes of tables in all
     bool batch_split = true;        // uneven batch products split into chunk products
     int split_ratio_log = 3;        // ... when the longer operand is >= 2^this x the shorter
     uint64_t garner2[2] = {0, 0};   // two-prime Garner constants (p3 Montgomery multipliers)
@@ -185,6 +187,71 @@ static uint64_t *tw_ptr(int pi, int dir, int hi)
     return g.d_tw + (((size_t)pi * 2 + dir) * 2 + hi) * kTwSize;
 }
 
+// Pass twiddle tables (PassArgs::ptw), built on first use and kept until
+// teardown: one per (prime, direction, sub-problem log, column-stride log,
+// scaled). A strided pass then loads each element's twiddle w_M^(j m)
+// instead of forming it from the two-level tables with one more Montgomery
+// product per element. Tables are shared by every transform length whose
+// plan has a pass of the same shape. Guarded by their own mutex: the server
+// thread runs passes without the engine lock.
+static std::map<std::tuple<int, int, int, int, int>, uint64_t *> g_ptw;
+static std::mutex g_ptw_mu;
+static size_t g_ptw_bytes = 0;
+
+static cudaError_t launch_build_ptw_any(int pi, uint64_t *t, const uint64_t *hi, const uint64_t *lo, int log_m,
+                                        int log_s, int scaled, uint64_t scale, cudaStream_t st)
+{
+    switch (pi) {
+    case 0: return launch_build_pass_twiddles<0>(t, hi, lo, log_m, log_s, scaled, scale, st);
+    case 1: return launch_build_pass_twiddles<1>(t, hi, lo, log_m, log_s, scaled, scale, st);
+    case 2: return launch_build_pass_twiddles<2>(t, hi, lo, log_m, log_s, scaled, scale, st);
+    case 3: return launch_build_pass_twiddles<3>(t, hi, lo, log_m, log_s, scaled, scale, st);
+    default: return launch_build_pass_twiddles<4>(t, hi, lo, log_m, log_s, scaled, scale, st);
+    }
+}
+
+// The table of one strided pass, or nullptr (tables off, over the budget,
+// allocation failed, or a stream capture in progress: the pass then forms
+// its twiddles itself). A new table is built on st and st is synchronised
+// before the table is published, so any stream may use it afterwards.
+static const uint64_t *pass_table(int pi, int dir, int log_m, int log_s, bool scaled, uint64_t scale, cudaStream_t st)
+{
+    if (!g.pass_tables || log_s <= 0) return nullptr;
+    const auto key = std::make_tuple(pi, dir, log_m, log_s, scaled ? 1 : 0);
+    std::lock_guard<std::mutex> lk(g_ptw_mu);
+    const auto it = g_ptw.find(key);
+    if (it != g_ptw.end()) return it->second;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return nullptr;
+    const size_t bytes = ((size_t)1 << log_m) * (pi == 3 ? 4 : 8);
+    if (g_ptw_bytes + bytes > g.ptw_budget) return nullptr;
+    uint64_t *d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    const uint64_t *hi, *lo;
+    if (pi == 3) {
+        hi = (const uint64_t *)(g.d_tw3 + ((size_t)dir * 2 + 0) * kTwSize);
+        lo = (const uint64_t *)(g.d_tw3 + ((size_t)dir * 2 + 1) * kTwSize);
+    } else {
+        const int ts = pi == 4 ? 3 : pi;
+        hi = tw_ptr(ts, dir, 0);
+        lo = tw_ptr(ts, dir, 1);
+    }
+    cudaError_t e = launch_build_ptw_any(pi, d, hi, lo, log_m, log_s, scaled ? 1 : 0, scale, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { cudaFree(d); cudaGetLastError(); return nullptr; }
+    g_ptw[key] = d;
+    g_ptw_bytes += bytes;
+    return d;
+}
+
+static void free_pass_tables()
+{
+    std::lock_guard<std::mutex> lk(g_ptw_mu);
+    for (auto &kv : g_ptw) cudaFree(kv.second);
+    g_ptw.clear();
+    g_ptw_bytes = 0;
+}
+
 // Per-length plan overrides (set by gbntt_set_plan, e.g. from an autotuner):
 // [log_n][0] = pass count (0: default plan), [1..kMaxPasses] = pass sizes.
 static int g_plan_override[kMaxLog + 1][1 + kMaxPasses];
@@ -270,6 +337,7 @@ static void free_all()
     cudaFree(g.d_ctl);
     cudaFree(g.d_io);
     if (g.stream2) cudaStreamSynchronize(g.stream2);
+    free_pass_tables();
     if (g.ev_fork) cudaEventDestroy(g.ev_fork);
     if (g.ev_join) cudaEventDestroy(g.ev_join);
     if (g.cstream) cudaStreamSynchronize(g.cstream);
@@ -453,6 +521,15 @@ static int init_impl(int max_log)
         g.stage_inputs = !(si && si[0] == '0');
         const char *zc = getenv("GBNTT_ZERO_COPY");
         g.zero_copy = !(zc && zc[0] == '0');
+        // pass twiddle tables: on unless GBNTT_PASS_TABLES=0; budget
+        // GBNTT_PASS_TABLES_MB, else a quarter of the memory left after the
+        // workspace (a 2^29-point multiply needs about 12 GiB of them)
+        const char *pt = getenv("GBNTT_PASS_TABLES");
+        g.pass_tables = !(pt && pt[0] == '0');
+        const char *pb = getenv("GBNTT_PASS_TABLES_MB");
+        size_t fr = 0, tot = 0;
+        if (pb) g.ptw_budget = (size_t)std::max(0L, atol(pb)) << 20;
+        else if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) g.ptw_budget = fr / 4;
     }
     g.ready = true;
     return GBNTT_OK;
@@ -552,6 +629,7 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
             } else {
                 a.stage_out = staged ? stage : nullptr;
             }
+            a.ptw[k] = a.twiddle ? pass_table(ps.pi[k], 0, a.log_m, a.log_s, false, 0, sk) : nullptr;
             rec_begin(sk, i == 0 ? 0 : 1, pl[i], i == 0 ? (packed ? 8.0 : 4.0) * (double)n + nbw : 2.0 * nbw);
             const int ld0 = preloaded ? LD_U64 : (packed ? LD_U64LIMB : LD_U32);
             CK(launch_pass_any(ps.pi[k], pl[i], 0, i == 0 ? ld0 : LD_U64, a, sk));
@@ -600,6 +678,8 @@ static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, s
         for (int k = 0; k < ps.n; k++) {
             const double nbw = word_bytes(ps.pi[k]) * (double)((size_t)1 << L) * (double)W;
             cudaStream_t sk = (aux && k == 1) ? aux : st;
+            a.ptw[k] = a.twiddle ? pass_table(ps.pi[k], 1, a.log_m, a.log_s, a.use_scale != 0, a.scale[k], sk)
+                                 : nullptr;
             rec_begin(sk, first ? 2 : 3, pl[i], first ? (square ? 2.0 : 3.0) * nbw : 2.0 * nbw);
             CK(launch_pass_any(ps.pi[k], pl[i], 1, first ? LD_PW : LD_U64, a, sk));
             rec_end(sk);
@@ -1547,6 +1627,7 @@ int gbntt_autotune(int log_lo, int log_hi, int reps, int *plans, float *ms)
         set_err("gbntt_autotune: range [%d, %d] outside [%d, %d] or reps < 1", log_lo, log_hi, kMinLog, g.max_log);
         return GBNTT_ERR_ARG;
     }
+    if (g_srv) { set_err("gbntt_autotune: stop the server first"); return GBNTT_ERR_ARG; }
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -1592,6 +1673,12 @@ int gbntt_autotune(int log_lo, int log_hi, int reps, int *plans, float *ms)
                 t_min = std::min(t_min, t);
             }
             if (rc == GBNTT_OK && t_min < best) { best = t_min; best_plan = c; }
+            // every candidate builds tables for its own pass shapes; drop
+            // them between candidates so they stay within the budget (the
+            // server thread, which reads them without the engine lock, is
+            // not running: gbntt_autotune refuses to run beside it)
+            CK(cudaDeviceSynchronize());
+            free_pass_tables();
         }
         g_plan_override[L][0] = best_plan[0];
         for (int i = 0; i < kMaxPasses; i++) g_plan_override[L][1 + i] = best_plan[1 + i];
@@ -1613,7 +1700,10 @@ int gbntt_autotune(int log_lo, int log_hi, int reps, int *plans, float *ms)
 int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t n,
                        void *stream)
 {
-    if (prime < 0 || prime > 4 || op < 0 || op > 5) { set_err("gbntt_debug_modops: bad prime/op"); return GBNTT_ERR_ARG; }
+    if (prime < 0 || prime > 4 || op < 0 || op > 6 || (op == 6 && prime != 0)) {
+        set_err("gbntt_debug_modops: bad prime/op");
+        return GBNTT_ERR_ARG;
+    }
     cudaStream_t st = stream ? (cudaStream_t)stream : (g.ready ? g.stream : (cudaStream_t)0);
     CK(launch_modops(prime, op, d_a, d_b, d_out, (long long)n, st));
     return GBNTT_OK;
@@ -1864,9 +1954,22 @@ int gbntt_mul_u32_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t
 
 int gbntt_device_errors(unsigned int *flags)
 {
+    // the engine's sticky error word, OR the no-allocation multiply's (its
+    // own word in its static scratch) on the current device
     std::lock_guard<std::recursive_mutex> lk(g_mu);
-    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
-    return read_errors(flags);
+    unsigned na = 0;
+    int na_set_up = 0;
+    const int rc = noalloc_read_errors(&na, &na_set_up);
+    if (rc) { set_err("reading the no-allocation multiply's error word failed"); return rc; }
+    if (!g.ready) {
+        if (!na_set_up) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+        if (flags) *flags = na;
+        return GBNTT_OK;
+    }
+    unsigned v = 0;
+    const int rc2 = read_errors(&v);
+    if (flags) *flags = v | na;
+    return rc2;
 }
 
 int gbntt_debug_lookback_timeout(unsigned int *flags, double *seconds)

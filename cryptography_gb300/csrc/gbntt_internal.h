@@ -60,6 +60,11 @@ struct PassArgs {
     long long n_limbs;          // limbs beyond this index read as zero
     uint32_t *stage_out;        // first pass: also store each limb read here (a copy in HBM), or null
     TwTables tw;
+    // pass twiddle tables (per slot, or null): entry j + m S of the table of
+    // a pass over sub-problems of M = 2^log_m points is w_M^(+-j m) (times
+    // scale[] in the outermost inverse pass), indexed by the element's offset
+    // within its sub-problem; null: the pass builds w_M^(j m) from tw.hi/lo
+    const uint64_t *ptw[3];
     uint64_t scale[3];          // Montgomery constant folded into inverse twiddles
     long long ncols;            // N / L columns per prime
     int log_m;                  // log2 of the sub-problem length M
@@ -100,6 +105,12 @@ enum ErrorBits : unsigned int {
 // Launchers (gbntt_kernels.cu).
 template <int PI>
 cudaError_t launch_pass_prime(int log_l, int dir, int ld, const PassArgs &a, cudaStream_t st);
+// Fill one pass twiddle table (see PassArgs::ptw) of prime PI from the
+// two-level tables hi/lo of the wanted direction; use_scale multiplies every
+// entry by scale (the outermost inverse pass).
+template <int PI>
+cudaError_t launch_build_pass_twiddles(uint64_t *table, const uint64_t *hi, const uint64_t *lo, int log_m,
+                                       int log_s, int use_scale, uint64_t scale, cudaStream_t st);
 cudaError_t launch_garner_carry(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out);
 cudaError_t launch_garner_carry64(const CarryArgs &args, cudaStream_t stream, long long *ntiles_out);
 cudaError_t launch_garner_carry_batch(const CarryArgs &args, long long grid_tiles, cudaStream_t stream);
@@ -135,5 +146,10 @@ cudaError_t launch_modops(int prime, int op, const uint64_t *a, const uint64_t *
 
 // Message returned by gbntt_last_error (gbntt_engine.cu).
 void set_error_message(const char *msg);
+
+// Sticky error bits of the no-allocation multiply's scratch on the current
+// device, cleared on read (gbntt_noalloc.cu); *set_up = 0 when that scratch
+// was never set up on this device.
+int noalloc_read_errors(unsigned *flags, int *set_up);
 
 }  // namespace gbntt

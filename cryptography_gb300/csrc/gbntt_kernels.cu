@@ -23,7 +23,9 @@ namespace gbntt {
 // ---------------------------------------------------------------------------
 // Element-wise modular operations over device arrays (self-test of the
 // arithmetic, as the reference's test_modops.hip pins primes.h / shoup.h).
-// op: 0 add_mod, 1 sub_mod, 2 mont_mul, 3..5 the plain C++ forms.
+// op: 0 add_mod, 1 sub_mod, 2 mont_mul, 3..5 the plain C++ forms;
+// q0 only: 6 a * 2^(b mod 96) through gl_mul_pow2 (the register DFTs'
+// power-of-two twiddles; here with the exponent known only at run time).
 // ---------------------------------------------------------------------------
 template <int PI>
 __device__ __forceinline__ uint64_t modop(int op, uint64_t a, uint64_t b)
@@ -68,6 +70,10 @@ __global__ void modops_kernel(int prime, int op, const uint64_t *a, const uint64
         default: r = p3_mul_ref(u, v); break;
         }
         out[i] = r;
+        return;
+    }
+    if (prime == 0 && op == 6) {
+        out[i] = gl_mul_pow2(x, (int)(y % 96));
         return;
     }
     out[i] = prime == 0 ? modop<0>(op, x, y) : (prime == 1 ? modop<1>(op, x, y) : modop<2>(op, x, y));

@@ -19,7 +19,16 @@
 // first call should therefore come before any stream capture. All calls
 // share the one array: calls that overlap on the GPU (different streams, or
 // different host threads) race and produce wrong results; serialise them.
+// The set-up is cached per device for the life of the process: after
+// cudaDeviceReset the array comes back zeroed while the cache still says it
+// is ready, so this entry point must not be used across a device reset.
+//
+// Device checks (the Garner bound, the bounded carry look-back waits) set
+// bits in an error word inside the array that stays set across calls until
+// gbntt_device_errors reads and clears it; each call clears only the carry
+// scan's ticket and tile status words.
 #include <cuda_runtime.h>
+#include <chrono>
 #include <mutex>
 #include <stdio.h>
 #include <string.h>
@@ -29,8 +38,6 @@
 #include "gbntt.h"
 
 namespace gbntt {
-
-int plan_passes(int log_n, int *p);   // gbntt_engine.cu
 
 namespace {
 
@@ -44,8 +51,10 @@ constexpr size_t kScratchWords = kTwWords + kSpecWords + kCtlWords;
 
 }  // namespace
 
-// The scratch array (8-byte words): twiddle tables, spectra, control words.
+// The scratch array (8-byte words): twiddle tables, spectra, control words;
+// 6,390,784 bytes (about 6.4 MB) of static device memory per GPU.
 static __device__ __align__(256) uint64_t g_noalloc_scratch[kScratchWords];
+static_assert(sizeof(g_noalloc_scratch) == 6390784, "the documented scratch size (include/gbntt.h) is out of date");
 
 namespace {
 
@@ -128,6 +137,19 @@ int setup_device(int dev, uint64_t **out, char *err, size_t errlen)
     return GBNTT_OK;
 }
 
+// Fixed pass plan for the lengths this entry point takes (L <= 16): one
+// pass up to 2^10 points, otherwise two of ceil(L/2) and floor(L/2). It
+// does not read the engine's plan-override table, which gbntt_set_plan and
+// gbntt_autotune may rewrite from another thread; every plan gives the same
+// product.
+int local_plan(int L, int *p)
+{
+    if (L <= kMaxPassLog) { p[0] = L; return 1; }
+    p[0] = (L + 1) / 2;
+    p[1] = L / 2;
+    return 2;
+}
+
 cudaError_t pass_launch(int pi, int log_l, int dir, int ld, PassArgs &a, cudaStream_t st)
 {
     memcpy(a.w64, g_na_w64[pi][dir], sizeof a.w64);
@@ -178,7 +200,7 @@ extern "C" int gbntt_mul_u32_noalloc(uint32_t *d_c, const uint32_t *d_a, size_t 
     PassArgs a;
     memset(&a, 0, sizeof a);
     int pl[kMaxPasses];
-    const int np = plan_passes(L, pl);
+    const int np = local_plan(L, pl);
     const bool square = (d_a == d_b && na == nb);
     // forward transforms of both operands
     for (int op = 0; op < (square ? 1 : 2); op++) {
@@ -227,7 +249,8 @@ extern "C" int gbntt_mul_u32_noalloc(uint32_t *d_c, const uint32_t *d_a, size_t 
                 if (pass_launch(pi, pl[i], 1, i == np - 1 ? LD_PW : LD_U64, a, st) != cudaSuccess) return GBNTT_ERR_CUDA;
         }
     }
-    // Garner + carry; the ticket and the tile status words must start at zero
+    // Garner + carry; the ticket and the tile status words must start at
+    // zero; the error word ctl[1] is left as it is (sticky until read)
     CarryArgs c;
     memset(&c, 0, sizeof c);
     for (int pi = 0; pi < 3; pi++) c.res[pi] = specA + pi * stride;
@@ -239,7 +262,88 @@ extern "C" int gbntt_mul_u32_noalloc(uint32_t *d_c, const uint32_t *d_a, size_t 
     c.status = ctl + 2;
     for (int i = 0; i < 3; i++) c.garner[i] = g_na_garner[i];
     const long long nt = carry_tiles((long long)n_out);
-    if (cudaMemsetAsync(ctl, 0, (2 + (size_t)nt) * sizeof(unsigned), st) != cudaSuccess) return GBNTT_ERR_CUDA;
+    if (cudaMemsetAsync(ctl, 0, sizeof(unsigned), st) != cudaSuccess) return GBNTT_ERR_CUDA;
+    if (cudaMemsetAsync(ctl + 2, 0, (size_t)nt * sizeof(unsigned), st) != cudaSuccess) return GBNTT_ERR_CUDA;
     if (launch_garner_carry(c, st, nullptr) != cudaSuccess) return GBNTT_ERR_CUDA;
     return GBNTT_OK;
+}
+
+namespace gbntt {
+
+// Error bits the no-allocation multiply's device checks left on the current
+// device (0 when it was never set up there; *set_up says which), cleared on
+// read. Synchronises the device. Called by gbntt_device_errors.
+int noalloc_read_errors(unsigned *flags, int *set_up)
+{
+    *flags = 0;
+    *set_up = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GBNTT_ERR_CUDA;
+    uint64_t *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_na_mu);
+        if (dev >= 0 && dev < kMaxDevices) base = g_na_ptr[dev];
+    }
+    if (!base) return GBNTT_OK;
+    *set_up = 1;
+    unsigned *err = (unsigned *)(base + kTwWords + kSpecWords) + 1;
+    if (cudaDeviceSynchronize() != cudaSuccess) return GBNTT_ERR_CUDA;
+    if (cudaMemcpy(flags, err, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) return GBNTT_ERR_CUDA;
+    if (cudaMemset(err, 0, sizeof(unsigned)) != cudaSuccess) return GBNTT_ERR_CUDA;
+    return GBNTT_OK;
+}
+
+// Test hook for the bounded waits in this entry point's scratch: the carry
+// kernel over three tiles with the ticket started at 1, so no CTA takes
+// tile 0 and tile 1's look-back waits on a status word nothing writes. The
+// wait runs out by itself and sets ERR_LOOKBACK_TIMEOUT in the scratch's
+// error word (read back by gbntt_device_errors). Sets the scratch up first
+// if needed. Synchronises.
+int noalloc_debug_lookback_timeout(double *seconds)
+{
+    static char err[256];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GBNTT_ERR_CUDA;
+    uint64_t *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_na_mu);
+        const int rc = setup_device(dev, &base, err, sizeof err);
+        if (rc) return rc;
+    }
+    long long n_out = 1;
+    while (carry_tiles(n_out) < 3) n_out *= 2;   // smallest power of two spanning three carry tiles
+    if ((size_t)n_out > kNoAllocMaxN) return GBNTT_ERR_SIZE;
+    uint64_t *specA = base + kTwWords;
+    unsigned *ctl = (unsigned *)(specA + kSpecWords);
+    CarryArgs c;
+    memset(&c, 0, sizeof c);
+    for (int pi = 0; pi < 3; pi++) c.res[pi] = specA + pi * kNoAllocMaxN;
+    // output into operand B's spectrum area (scratch the check may overwrite)
+    c.out = (uint32_t *)(specA + 3 * kNoAllocMaxN);
+    c.n_coef = n_out;
+    c.n_out = n_out;
+    c.ticket = ctl;
+    c.error = ctl + 1;
+    c.status = ctl + 2;
+    for (int i = 0; i < 3; i++) c.garner[i] = g_na_garner[i];
+    const unsigned start = 1u;
+    if (cudaDeviceSynchronize() != cudaSuccess) return GBNTT_ERR_CUDA;
+    if (cudaMemset(ctl + 2, 0, 8 * sizeof(unsigned)) != cudaSuccess) return GBNTT_ERR_CUDA;
+    if (cudaMemcpy(ctl, &start, sizeof start, cudaMemcpyHostToDevice) != cudaSuccess) return GBNTT_ERR_CUDA;
+    const auto t0 = std::chrono::steady_clock::now();
+    if (launch_garner_carry(c, nullptr, nullptr) != cudaSuccess) return GBNTT_ERR_CUDA;
+    if (cudaDeviceSynchronize() != cudaSuccess) return GBNTT_ERR_CUDA;
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return GBNTT_OK;
+}
+
+}  // namespace gbntt
+
+// Test hook (no counterpart in the reference): makes one carry look-back wait
+// in the no-allocation multiply's scratch run out (see
+// noalloc_debug_lookback_timeout) and reports the time it took; the error
+// bit is then read with gbntt_device_errors.
+extern "C" int gbntt_debug_noalloc_lookback_timeout(double *seconds)
+{
+    return gbntt::noalloc_debug_lookback_timeout(seconds);
 }

@@ -1,6 +1,6 @@
 // gbntt_pass.cuh — one NTT pass of 2^l points (l = 5..10) for one prime.
 //
-// The transform of N = 2^L points is a chain of 1-3 passes (outermost
+// The transform of N = 2^L points is a chain of 1-4 passes (outermost
 // first). Pass i owns sub-problems of M_i points; inside each, element
 // (j, m) sits at j + S_i m (column j < S_i, row m < 2^l, S_i = M_i / 2^l).
 // A forward (decimation-in-frequency) pass computes, for every column, the
@@ -333,7 +333,15 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
             const int g = t & (G - 1), m0 = t >> LOG_G;
             const uint64_t j = j0 + (uint64_t)g;
             V *dst = sm + g * RS + m0;
-            if (a.twiddle) {
+            const V *ptw = (const V *)a.ptw[F::SLOT];
+            if (a.twiddle && ptw) {
+                // table entry j + m S (the scale already folded in)
+                const long long S = 1LL << log_s;
+                const V *tp = ptw + (long long)j + (long long)m0 * S;
+                const long long stepg = (long long)B * S;
+#pragma unroll 4
+                for (int it = 0; it < A; it++) dst[it * (B + 1)] = F::mul(dst[it * (B + 1)], __ldg(tp + it * stepg));
+            } else if (a.twiddle) {
                 V tw = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)m0 * j) << sh));
                 const V step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * j) << sh));
                 if (a.use_scale) tw = F::mul(tw, (V)a.scale[F::SLOT]);
@@ -466,7 +474,14 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
         const long long stepg = (long long)B * S;
         const V *src = sm + g * RS + m0;
-        if (DIR == 0 && a.twiddle) {
+        const V *ptw = (const V *)a.ptw[F::SLOT];
+        if (DIR == 0 && a.twiddle && ptw) {
+            // forward pass, twiddle w_M^(j k) from the pass table (entry
+            // j + k S, the element's offset within its sub-problem)
+            const V *tp = ptw + (long long)(j0 + (uint64_t)g) + (long long)m0 * S;
+#pragma unroll 4
+            for (int it = 0; it < A; it++) data[base + it * stepg] = F::mul(src[it * (B + 1)], __ldg(tp + it * stepg));
+        } else if (DIR == 0 && a.twiddle) {
             // forward pass: output k = m0 + it B of column j gets w_M^(j k),
             // applied here (a partly rolled loop) instead of in the
             // unrolled register step
@@ -600,6 +615,36 @@ static cudaError_t launch_pass_l(int dir, int ld, const PassArgs &a, cudaStream_
     if (!fn) return cudaErrorInvalidValue;
     const long long gx = (a.ncols + S_::G - 1) / S_::G;
     fn<<<(unsigned)gx, kPassThreads, S_::SMEM, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Pass twiddle table: entry e = j + m S (m < 2^(log_m - log_s), j < S) is
+// w_M^(j m) from the two-level tables of the wanted direction, times scale
+// when use_scale is set.
+template <int PI>
+__global__ void build_pass_twiddles_kernel(typename Field<PI>::T *table, const typename Field<PI>::T *hi,
+                                           const typename Field<PI>::T *lo, int log_m, int log_s, int use_scale,
+                                           typename Field<PI>::T scale)
+{
+    const long long M = 1LL << log_m;
+    const int sh = kMaxLog - log_m;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < M; e += (long long)gridDim.x * blockDim.x) {
+        const uint64_t m = (uint64_t)e >> log_s, j = (uint64_t)e & ((1ull << log_s) - 1);
+        typename Field<PI>::T w = tw_exp<PI>(hi, lo, (uint32_t)((m * j) << sh));
+        if (use_scale) w = Field<PI>::mul(w, scale);
+        table[e] = w;
+    }
+}
+
+template <int PI>
+cudaError_t launch_build_pass_twiddles(uint64_t *table, const uint64_t *hi, const uint64_t *lo, int log_m, int log_s,
+                                       int use_scale, uint64_t scale, cudaStream_t st)
+{
+    using V = typename Field<PI>::T;
+    const long long M = 1LL << log_m;
+    const long long grid = std::min<long long>((M + 255) / 256, 152 * 16);
+    build_pass_twiddles_kernel<PI><<<(unsigned)grid, 256, 0, st>>>((V *)table, (const V *)hi, (const V *)lo, log_m,
+                                                                   log_s, use_scale, (V)scale);
     return cudaGetLastError();
 }
 

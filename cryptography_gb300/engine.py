@@ -47,7 +47,7 @@ EXPORTS = (
     "gbntt_split_terms_needed", "gbntt_e_required_log", "gbntt_binary_split", "gbntt_newton_reciprocal_u32",
     "gbntt_div_newton_u32", "gbntt_pow10_u32", "gbntt_to_decimal_u32", "gbntt_compute_e",
     "gbntt_set_prime_set", "gbntt_prime_set", "gbntt_debug_lookback_timeout", "gbntt_autotune",
-    "gbntt_wave_graphs", "gbntt_negacyclic_mul_u64",
+    "gbntt_wave_graphs", "gbntt_negacyclic_mul_u64", "gbntt_debug_noalloc_lookback_timeout",
 )
 
 _lib = None
@@ -131,6 +131,8 @@ def lib():
     L.gbntt_batch_mul_u32.restype = ctypes.c_int
     L.gbntt_mul_u32_noalloc.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp]
     L.gbntt_mul_u32_noalloc.restype = ctypes.c_int
+    L.gbntt_debug_noalloc_lookback_timeout.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    L.gbntt_debug_noalloc_lookback_timeout.restype = ctypes.c_int
     L.gbntt_set_plan.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.gbntt_set_plan.restype = ctypes.c_int
     L.gbntt_launch_log.argtypes = [ctypes.c_int]

@@ -33,3 +33,13 @@ def operand(n, seed, chunk=1 << 24):
     if n:
         out[n - 1] |= np.uint32(1 << 31)
     return out
+
+
+def batched_sizes(pairs, seed, lo=10, hi=22):
+    """Operand sizes of a batch of uneven products: log2(n) uniform in
+    [lo, hi) per operand, drawn independently for the two operands of every
+    pair from a seeded generator (limb counts, int64 arrays)."""
+    rng = np.random.default_rng(seed)
+    na = np.floor(2.0 ** rng.uniform(lo, hi, pairs)).astype(np.int64)
+    nb = np.floor(2.0 ** rng.uniform(lo, hi, pairs)).astype(np.int64)
+    return na, nb

@@ -207,7 +207,11 @@ int gbntt_coeff_bits(void);
 int gbntt_mul_u32_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b, size_t nb);
 
 /* Synchronise the engine stream, return and clear the device error bits
- * (1 = Garner digit check, 2 = look-back wait gave up). */
+ * (1 = Garner digit check, 2 = look-back wait gave up). The bits of
+ * gbntt_mul_u32_noalloc on the current device (a separate sticky word in
+ * its static scratch) are ORed in and cleared too; without an initialised
+ * engine only those are returned (GBNTT_ERR_NOT_INIT when neither the
+ * engine nor the no-allocation multiply was set up). */
 int gbntt_device_errors(unsigned int *flags);
 
 /* Forward spectra of a limb vector for each prime (3 x 2^log_n uint64, in
@@ -232,7 +236,8 @@ int gbntt_debug_lookback_timeout(unsigned int *flags, double *seconds);
  * word, op 2 = a*b*2^-32 mod p3 (a may be any 32-bit value for op 2 and 5).
  * Prime index 4 is q0 in lazy normal form: any 64-bit operands, op 2 =
  * a*b mod q0, results in [0, 2^64) congruent mod q0 (canonical for 3..5).
- * Stream-ordered. */
+ * Prime index 0 also takes op 6: a * 2^(b mod 96) mod q0, the register
+ * DFTs' power-of-two multiply (a canonical). Stream-ordered. */
 int gbntt_debug_modops(int prime, int op, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t n,
                        void *stream);
 
@@ -257,14 +262,24 @@ int gbntt_launch_records(int *kind, int *log_l, double *bytes, float *ms, int ma
  * forbids cudaMalloc/cudaFree, latency-critical loops where cudaMalloc would
  * synchronise the device, or code that has no engine initialised).
  * d_c[0 .. na+nb) = d_a * d_b for na + nb - 1 <= 2^16 (GBNTT_ERR_SIZE above
- * that); needs no gbntt_init. All scratch (about 4.6 MB) is one static
- * device array that every GPU loading this library keeps until exit. The
- * first call on each device (with that device current) sets the array up
- * with cudaGetSymbolAddress and cudaMemcpy, so make that first call before
- * any stream capture. Calls share the array: calls that overlap on the GPU
- * race; serialise them (one stream, one thread at a time). Stream-ordered. */
+ * that); needs no gbntt_init. All scratch (6,390,784 bytes, about 6.4 MB)
+ * is one static device array that every GPU loading this library keeps
+ * until exit. The first call on each device (with that device current)
+ * sets the array up with cudaGetSymbolAddress and cudaMemcpy, so make that
+ * first call before any stream capture; do not use it across a
+ * cudaDeviceReset (the array comes back zeroed, the set-up is not redone).
+ * Calls share the array: calls that overlap on the GPU race; serialise them
+ * (one stream, one thread at a time). Stream-ordered. Device check failures
+ * (Garner bound, look-back wait limit) set a sticky error word in the
+ * scratch that gbntt_device_errors reads and clears. */
 int gbntt_mul_u32_noalloc(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb,
                           void *stream);
+
+/* Test hook (no counterpart in the reference): one carry look-back wait in
+ * gbntt_mul_u32_noalloc's scratch waits on a status word nothing writes and
+ * runs out by itself; the error bit 2 is then reported by
+ * gbntt_device_errors. Synchronises the device. */
+int gbntt_debug_noalloc_lookback_timeout(double *seconds);
 
 /* ---- e pipeline and the arith layer above the multiply ----
  * Host operands and results, 32-bit limbs little-endian; every product runs

@@ -53,6 +53,8 @@ def lib():
         L.oracle_mod_u32_par.argtypes = [_u32p, ctypes.c_long, ctypes.c_uint64]
         L.oracle_gmp_available.restype = ctypes.c_int
         L.oracle_num_threads.restype = ctypes.c_int
+        L.oracle_set_threads.restype = None
+        L.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
 
@@ -177,6 +179,11 @@ def from_int(v, n=None):
 
 def num_threads():
     return int(lib().oracle_num_threads())
+
+
+def set_threads(n):
+    """OpenMP thread count of the oracle's parallel regions from now on."""
+    lib().oracle_set_threads(int(n))
 
 
 def negacyclic_mul(f, g):

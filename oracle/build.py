@@ -15,7 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libref.so")
-REFERENCE_ROOT = os.environ.get("GBNTT_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: GBNTT_REFERENCE_ROOT, else a directory named
+# "reference" beside this repository's root (absent on machines without it).
+REFERENCE_ROOT = os.environ.get("GBNTT_REFERENCE_ROOT") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def _stale(target, sources):

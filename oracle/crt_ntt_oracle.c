@@ -364,3 +364,14 @@ int oracle_num_threads(void)
     return 1;
 #endif
 }
+
+/* Thread count of the OpenMP regions that follow (the CPU-baseline timing
+ * runs the port on all cores but one while GMP uses the last). */
+void oracle_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}

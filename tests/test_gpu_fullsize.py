@@ -1,6 +1,10 @@
-"""Full-size product (two 2^28-limb operands, transform length 2^29): too
-large for the oracle or GMP within a test budget, so it is checked through
-size-independent properties:
+"""Full-size product (two 2^28-limb operands, transform length 2^29).
+
+The multiply of the benchmark's operands (seeds 1 and 2) is compared limb
+for limb with GMP mpz_mul of the same operands (about two minutes of one
+host core, run in a thread while the GPU works), the shape of the
+reference's oracle test (ntt/app/compute_e/test_gmp_oracle.c:70-76). Every
+full-size product is also checked through size-independent properties:
   * the device Garner check reports no error (two primes: every
     coefficient below N 2^64; three primes: the third mixed-radix digit
     is 0);
@@ -9,8 +13,11 @@ size-independent properties:
   * the low 2^20 limbs equal the low limbs of the GMP product of the low
     2^20 limbs of each operand (exact, limb for limb);
   * the limb count is exactly 2 n (both top bits set);
-  * squaring satisfies the same checks.
+  * squaring and the packed (64-bit coefficient) form satisfy the same
+    checks.
 """
+import threading
+
 import numpy as np
 import pytest
 
@@ -47,13 +54,24 @@ def _check_product(a, b, c):
 
 
 @pytest.mark.gpu
-def test_full_size_multiply(big_engine):
+@pytest.mark.slow
+def test_full_size_multiply_every_limb_vs_gmp(big_engine):
+    if not oracle.gmp_available():
+        pytest.skip("libgmp.so.10 not available")
     n = 1 << 28
     a = synth.operand(n, 1)
     b = synth.operand(n, 2)
+    ref = {}
+    t = threading.Thread(target=lambda: ref.setdefault("c", oracle.gmp_mul(a, b)))
+    t.start()                         # GMP on one host core while the GPU multiplies
     c = big_engine.mul(a, b)          # host path: raises on any device error flag
     _check_product(a, b, c)
     assert big_engine.device_errors() == 0
+    t.join()
+    want = ref["c"]
+    assert len(want) == 2 * n
+    diff = np.flatnonzero(c != want)
+    assert diff.size == 0, "first differing limb %d of %d" % (int(diff[0]), diff.size)
 
 
 @pytest.mark.gpu

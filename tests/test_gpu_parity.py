@@ -274,6 +274,31 @@ def test_device_modops(engine, prime):
         buf.free()
 
 
+def test_device_pow2_q0(engine):
+    # x * 2^e mod q0 (every e < 96) as the register DFTs multiply by powers
+    # of two: the per-range forms against Python integers, corners included
+    p = oracle.PRIMES[0]
+    rng = np.random.default_rng(45)
+    corners = [0, 1, 2, p - 1, p - 2, (1 << 32) - 1, 1 << 32, (1 << 63) - 1, 1 << 63, p - (1 << 32),
+               (1 << 64) - (1 << 33), 0xFFFFFFFE00000001, 0x00000000FFFFFFFF, 0x80000000FFFFFFFF]
+    per_e = 700
+    xs = [c for c in corners] + [int(v) % p for v in rng.integers(0, 1 << 64, per_e - len(corners), dtype=np.uint64)]
+    a = np.array(xs * 96, dtype=np.uint64)
+    e = np.repeat(np.arange(96, dtype=np.uint64), per_e)
+    n = len(a)
+    da, de, dout = (cudart.DeviceBuffer(8 * n) for _ in range(3))
+    da.upload(a)
+    de.upload(e)
+    assert engine.lib().gbntt_debug_modops(0, 6, da.ptr, de.ptr, dout.ptr, n, None) == 0
+    cudart.stream_sync(engine.lib().gbntt_stream())
+    got = [int(v) for v in dout.download(np.uint64, n)]
+    want = [int(x) * pow(2, int(k), p) % p for x, k in zip(a, e)]
+    bad = [i for i in range(n) if got[i] != want[i]]
+    assert not bad, [(hex(int(a[i])), int(e[i]), hex(got[i]), hex(want[i])) for i in bad[:5]]
+    for buf in (da, de, dout):
+        buf.free()
+
+
 def test_device_modops_lazy_q0(engine):
     # q0 in lazy normal form: operands are any 64-bit words (standing for
     # their value mod q0), results lie in [0, 2^64) and must agree mod q0

@@ -1,11 +1,13 @@
 """Serving loop (continuous batching): requests of mixed sizes submitted
 while others are running must each produce exactly the product computed
-alone (tolerance 0), oversized requests are refused, stop() drains."""
+alone (tolerance 0) and the GMP product, oversized requests are refused,
+stop() drains."""
 import time
 
 import numpy as np
 import pytest
 
+import oracle
 from cryptography_gb300 import cudart
 
 pytestmark = pytest.mark.gpu
@@ -36,7 +38,9 @@ def test_serving_mix_equals_alone(engine):
             state, lat = srv.query(t)
             assert state == 2 and lat > 0
             got = dc.download(np.uint32, len(a) + len(b))
-            assert np.array_equal(got, engine.mul(a, b)), t
+            assert np.array_equal(got, engine.mul(a, b)), t      # the same product computed alone
+            want = oracle.gmp_mul(a, b) if oracle.gmp_available() else oracle.mul(a, b)
+            assert np.array_equal(got[:len(want)], want) and not got[len(want):].any(), t
         with pytest.raises(engine.EngineError) as ei:
             big = cudart.DeviceBuffer(8)
             srv.submit(big.ptr, big.ptr, 1 << 20, big.ptr, 1 << 20)
