@@ -163,6 +163,29 @@ __device__ __forceinline__ void cp_async_wait_all()
 {
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;\n" ::: "memory");
 }
+// 4-byte asynchronous copy that reads src_bytes (4 or 0) from gmem and
+// zero-fills the rest
+__device__ __forceinline__ void cp_async_u32_zfill(void *smem, const void *gmem, int src_bytes)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
+}
+
+#ifndef GBNTT_PASS_LIMB_ASYNC
+#define GBNTT_PASS_LIMB_ASYNC 1   // first forward pass: limbs go to the tile through cp.async (all in flight)
+#endif
+
+// Tile word as the first DFT step reads it. In a first forward pass (LD_U32)
+// the slot holds a 32-bit limb in its low word (the rest of an 8-byte slot
+// is not written), reduced here: the limb itself for a 64-bit prime, one
+// conditional subtract for p3. A slot that already holds the reduced value
+// reads the same.
+template <int PI, int LD>
+__device__ __forceinline__ typename Field<PI>::T tile_in(const typename Field<PI>::T *p)
+{
+    if constexpr (LD == LD_U32) return Field<PI>::from_u32(*(const uint32_t *)p);
+    else return *p;
+}
 
 // value of tile element at address addr for the load kind LD
 template <int PI, int LD>
@@ -253,12 +276,31 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
         const long long stepg = (long long)B * S;
         V *dst = sm + g * RS + m0;
-        if constexpr (sizeof(V) == 4) {   // all A loads in flight (registers allow it)
+        bool loaded = false;
+        if constexpr (LD == LD_U32 && GBNTT_PASS_LIMB_ASYNC) {
+            if (!a.limb_tab) {
+                // one operand's limbs: every copy of the thread in flight at
+                // once, zero-filled beyond the operand (the slot's low word;
+                // tile_in reduces it when step 1 reads it)
+                const uint32_t *limbs = a.limbs;
 #pragma unroll
-            for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
-        } else {
+                for (int it = 0; it < A; it++) {
+                    const long long addr = base + it * stepg;
+                    const bool in = addr < a.n_limbs;
+                    cp_async_u32_zfill(dst + it * (B + 1), limbs + (in ? addr : 0), in ? 4 : 0);
+                }
+                cp_async_wait_all();
+                loaded = true;
+            }
+        }
+        if (!loaded) {
+            if constexpr (sizeof(V) == 4) {   // all A loads in flight (registers allow it)
+#pragma unroll
+                for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
+            } else {
 #pragma unroll 8
-            for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
+                for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
+            }
         }
         if constexpr (LD == LD_U32 && sizeof(V) == 8) {
             // staged first pass (64-bit prime, whose residue of a limb is
@@ -381,8 +423,13 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
             V x[A];
             const int rbase = g * RS + (phase == 0 ? lane : lane * (B + 1));
             const int rstride = phase == 0 ? (B + 1) : 1;
+            if (phase == 0) {
 #pragma unroll
-            for (int i = 0; i < A; i++) x[i] = sm[rbase + i * rstride];
+                for (int i = 0; i < A; i++) x[i] = tile_in<PI, LD>(&sm[rbase + i * rstride]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < A; i++) x[i] = sm[rbase + i * rstride];
+            }
             dft_reg<PI, S_::LOG_A, DIR>(x, w64);
             if (phase == 0) {
                 if (lane > 0) {   // w_L^(lane ka)
@@ -404,7 +451,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         const int g = t >> LOG_B, b = t & (B - 1);
         V x[A];
 #pragma unroll
-        for (int i = 0; i < A; i++) x[i] = sm[g * RS + i * (B + 1) + b];
+        for (int i = 0; i < A; i++) x[i] = tile_in<PI, LD>(&sm[g * RS + i * (B + 1) + b]);
         dft_reg<PI, S_::LOG_A, DIR>(x, w64);
 #pragma unroll
         for (int ka = 0; ka < A; ka++) {
