@@ -34,7 +34,7 @@ def _flags():
         extra.append("-DGBNTT_PASS_MIN_BLOCKS=%d" % int(os.environ["GBNTT_PASS_MIN_BLOCKS"]))
     if os.environ.get("GBNTT_PASS_SHARED_DFT"):
         extra.append("-DGBNTT_PASS_SHARED_DFT=%d" % int(os.environ["GBNTT_PASS_SHARED_DFT"]))
-    for knob in ("GBNTT_PASS_PIPE32", "GBNTT_PASS_PIPE64", "GBNTT_PASS_PW_ASYNC", "GBNTT_Q0_ALU", "GBNTT_P3_ALU", "GBNTT_CARRY_MIN_BLOCKS", "GBNTT_PASS_MIN_BLOCKS_SMALL", "GBNTT_Q0_POW2",
+    for knob in ("GBNTT_PASS_PIPE32", "GBNTT_PASS_PIPE64", "GBNTT_PASS_PW_ASYNC", "GBNTT_Q0_ALU", "GBNTT_P3_ALU", "GBNTT_CARRY_MIN_BLOCKS", "GBNTT_PASS_MIN_BLOCKS_SMALL", "GBNTT_Q0_POW2", "GBNTT_FUSED_MIN_BLOCKS",
                  "GBNTT_PASS_LIMB_ASYNC"):
         if os.environ.get(knob):
             extra.append("-D%s=%d" % (knob, int(os.environ[knob])))

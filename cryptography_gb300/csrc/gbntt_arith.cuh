@@ -682,6 +682,9 @@ __device__ __forceinline__ uint64_t gl_mul_ref(uint64_t a, uint64_t b)
 // 0..2 are the 64-bit Montgomery primes above (slots 0..2); prime 3 is p3
 // and prime 4 is lazy normal-form q0 (slots 1 and 0 of the two-prime set).
 // ---------------------------------------------------------------------------
+// Beside add/sub/mul every policy converts from a 32-bit limb (from_u32)
+// and from the 64-bit form host code uses (from_u64), gives zero() and the
+// low 32 bits of a residue (low32).
 template <int PI>
 struct Field {
     typedef uint64_t T;
@@ -691,7 +694,11 @@ struct Field {
     static __device__ __forceinline__ T sub(T a, T b) { return sub_mod<PI>(a, b); }
     static __device__ __forceinline__ T mul(T a, T b) { return mont_mul<PI>(a, b); }
     static __device__ __forceinline__ T from_u32(uint32_t v) { return v; }   // v < 2^32 < p
+    static __device__ __forceinline__ T from_u64(uint64_t v) { return v; }
+    static __device__ __forceinline__ T zero() { return 0; }
+    static __device__ __forceinline__ uint32_t low32(T v) { return (uint32_t)v; }
 };
+
 template <>
 struct Field<3> {
     typedef uint32_t T;
@@ -701,6 +708,9 @@ struct Field<3> {
     static __device__ __forceinline__ T sub(T a, T b) { return p3_sub(a, b); }
     static __device__ __forceinline__ T mul(T a, T b) { return p3_mul(a, b); }
     static __device__ __forceinline__ T from_u32(uint32_t v) { return v >= kP3 ? v - kP3 : v; }   // 2^32 < 2 p3
+    static __device__ __forceinline__ T from_u64(uint64_t v) { return (uint32_t)v; }
+    static __device__ __forceinline__ T zero() { return 0; }
+    static __device__ __forceinline__ uint32_t low32(T v) { return v; }
 };
 
 // Prime 4 is q0 again, in normal form with lazy residues (slot 0 of the
@@ -714,6 +724,9 @@ struct Field<4> {
     static __device__ __forceinline__ T sub(T a, T b) { return gl_sub(a, b); }
     static __device__ __forceinline__ T mul(T a, T b) { return gl_mul(a, b); }
     static __device__ __forceinline__ T from_u32(uint32_t v) { return v; }
+    static __device__ __forceinline__ T from_u64(uint64_t v) { return v; }
+    static __device__ __forceinline__ T zero() { return 0; }
+    static __device__ __forceinline__ uint32_t low32(T v) { return (uint32_t)v; }
 };
 
 // Runtime prime dispatch helpers used by host-side tables.

@@ -79,6 +79,7 @@ struct Engine {
     bool zero_copy = true;          // host-pointer calls: kernels read/write pinned host memory directly
     bool stage_inputs = true;       // ... except the operands, copied once to HBM (B's copy overlaps A's transform)
     bool graphs = true;             // batched waves replayed as CUDA graphs
+    bool fuse_inner = true;         // innermost forward passes, pointwise product and innermost inverse pass in one launch
     bool pass_tables = true;        // strided passes read their twiddles from pass tables (PassArgs::ptw)
     size_t ptw_budget = 0;          // ... up to this many bytes of tables in all
     bool batch_split = true;        // uneven batch products split into chunk products
@@ -264,18 +265,20 @@ int plan_passes(int log_n, int *p)
         return np;
     }
     if (log_n <= kMaxPassLog) { p[0] = log_n; return 1; }
-    // 2^18 .. 2^30: the plans gbntt_autotune measured fastest on GB300 for
-    // 2^(L-1) x 2^(L-1)-limb products (two-prime set). Passes of 2^6 to 2^8
-    // points beat 2^9 and 2^10 even at the cost of a fourth pass: their
-    // register DFTs are shorter (fewer registers, a smaller loop body), and
-    // the extra sweep over HBM is cheap next to the integer work (2^29:
-    // [7, 7, 8, 7] 58.8 ms, [9, 10, 10] about 67 ms).
-    constexpr int kTunedLo = 18;
+    // 2^14 .. 2^30: the plans gbntt_autotune measured fastest on GB300 for
+    // 2^(L-1) x 2^(L-1)-limb products (two-prime set, innermost passes
+    // fused). Passes of 2^6 to 2^8 points beat 2^9 and 2^10 even at the cost
+    // of a fourth pass: their register DFTs are shorter (fewer registers, a
+    // smaller loop body), and the extra sweep over HBM is cheap next to the
+    // integer work. With the innermost passes fused a larger innermost pass
+    // pays (2^29: [7, 7, 7, 8] 51.8 ms, [7, 7, 8, 7] 53.3 ms).
+    constexpr int kTunedLo = 14;
     static const signed char kTuned[kMaxLog + 1 - kTunedLo][1 + kMaxPasses] = {
-        {3, 6, 6, 6},    {3, 6, 7, 6},    {3, 6, 6, 8},    {3, 5, 8, 8},     // 2^18 .. 2^21
-        {3, 6, 8, 8},    {3, 8, 8, 7},    {3, 8, 8, 8},    {3, 8, 8, 9},     // 2^22 .. 2^25
-        {3, 8, 8, 10},   {4, 6, 7, 7, 7}, {4, 7, 7, 7, 7}, {4, 7, 7, 8, 7},  // 2^26 .. 2^29
-        {4, 7, 8, 8, 7},                                                    // 2^30
+        {2, 6, 8},       {2, 7, 8},       {2, 8, 8},       {3, 5, 6, 6},     // 2^14 .. 2^17
+        {3, 6, 6, 6},    {3, 5, 6, 8},    {3, 6, 6, 8},    {3, 6, 7, 8},     // 2^18 .. 2^21
+        {3, 7, 7, 8},    {3, 7, 8, 8},    {3, 8, 8, 8},    {3, 8, 9, 8},     // 2^22 .. 2^25
+        {4, 7, 7, 6, 6}, {4, 7, 7, 7, 6}, {4, 7, 8, 7, 6}, {4, 7, 7, 7, 8},  // 2^26 .. 2^29
+        {4, 7, 7, 8, 8},                                                    // 2^30
     };
     if (log_n >= kTunedLo && log_n <= kMaxLog) {
         const signed char *t = kTuned[log_n - kTunedLo];
@@ -524,6 +527,8 @@ static int init_impl(int max_log)
         // pass twiddle tables: on unless GBNTT_PASS_TABLES=0; budget
         // GBNTT_PASS_TABLES_MB, else a quarter of the memory left after the
         // workspace (a 2^29-point multiply needs about 12 GiB of them)
+        const char *fi = getenv("GBNTT_FUSE_INNER");
+        g.fuse_inner = !(fi && fi[0] == '0');
         const char *pt = getenv("GBNTT_PASS_TABLES");
         g.pass_tables = !(pt && pt[0] == '0');
         const char *pb = getenv("GBNTT_PASS_TABLES_MB");
@@ -592,13 +597,14 @@ static int join_aux(cudaStream_t st, cudaStream_t aux)
 static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void *limbs, size_t n, int L,
                    cudaStream_t st, bool packed = false, long long W = 1, const uint32_t *const *limb_tab = nullptr,
                    const long long *len_tab = nullptr, cudaStream_t aux = nullptr, uint32_t *stage = nullptr,
-                   bool preloaded = false, cudaEvent_t after_first = nullptr)
+                   bool preloaded = false, cudaEvent_t after_first = nullptr, bool skip_last = false)
 {
     // after_first (optional): recorded on st once the first pass of the
     // first prime is enqueued (the operand's limbs have then been read)
     // preloaded: spec already holds the residues (the first pass reads them)
+    // skip_last: leave the innermost pass to the fused kernel (inner_fused)
     int pl[kMaxPasses];
-    const int np = plan_passes(L, pl);
+    const int np = plan_passes(L, pl) - (skip_last ? 1 : 0);
     PassArgs a;
     memset(&a, 0, sizeof a);
     for (int k = 0; k < ps.n; k++) a.data[k] = spec + k * stride;
@@ -646,8 +652,11 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
 // shared_b: specB holds one spectrum (2^L points) that every product of
 // the wave multiplies by.
 static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, size_t stride, int L,
-                   cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr, bool shared_b = false)
+                   cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr, bool shared_b = false,
+                   bool skip_first = false)
 {
+    // skip_first: the pointwise product and the innermost inverse pass were
+    // done by the fused kernel (inner_fused); start at the next pass
     int pl[kMaxPasses];
     const int np = plan_passes(L, pl);
     PassArgs a;
@@ -668,13 +677,13 @@ static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, s
     int log_ms[kMaxPasses];
     int log_m = L;
     for (int i = 0; i < np; i++) { log_ms[i] = log_m; log_m -= pl[i]; }
-    for (int i = np - 1; i >= 0; i--) {
+    for (int i = np - 1 - (skip_first ? 1 : 0); i >= 0; i--) {
         a.log_m = log_ms[i];
         a.log_s = log_ms[i] - pl[i];
         a.ncols = W << (L - pl[i]);
         a.twiddle = a.log_s > 0;
         a.use_scale = (i == 0);
-        const bool first = (i == np - 1);
+        const bool first = (i == np - 1);   // the pointwise pass
         for (int k = 0; k < ps.n; k++) {
             const double nbw = word_bytes(ps.pi[k]) * (double)((size_t)1 << L) * (double)W;
             cudaStream_t sk = (aux && k == 1) ? aux : st;
@@ -684,6 +693,57 @@ static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, s
             CK(launch_pass_any(ps.pi[k], pl[i], 1, first ? LD_PW : LD_U64, a, sk));
             rec_end(sk);
         }
+    }
+    return GBNTT_OK;
+}
+
+// Whether a product of transform length 2^L runs its innermost passes
+// fused (plans of two or more passes; off with GBNTT_FUSE_INNER=0).
+static bool fuse_inner(int L)
+{
+    int pl[kMaxPasses];
+    return g.fuse_inner && plan_passes(L, pl) >= 2;
+}
+
+// The innermost forward pass of specA and specB (specB == specA: a square),
+// the pointwise product and the innermost inverse pass in one launch per
+// prime, in place in specA (see ntt_inner_fused_kernel). Runs between
+// forward(..., skip_last) of both operands and inverse(..., skip_first).
+static int inner_fused(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, size_t stride, int L,
+                       cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr)
+{
+    int pl[kMaxPasses];
+    const int np = plan_passes(L, pl);
+    const int l = pl[np - 1];
+    PassArgs a;
+    memset(&a, 0, sizeof a);
+    a.tw = tables(ps, 0);
+    const TwTables ti = tables(ps, 1);
+    for (int k = 0; k < ps.n; k++) {
+        a.data[k] = specA + k * stride;
+        a.other[k] = square ? specA + k * stride : specB + k * stride;
+        a.st1_inv[k] = ti.st1[k];
+    }
+    a.log_m = l;
+    a.log_s = 0;
+    a.ncols = W << (L - l);
+    for (int k = 0; k < ps.n; k++) {
+        const int pi = ps.pi[k];
+        const double nbw = word_bytes(pi) * (double)((size_t)1 << L) * (double)W;
+        cudaStream_t sk = (aux && k == 1) ? aux : st;
+        memcpy(a.w64, g_w64[pi][0], sizeof a.w64);
+        memcpy(a.w64_inv, g_w64[pi][1], sizeof a.w64_inv);
+        rec_begin(sk, 5, l, (square ? 2.0 : 3.0) * nbw);
+        cudaError_t e;
+        switch (pi) {
+        case 0: e = launch_inner_fused_prime<0>(l, a, sk); break;
+        case 1: e = launch_inner_fused_prime<1>(l, a, sk); break;
+        case 2: e = launch_inner_fused_prime<2>(l, a, sk); break;
+        case 3: e = launch_inner_fused_prime<3>(l, a, sk); break;
+        default: e = launch_inner_fused_prime<4>(l, a, sk); break;
+        }
+        CK(e);
+        rec_end(sk);
     }
     return GBNTT_OK;
 }
@@ -757,9 +817,10 @@ static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t
     uint64_t *specA = g.d_spec;
     uint64_t *specB = g.d_spec + 3 * g.n_max;
     const PrimeSet &ps = coef32_set();
+    const bool fused = fuse_inner(L);
     cudaStream_t aux = fork_aux(ps, st, g.stream2);
     int rc = forward(ps, specA, g.n_max, d_a, na, L, st, false, 1, nullptr, nullptr, aux, stage_a, false,
-                     stage_b ? g.ev_a : nullptr);
+                     stage_b ? g.ev_a : nullptr, fused);
     if (rc) return rc;
     if (!square) {
         if (stage_b) {
@@ -770,10 +831,15 @@ static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t
             CK(cudaStreamWaitEvent(st, g.ev_b, 0));
             if (aux) CK(cudaStreamWaitEvent(aux, g.ev_b, 0));
         }
-        rc = forward(ps, specB, g.n_max, d_b, nb, L, st, false, 1, nullptr, nullptr, aux);
+        rc = forward(ps, specB, g.n_max, d_b, nb, L, st, false, 1, nullptr, nullptr, aux, nullptr, false, nullptr,
+                     fused);
         if (rc) return rc;
     }
-    rc = inverse(ps, specA, square ? specA : specB, g.n_max, L, st, square, 1, aux);
+    if (fused) {
+        rc = inner_fused(ps, specA, square ? specA : specB, g.n_max, L, st, square, 1, aux);
+        if (rc) return rc;
+    }
+    rc = inverse(ps, specA, square ? specA : specB, g.n_max, L, st, square, 1, aux, false, fused);
     if (rc) return rc;
     rc = join_aux(st, aux);
     if (rc) return rc;
@@ -822,13 +888,20 @@ static int mul_dev64(uint64_t *d_c, const uint64_t *d_a, size_t na, const uint64
     const bool square = (d_a == d_b && na == nb);
     uint64_t *specA = g.d_spec;
     uint64_t *specB = g.d_spec + 3 * g.n_max;
-    int rc = forward(kSet3, specA, g.n_max, d_a, na, L, st, true);
+    const bool fused = fuse_inner(L);
+    int rc = forward(kSet3, specA, g.n_max, d_a, na, L, st, true, 1, nullptr, nullptr, nullptr, nullptr, false, nullptr,
+                     fused);
     if (rc) return rc;
     if (!square) {
-        rc = forward(kSet3, specB, g.n_max, d_b, nb, L, st, true);
+        rc = forward(kSet3, specB, g.n_max, d_b, nb, L, st, true, 1, nullptr, nullptr, nullptr, nullptr, false, nullptr,
+                     fused);
         if (rc) return rc;
     }
-    rc = inverse(kSet3, specA, square ? specA : specB, g.n_max, L, st, square);
+    if (fused) {
+        rc = inner_fused(kSet3, specA, square ? specA : specB, g.n_max, L, st, square);
+        if (rc) return rc;
+    }
+    rc = inverse(kSet3, specA, square ? specA : specB, g.n_max, L, st, square, 1, nullptr, false, fused);
     if (rc) return rc;
     return carry64(d_c, n_out, specA, g.n_max, L, st);
 }
@@ -907,15 +980,22 @@ static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaSt
     uint64_t *specA = x.spec, *specB = x.spec + 3 * x.cap;
     const PrimeSet &ps = coef32_set();
     cudaStream_t aux = fork_aux(ps, st, aux_stream);
+    // a shared right operand is transformed once and read by every product's
+    // pointwise pass, so it keeps the unfused innermost passes
+    const bool fused = !shared_b && fuse_inner(L);
     int rc = forward(ps, specA, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab),
-                     (const long long *)(dtab + W), aux);
+                     (const long long *)(dtab + W), aux, nullptr, false, nullptr, fused);
     if (rc) return rc;
     // shared right operand: one transform (table entry 0), read by every
     // product's pointwise pass
     rc = forward(ps, specB, x.cap, nullptr, 0, L, st, false, shared_b ? 1 : W, (const uint32_t *const *)(dtab + 2 * W),
-                 (const long long *)(dtab + 3 * W), aux);
+                 (const long long *)(dtab + 3 * W), aux, nullptr, false, nullptr, fused);
     if (rc) return rc;
-    rc = inverse(ps, specA, specB, x.cap, L, st, false, W, aux, shared_b);
+    if (fused) {
+        rc = inner_fused(ps, specA, specB, x.cap, L, st, false, W, aux);
+        if (rc) return rc;
+    }
+    rc = inverse(ps, specA, specB, x.cap, L, st, false, W, aux, shared_b, fused);
     if (rc) return rc;
     rc = join_aux(st, aux);
     if (rc) return rc;

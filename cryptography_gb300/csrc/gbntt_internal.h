@@ -73,6 +73,10 @@ struct PassArgs {
     int use_scale;              // fold scale[] into the inverse input twiddles
     int prime_base;             // unused (one launch per prime)
     uint64_t w64[64];           // Montgomery w_64^i of this launch's prime and direction
+    // fused innermost passes (forward, pointwise, inverse in one launch):
+    // the inverse direction's step-1 tables and w_64 powers
+    const uint64_t *st1_inv[3];
+    uint64_t w64_inv[64];
 };
 
 struct CarryArgs {
@@ -105,6 +109,12 @@ enum ErrorBits : unsigned int {
 // Launchers (gbntt_kernels.cu).
 template <int PI>
 cudaError_t launch_pass_prime(int log_l, int dir, int ld, const PassArgs &a, cudaStream_t st);
+// The innermost passes of a product in one launch: the last forward pass of
+// data[] and of other[] (other == data: a square), their pointwise product
+// and the first inverse pass, in place in data[] (contiguous blocks of
+// 2^log_l points; plans of two or more passes).
+template <int PI>
+cudaError_t launch_inner_fused_prime(int log_l, const PassArgs &a, cudaStream_t st);
 // Fill one pass twiddle table (see PassArgs::ptw) of prime PI from the
 // two-level tables hi/lo of the wanted direction; use_scale multiplies every
 // entry by scale (the outermost inverse pass).

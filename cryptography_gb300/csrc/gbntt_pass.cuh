@@ -196,8 +196,8 @@ __device__ __forceinline__ typename Field<PI>::T load_elem(const PassArgs &a, co
     if constexpr (LD == LD_U32) {
         return F::from_u32((uint32_t)limb32_at(a, addr));
     } else if constexpr (LD == LD_U64LIMB) {
-        if constexpr (sizeof(typename F::T) == 8) return limb64_residue<PI>(a, addr);
-        else return 0;
+        if constexpr (sizeof(typename F::T) == 8) return F::from_u64(limb64_residue<PI>(a, addr));
+        else return F::zero();
     } else if constexpr (LD == LD_PW) {
         const long long oaddr = a.other_log ? (addr & ((1LL << a.other_log) - 1)) : addr;
         return F::mul(data[addr], other[oaddr]);
@@ -210,7 +210,8 @@ __device__ __forceinline__ typename Field<PI>::T load_elem(const PassArgs &a, co
 // column is col0 into sm: tile element (g, m) -> sm[g*RS + m + m/B]; rows of
 // a contiguous tile beyond the pass are zero-filled with plain stores.
 template <int PI, int LOG_L, int LAYOUT>
-__device__ __forceinline__ void issue_tile_loads(const PassArgs &a, typename Field<PI>::T *sm, long long col0)
+__device__ __forceinline__ void issue_tile_loads_from(const PassArgs &a, const typename Field<PI>::T *data,
+                                                      typename Field<PI>::T *sm, long long col0)
 {
     using F = Field<PI>;
     using V = typename F::T;
@@ -219,7 +220,6 @@ __device__ __forceinline__ void issue_tile_loads(const PassArgs &a, typename Fie
     constexpr int T = S_::T, RS = S_::RS;
     const int t = threadIdx.x;
     const int log_s = a.log_s, log_m = a.log_m;
-    const V *data = (const V *)a.data[F::SLOT];
     if (LAYOUT == LAYOUT_STRIDED) {
         const uint64_t j0 = (uint64_t)(col0 & ((1LL << log_s) - 1));
         const int g = t & (G - 1), m0 = t >> LOG_G;
@@ -238,181 +238,31 @@ __device__ __forceinline__ void issue_tile_loads(const PassArgs &a, typename Fie
             const int g = e >> LOG_L, m = e & (L - 1);
             V *d = sm + g * RS + m + (m >> LOG_B);
             if (g < rows_left) cp_async_word<sizeof(V)>(d, data + base + e);
-            else *d = 0;
+            else *d = F::zero();
         }
     }
 }
 
-// One tile of a pass: load (unless PRELOADED: the caller has already
-// brought this thread's words of the tile into sm), DFT steps, store.
-template <int PI, int LOG_L, int DIR, int LD, int LAYOUT, bool PRELOADED = false>
-__device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>::T *sm, const uint64_t *w64,
-                                          long long col0)
+template <int PI, int LOG_L, int LAYOUT>
+__device__ __forceinline__ void issue_tile_loads(const PassArgs &a, typename Field<PI>::T *sm, long long col0)
+{
+    issue_tile_loads_from<PI, LOG_L, LAYOUT>(a, (const typename Field<PI>::T *)a.data[Field<PI>::SLOT], sm, col0);
+}
+
+// The 2^l-point DFT of every column of a tile in shared memory, in place:
+// tile element (g, m) at sm[g RS + m + m/B] in natural order in, output k
+// at the same index out (forward: DIF, inverse: its transpose). Starts with
+// the tile complete in shared memory (after a barrier) and ends with a
+// barrier.
+template <int PI, int LOG_L, int DIR, int LD>
+__device__ __forceinline__ void tile_steps(typename Field<PI>::T *sm, const uint64_t *w64,
+                                           const typename Field<PI>::T *st1)
 {
     using F = Field<PI>;
     using V = typename F::T;
     using S_ = PassShape<LOG_L, sizeof(V)>;
-    constexpr int L = S_::L, A = S_::A, B = S_::B, LOG_B = S_::LOG_B, G = S_::G, LOG_G = S_::LOG_G;
-    constexpr int T = S_::T, RS = S_::RS;
+    constexpr int A = S_::A, B = S_::B, LOG_B = S_::LOG_B, RS = S_::RS;
     const int t = threadIdx.x;
-    const int log_s = a.log_s, log_m = a.log_m;
-    V *data = (V *)a.data[F::SLOT];
-    const V *other = (const V *)a.other[F::SLOT];
-    const V *twhi = (const V *)a.tw.hi[F::SLOT];
-    const V *twlo = (const V *)a.tw.lo[F::SLOT];
-    const V *st1 = (const V *)a.tw.st1[F::SLOT] + (L - 32);   // w_L^(ka b) at [ka B + b]
-    const int sh = kMaxLog - log_m;
-    // column index within the sub-problem of the first column of this CTA
-    const uint64_t j0 = LAYOUT == LAYOUT_STRIDED ? (uint64_t)(col0 & ((1LL << log_s) - 1)) : 0ull;
-
-    // ---- load: tile element (g, m) -> sm[g*RS + m + m/B]
-    if constexpr (PRELOADED) {
-    } else if constexpr (LD == LD_U64 && GBNTT_PASS_CPASYNC) {
-        issue_tile_loads<PI, LOG_L, LAYOUT>(a, sm, col0);
-        cp_async_wait_all();
-    } else if (LAYOUT == LAYOUT_STRIDED) {
-        const int g = t & (G - 1), m0 = t >> LOG_G;            // m = m0 + it*B
-        const long long S = 1LL << log_s;
-        const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
-        const long long stepg = (long long)B * S;
-        V *dst = sm + g * RS + m0;
-        bool loaded = false;
-        if constexpr (LD == LD_U32 && GBNTT_PASS_LIMB_ASYNC) {
-            if (!a.limb_tab) {
-                // one operand's limbs: every copy of the thread in flight at
-                // once, zero-filled beyond the operand (the slot's low word;
-                // tile_in reduces it when step 1 reads it)
-                const uint32_t *limbs = a.limbs;
-#pragma unroll
-                for (int it = 0; it < A; it++) {
-                    const long long addr = base + it * stepg;
-                    const bool in = addr < a.n_limbs;
-                    cp_async_u32_zfill(dst + it * (B + 1), limbs + (in ? addr : 0), in ? 4 : 0);
-                }
-                cp_async_wait_all();
-                loaded = true;
-            }
-        }
-        if (!loaded) {
-            if constexpr (sizeof(V) == 4) {   // all A loads in flight (registers allow it)
-#pragma unroll
-                for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
-            } else {
-#pragma unroll 8
-                for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
-            }
-        }
-        if constexpr (LD == LD_U32 && sizeof(V) == 8) {
-            // staged first pass (64-bit prime, whose residue of a limb is
-            // the limb): copy the limbs just read to stage_out in HBM
-            if (a.stage_out) {
-#pragma unroll 4
-                for (int it = 0; it < A; it++) {
-                    const long long addr = base + it * stepg;
-                    if (addr < a.n_limbs) a.stage_out[addr] = (uint32_t)dst[it * (B + 1)];
-                }
-            }
-        }
-    } else if constexpr (LD == LD_PW && GBNTT_PASS_PW_ASYNC) {
-        // pointwise product: this spectrum's words go to the tile through
-        // cp.async while the other spectrum's words are loaded into
-        // registers, all in flight at once; each thread then multiplies the
-        // words it copied (visible to it after the wait)
-        const long long rows_left = a.ncols - col0;
-        const long long base = col0 << LOG_L;
-        // a shared second spectrum (one operand common to the whole batch)
-        // is read at the position within its product
-        const long long omask = a.other_log ? ((1LL << a.other_log) - 1) : -1LL;
-        V o[A];
-#pragma unroll
-        for (int it = 0; it < A; it++) {
-            const int e = t + it * T;
-            const int g = e >> LOG_L, m = e & (L - 1);
-            V *d = sm + g * RS + m + (m >> LOG_B);
-            if (g < rows_left) {
-                cp_async_word<sizeof(V)>(d, data + base + e);
-                o[it] = __ldg(other + ((base + e) & omask));
-            } else {
-                *d = 0;
-                o[it] = 0;
-            }
-        }
-        cp_async_wait_all();
-#pragma unroll
-        for (int it = 0; it < A; it++) {
-            const int e = t + it * T;
-            const int m = e & (L - 1);
-            V *d = sm + (e >> LOG_L) * RS + m + (m >> LOG_B);
-            *d = F::mul(*d, o[it]);
-        }
-    } else {
-        const long long rows_left = a.ncols - col0;
-        const long long base = col0 << LOG_L;
-#pragma unroll 8
-        for (int it = 0; it < A; it++) {
-            const int e = t + it * T;
-            const int g = e >> LOG_L, m = e & (L - 1);
-            V v = 0;
-            if (g < rows_left) v = load_elem<PI, LD>(a, data, other, base + e);
-            sm[g * RS + m + (m >> LOG_B)] = v;
-        }
-        if constexpr (LD == LD_U32 && sizeof(V) == 8) {
-            if (a.stage_out) {   // staged first pass, as in the strided layout
-#pragma unroll 4
-                for (int it = 0; it < A; it++) {
-                    const int e = t + it * T;
-                    const int g = e >> LOG_L, m = e & (L - 1);
-                    if (g < rows_left && base + e < a.n_limbs) a.stage_out[base + e] = (uint32_t)sm[g * RS + m + (m >> LOG_B)];
-                }
-            }
-        }
-    }
-    if (DIR == 1 && (a.twiddle || a.use_scale)) {
-        // inverse pass: input row m of column j gets w_M^-(j m), times the
-        // scale in the last pass; each thread scales the words it loaded (a
-        // partly rolled loop instead of the unrolled register step)
-        if (LAYOUT == LAYOUT_STRIDED) {
-            const int g = t & (G - 1), m0 = t >> LOG_G;
-            const uint64_t j = j0 + (uint64_t)g;
-            V *dst = sm + g * RS + m0;
-            const V *ptw = (const V *)a.ptw[F::SLOT];
-            if (a.twiddle && ptw) {
-                // table entry j + m S (the scale already folded in)
-                const long long S = 1LL << log_s;
-                const V *tp = ptw + (long long)j + (long long)m0 * S;
-                const long long stepg = (long long)B * S;
-#pragma unroll 4
-                for (int it = 0; it < A; it++) dst[it * (B + 1)] = F::mul(dst[it * (B + 1)], __ldg(tp + it * stepg));
-            } else if (a.twiddle) {
-                V tw = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)m0 * j) << sh));
-                const V step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * j) << sh));
-                if (a.use_scale) tw = F::mul(tw, (V)a.scale[F::SLOT]);
-#pragma unroll 4
-                for (int it = 0; it < A; it++) {
-                    dst[it * (B + 1)] = F::mul(dst[it * (B + 1)], tw);
-                    tw = F::mul(tw, step);
-                }
-            } else {
-                const V sc = (V)a.scale[F::SLOT];
-#pragma unroll 4
-                for (int it = 0; it < A; it++) dst[it * (B + 1)] = F::mul(dst[it * (B + 1)], sc);
-            }
-        } else {   // contiguous: no twiddle (S = 1), only the scale
-            const long long rows_left = a.ncols - col0;
-            const V sc = (V)a.scale[F::SLOT];
-#pragma unroll 4
-            for (int it = 0; it < A; it++) {
-                const int e = t + it * T;
-                const int g = e >> LOG_L, m = e & (L - 1);
-                if (g < rows_left) {
-                    V *d = sm + g * RS + m + (m >> LOG_B);
-                    *d = F::mul(*d, sc);
-                }
-            }
-        }
-    }
-    __syncthreads();
-
     if constexpr (S_::A == S_::B && GBNTT_PASS_SHARED_DFT) {
         // Even l: both steps are A-point DFTs whose outputs go to
         // sm[g RS + k (B + 1) + lane]; only the read differs (column, then
@@ -513,6 +363,179 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
     }
     __syncthreads();
     }
+}
+
+// One tile of a pass: load (unless PRELOADED: the caller has already
+// brought this thread's words of the tile into sm), DFT steps, store.
+template <int PI, int LOG_L, int DIR, int LD, int LAYOUT, bool PRELOADED = false>
+__device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>::T *sm, const uint64_t *w64,
+                                          long long col0)
+{
+    using F = Field<PI>;
+    using V = typename F::T;
+    using S_ = PassShape<LOG_L, sizeof(V)>;
+    constexpr int L = S_::L, A = S_::A, B = S_::B, LOG_B = S_::LOG_B, G = S_::G, LOG_G = S_::LOG_G;
+    constexpr int T = S_::T, RS = S_::RS;
+    const int t = threadIdx.x;
+    const int log_s = a.log_s, log_m = a.log_m;
+    V *data = (V *)a.data[F::SLOT];
+    const V *other = (const V *)a.other[F::SLOT];
+    const V *twhi = (const V *)a.tw.hi[F::SLOT];
+    const V *twlo = (const V *)a.tw.lo[F::SLOT];
+    const V *st1 = (const V *)a.tw.st1[F::SLOT] + (L - 32);   // w_L^(ka b) at [ka B + b]
+    const int sh = kMaxLog - log_m;
+    // column index within the sub-problem of the first column of this CTA
+    const uint64_t j0 = LAYOUT == LAYOUT_STRIDED ? (uint64_t)(col0 & ((1LL << log_s) - 1)) : 0ull;
+
+    // ---- load: tile element (g, m) -> sm[g*RS + m + m/B]
+    if constexpr (PRELOADED) {
+    } else if constexpr (LD == LD_U64 && GBNTT_PASS_CPASYNC) {
+        issue_tile_loads<PI, LOG_L, LAYOUT>(a, sm, col0);
+        cp_async_wait_all();
+    } else if (LAYOUT == LAYOUT_STRIDED) {
+        const int g = t & (G - 1), m0 = t >> LOG_G;            // m = m0 + it*B
+        const long long S = 1LL << log_s;
+        const long long base = ((col0 >> log_s) << log_m) + (long long)j0 + g + (long long)m0 * S;
+        const long long stepg = (long long)B * S;
+        V *dst = sm + g * RS + m0;
+        bool loaded = false;
+        if constexpr (LD == LD_U32 && GBNTT_PASS_LIMB_ASYNC) {
+            if (!a.limb_tab) {
+                // one operand's limbs: every copy of the thread in flight at
+                // once, zero-filled beyond the operand (the slot's low word;
+                // tile_in reduces it when step 1 reads it)
+                const uint32_t *limbs = a.limbs;
+#pragma unroll
+                for (int it = 0; it < A; it++) {
+                    const long long addr = base + it * stepg;
+                    const bool in = addr < a.n_limbs;
+                    cp_async_u32_zfill(dst + it * (B + 1), limbs + (in ? addr : 0), in ? 4 : 0);
+                }
+                cp_async_wait_all();
+                loaded = true;
+            }
+        }
+        if (!loaded) {
+            if constexpr (sizeof(V) == 4) {   // all A loads in flight (registers allow it)
+#pragma unroll
+                for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
+            } else {
+#pragma unroll 8
+                for (int it = 0; it < A; it++) dst[it * (B + 1)] = load_elem<PI, LD>(a, data, other, base + it * stepg);
+            }
+        }
+        if constexpr (LD == LD_U32 && sizeof(V) == 8) {
+            // staged first pass (64-bit prime, whose residue of a limb is
+            // the limb): copy the limbs just read to stage_out in HBM
+            if (a.stage_out) {
+#pragma unroll 4
+                for (int it = 0; it < A; it++) {
+                    const long long addr = base + it * stepg;
+                    if (addr < a.n_limbs) a.stage_out[addr] = F::low32(dst[it * (B + 1)]);
+                }
+            }
+        }
+    } else if constexpr (LD == LD_PW && GBNTT_PASS_PW_ASYNC) {
+        // pointwise product: this spectrum's words go to the tile through
+        // cp.async while the other spectrum's words are loaded into
+        // registers, all in flight at once; each thread then multiplies the
+        // words it copied (visible to it after the wait)
+        const long long rows_left = a.ncols - col0;
+        const long long base = col0 << LOG_L;
+        // a shared second spectrum (one operand common to the whole batch)
+        // is read at the position within its product
+        const long long omask = a.other_log ? ((1LL << a.other_log) - 1) : -1LL;
+        V o[A];
+#pragma unroll
+        for (int it = 0; it < A; it++) {
+            const int e = t + it * T;
+            const int g = e >> LOG_L, m = e & (L - 1);
+            V *d = sm + g * RS + m + (m >> LOG_B);
+            if (g < rows_left) {
+                cp_async_word<sizeof(V)>(d, data + base + e);
+                o[it] = __ldg(other + ((base + e) & omask));
+            } else {
+                *d = F::zero();
+                o[it] = F::zero();
+            }
+        }
+        cp_async_wait_all();
+#pragma unroll
+        for (int it = 0; it < A; it++) {
+            const int e = t + it * T;
+            const int m = e & (L - 1);
+            V *d = sm + (e >> LOG_L) * RS + m + (m >> LOG_B);
+            *d = F::mul(*d, o[it]);
+        }
+    } else {
+        const long long rows_left = a.ncols - col0;
+        const long long base = col0 << LOG_L;
+#pragma unroll 8
+        for (int it = 0; it < A; it++) {
+            const int e = t + it * T;
+            const int g = e >> LOG_L, m = e & (L - 1);
+            V v = F::zero();
+            if (g < rows_left) v = load_elem<PI, LD>(a, data, other, base + e);
+            sm[g * RS + m + (m >> LOG_B)] = v;
+        }
+        if constexpr (LD == LD_U32 && sizeof(V) == 8) {
+            if (a.stage_out) {   // staged first pass, as in the strided layout
+#pragma unroll 4
+                for (int it = 0; it < A; it++) {
+                    const int e = t + it * T;
+                    const int g = e >> LOG_L, m = e & (L - 1);
+                    if (g < rows_left && base + e < a.n_limbs) a.stage_out[base + e] = F::low32(sm[g * RS + m + (m >> LOG_B)]);
+                }
+            }
+        }
+    }
+    if (DIR == 1 && (a.twiddle || a.use_scale)) {
+        // inverse pass: input row m of column j gets w_M^-(j m), times the
+        // scale in the last pass; each thread scales the words it loaded (a
+        // partly rolled loop instead of the unrolled register step)
+        if (LAYOUT == LAYOUT_STRIDED) {
+            const int g = t & (G - 1), m0 = t >> LOG_G;
+            const uint64_t j = j0 + (uint64_t)g;
+            V *dst = sm + g * RS + m0;
+            const V *ptw = (const V *)a.ptw[F::SLOT];
+            if (a.twiddle && ptw) {
+                // table entry j + m S (the scale already folded in)
+                const long long S = 1LL << log_s;
+                const V *tp = ptw + (long long)j + (long long)m0 * S;
+                const long long stepg = (long long)B * S;
+#pragma unroll 4
+                for (int it = 0; it < A; it++) dst[it * (B + 1)] = F::mul(dst[it * (B + 1)], __ldg(tp + it * stepg));
+            } else if (a.twiddle) {
+                V tw = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)m0 * j) << sh));
+                const V step = tw_exp<PI>(twhi, twlo, (uint32_t)(((uint64_t)B * j) << sh));
+                if (a.use_scale) tw = F::mul(tw, F::from_u64(a.scale[F::SLOT]));
+#pragma unroll 4
+                for (int it = 0; it < A; it++) {
+                    dst[it * (B + 1)] = F::mul(dst[it * (B + 1)], tw);
+                    tw = F::mul(tw, step);
+                }
+            } else {
+                const V sc = F::from_u64(a.scale[F::SLOT]);
+#pragma unroll 4
+                for (int it = 0; it < A; it++) dst[it * (B + 1)] = F::mul(dst[it * (B + 1)], sc);
+            }
+        } else {   // contiguous: no twiddle (S = 1), only the scale
+            const long long rows_left = a.ncols - col0;
+            const V sc = F::from_u64(a.scale[F::SLOT]);
+#pragma unroll 4
+            for (int it = 0; it < A; it++) {
+                const int e = t + it * T;
+                const int g = e >> LOG_L, m = e & (L - 1);
+                if (g < rows_left) {
+                    V *d = sm + g * RS + m + (m >> LOG_B);
+                    *d = F::mul(*d, sc);
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    tile_steps<PI, LOG_L, DIR, LD>(sm, w64, st1);
 
     // ---- store: same addressing as the load
     if (LAYOUT == LAYOUT_STRIDED) {
@@ -665,14 +688,110 @@ static cudaError_t launch_pass_l(int dir, int ld, const PassArgs &a, cudaStream_
     return cudaGetLastError();
 }
 
+#ifndef GBNTT_FUSED_MIN_BLOCKS
+#define GBNTT_FUSED_MIN_BLOCKS 6   // resident CTAs the fused kernel's registers target (64-bit primes; two tiles of shared memory each)
+#endif
+template <int PI, int LOG_L>
+struct FusedMinBlocks {
+    // 2^9- and 2^10-point tiles of 64-bit words: two of them take 54-68 KB
+    // of shared memory, so at most three CTAs are resident anyway
+    static constexpr int value = sizeof(typename Field<PI>::T) == 4 ? GBNTT_PASS_MIN_BLOCKS32
+                                                                    : (LOG_L <= 8 ? GBNTT_FUSED_MIN_BLOCKS : 3);
+};
+
+// Innermost passes of a product in one launch. The innermost forward pass
+// of each operand, the pointwise product and the innermost inverse pass all
+// work on the same contiguous blocks of 2^l points, so a CTA loads G blocks
+// of both spectra (as they are before their last forward pass), runs both
+// forward DFTs, multiplies, runs the inverse DFT and stores the blocks of
+// the product spectrum: three words of traffic per point instead of seven
+// over three launches. No pass twiddle and no scale occur in these passes
+// (plans of two or more passes). a.other == a.data: a square.
+template <int PI, int LOG_L>
+__global__ void __launch_bounds__(kPassThreads, FusedMinBlocks<PI, LOG_L>::value) ntt_inner_fused_kernel(PassArgs a)
+{
+    extern __shared__ uint64_t smraw[];
+    using F = Field<PI>;
+    using V = typename F::T;
+    using S_ = PassShape<LOG_L, sizeof(V)>;
+    constexpr int L = S_::L, A = S_::A, LOG_B = S_::LOG_B, LOG_L_ = LOG_L, T = S_::T, RS = S_::RS;
+    constexpr size_t TW = S_::SMEM / sizeof(V);   // words per tile buffer
+    V *const smA = reinterpret_cast<V *>(smraw);
+    V *const smB = smA + TW;
+    const long long col0 = (long long)blockIdx.x * S_::G;
+    const bool square = a.other[F::SLOT] == a.data[F::SLOT];
+    const int t = threadIdx.x;
+    // both tiles' copies in flight at once
+    issue_tile_loads_from<PI, LOG_L, LAYOUT_CONTIG>(a, (const V *)a.data[F::SLOT], smA, col0);
+    if (!square) issue_tile_loads_from<PI, LOG_L, LAYOUT_CONTIG>(a, (const V *)a.other[F::SLOT], smB, col0);
+    cp_async_wait_all();
+    __syncthreads();
+    const V *st1f = (const V *)a.tw.st1[F::SLOT] + (L - 32);
+    const V *st1i = (const V *)a.st1_inv[F::SLOT] + (L - 32);
+#pragma unroll 1
+    for (int op = 0; op < (square ? 1 : 2); op++) tile_steps<PI, LOG_L, 0, LD_U64>(op ? smB : smA, a.w64, st1f);
+    // pointwise product (Montgomery: leaves R^-1, folded into the scale of
+    // the outermost inverse pass as in the unfused pointwise pass)
+#pragma unroll 4
+    for (int it = 0; it < A; it++) {
+        const int e = t + it * T;
+        const int g = e >> LOG_L_, m = e & (L - 1);
+        const int idx = g * RS + m + (m >> LOG_B);
+        smA[idx] = F::mul(smA[idx], square ? smA[idx] : smB[idx]);
+    }
+    __syncthreads();
+    tile_steps<PI, LOG_L, 1, LD_U64>(smA, a.w64_inv, st1i);
+    V *data = (V *)a.data[F::SLOT];
+    const long long rows_left = a.ncols - col0;
+    const long long base = col0 << LOG_L;
+#pragma unroll 8
+    for (int it = 0; it < A; it++) {
+        const int e = t + it * T;
+        const int g = e >> LOG_L_, m = e & (L - 1);
+        if (g < rows_left) data[base + e] = smA[g * RS + m + (m >> LOG_B)];
+    }
+}
+
+template <int PI, int LOG_L>
+static cudaError_t launch_inner_fused_l(const PassArgs &a, cudaStream_t st)
+{
+    using S_ = PassShape<LOG_L, sizeof(typename Field<PI>::T)>;
+    const long long gx = (a.ncols + S_::G - 1) / S_::G;
+    const size_t smem = 2 * S_::SMEM;
+    auto fn = ntt_inner_fused_kernel<PI, LOG_L>;
+    static bool attr_set = false;   // once per instantiation (before any graph capture uses it)
+    if (smem > 48 * 1024 && !attr_set) {
+        const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    fn<<<(unsigned)gx, kPassThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int PI>
+cudaError_t launch_inner_fused_prime(int log_l, const PassArgs &a, cudaStream_t st)
+{
+    switch (log_l) {
+    case 5: return launch_inner_fused_l<PI, 5>(a, st);
+    case 6: return launch_inner_fused_l<PI, 6>(a, st);
+    case 7: return launch_inner_fused_l<PI, 7>(a, st);
+    case 8: return launch_inner_fused_l<PI, 8>(a, st);
+    case 9: return launch_inner_fused_l<PI, 9>(a, st);
+    case 10: return launch_inner_fused_l<PI, 10>(a, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 // Pass twiddle table: entry e = j + m S (m < 2^(log_m - log_s), j < S) is
 // w_M^(j m) from the two-level tables of the wanted direction, times scale
 // when use_scale is set.
 template <int PI>
 __global__ void build_pass_twiddles_kernel(typename Field<PI>::T *table, const typename Field<PI>::T *hi,
                                            const typename Field<PI>::T *lo, int log_m, int log_s, int use_scale,
-                                           typename Field<PI>::T scale)
+                                           uint64_t scale64)
 {
+    const typename Field<PI>::T scale = Field<PI>::from_u64(scale64);
     const long long M = 1LL << log_m;
     const int sh = kMaxLog - log_m;
     for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < M; e += (long long)gridDim.x * blockDim.x) {
@@ -691,7 +810,7 @@ cudaError_t launch_build_pass_twiddles(uint64_t *table, const uint64_t *hi, cons
     const long long M = 1LL << log_m;
     const long long grid = std::min<long long>((M + 255) / 256, 152 * 16);
     build_pass_twiddles_kernel<PI><<<(unsigned)grid, 256, 0, st>>>((V *)table, (const V *)hi, (const V *)lo, log_m,
-                                                                   log_s, use_scale, (V)scale);
+                                                                   log_s, use_scale, scale);
     return cudaGetLastError();
 }
 

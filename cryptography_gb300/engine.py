@@ -208,7 +208,7 @@ def plan(log_n):
     return [p[i] for i in range(n)]
 
 
-LAUNCH_KINDS = ("fwd_pass_first", "fwd_pass", "inv_pass_first", "inv_pass", "garner_carry")
+LAUNCH_KINDS = ("fwd_pass_first", "fwd_pass", "inv_pass_first", "inv_pass", "garner_carry", "fused_inner_pass")
 
 
 def launch_log(enable):

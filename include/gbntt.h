@@ -249,7 +249,9 @@ int gbntt_fill_operand(uint32_t *d, size_t n, uint64_t seed, void *stream);
 /* Per-launch timing for roofline reports. gbntt_launch_log(1) makes every
  * following kernel launch record CUDA events (kind: 0 first forward pass,
  * 1 forward pass, 2 first inverse pass with the pointwise product,
- * 3 inverse pass, 4 Garner + carry), its pass size log2 and its algorithmic
+ * 3 inverse pass, 4 Garner + carry, 5 the fused innermost passes: both
+ * operands' last forward pass, the pointwise product and the first inverse
+ * pass in one launch), its pass size log2 and its algorithmic
  * bytes; gbntt_launch_log(0) stops and clears. gbntt_launch_records
  * synchronises and copies up to max_records entries; returns the count or
  * a negative GBNTT_* code. */

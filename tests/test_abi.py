@@ -42,9 +42,10 @@ def test_library_is_native_sm103a(built_lib):
 
 def test_pure_host_queries(built_lib):
     # no device needed: planning and sizing are host logic
-    assert engine.plan(29) == [7, 7, 8, 7]
-    assert engine.plan(30) == [7, 8, 8, 7]
-    assert engine.plan(21) == [5, 8, 8]
+    assert engine.plan(29) == [7, 7, 7, 8]
+    assert engine.plan(30) == [7, 7, 8, 8]
+    assert engine.plan(21) == [6, 7, 8]
+    assert engine.plan(14) == [6, 8]
     assert engine.plan(12) == [6, 6]
     assert engine.plan(5) == [5]
     assert engine.transform_log(1 << 28, 1 << 28) == 29
