@@ -111,6 +111,29 @@ def build_ref_compute_e(force=False):
     return REF_E
 
 
+REF_NEGA_SO = os.path.join(REF_DIR, "libref_nega.so")
+
+
+def build_ref_negacyclic(force=False):
+    """The reference's CPU negacyclic multiply (ntt/ref/ntt_polymul_negacyclic.c,
+    library form -DNTT_NEGACYC_NO_MAIN) compiled by path with
+    ref_negacyclic_shim.c into oracle/_ref/libref_nega.so. None when the
+    reference checkout is absent."""
+    if not reference_available():
+        return None
+    ref = os.path.join(REFERENCE_ROOT, "ntt", "ref")
+    src = os.path.join(ref, "ntt_polymul_negacyclic.c")
+    shim = os.path.join(HERE, "ref_negacyclic_shim.c")
+    if not (force or _stale(REF_NEGA_SO, [src, shim, __file__])):
+        return REF_NEGA_SO
+    os.makedirs(REF_DIR, exist_ok=True)
+    tmp = REF_NEGA_SO + ".tmp"
+    subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-DNTT_NEGACYC_NO_MAIN", "-I", ref,
+                           src, shim, "-o", tmp])
+    os.replace(tmp, REF_NEGA_SO)
+    return REF_NEGA_SO
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     print(build_e_oracle(force=True))

@@ -21,6 +21,28 @@ def test_negacyclic_matches_oracle(engine):
     assert engine.device_errors() == 0
 
 
+def test_negacyclic_matches_reference_cpu_multiply(engine):
+    # the reference's own CPU negacyclic multiply (polymul_ntt_negacyclic,
+    # ntt/ref/ntt_polymul_negacyclic.c:178-213), recorded on seeded inputs in
+    # tests/golden/negacyclic_ref.json: the exact GPU coefficients reduced
+    # mod each case's q equal its outputs
+    import hashlib
+    import json
+    import os
+    from cryptography_gb300 import synth
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "negacyclic_ref.json")
+    cases = json.load(open(path))["cases"]
+    for label, c in cases.items():
+        n, q = c["n"], c["q"]
+        f = (synth.splitmix64(c["seed_f"], 0, n) % np.uint64(q)).astype(np.uint64)
+        g = (synth.splitmix64(c["seed_g"], 0, n) % np.uint64(q)).astype(np.uint64)
+        got = np.array([v % q for v in engine.negacyclic_mul(f, g)], dtype=np.uint64)
+        assert [int(v) for v in got[:8]] == c["head"], label
+        assert [int(v) for v in got[-8:]] == c["tail"], label
+        assert hashlib.sha256(got.astype("<u8").tobytes()).hexdigest() == c["sha256"], label
+    assert engine.device_errors() == 0
+
+
 def test_negacyclic_extreme_coefficients_and_squares(engine):
     n = 1 << 10
     top = np.full(n, (1 << 64) - 1, dtype=np.uint64)
