@@ -273,6 +273,11 @@ def batched_sizes(pairs, seed, lo=10, hi=22):
     return synth.batched_sizes(pairs, seed, lo, hi)
 
 
+# transform-length buckets (log2 N ranges, lower bound exclusive) of the
+# batched and serving breakdowns
+BUCKETS = (("N<=2^16", 0, 16), ("2^16<N<=2^20", 16, 20), ("N>2^20", 20, 64))
+
+
 def run_batched_leg(g, cudart, args, stream):
     """4096 independent pairs, batched engine against looping the plain
     single-product path on the same device-resident operands."""
@@ -325,6 +330,38 @@ def run_batched_leg(g, cudart, args, stream):
     for i in range(pairs):
         N = 1 << max(5, int(np.ceil(np.log2(na_l[i] + nb_l[i] - 1))))
         bm += 10 * 3 * N * 8 + 8 * (na_l[i] + nb_l[i])
+    # where batching pays: the same comparison over the pairs of each
+    # transform-length bucket alone
+    by_size = {}
+    logN = [max(5, int(np.ceil(np.log2(na_l[i] + nb_l[i] - 1)))) for i in range(pairs)]
+    for name, lo, hi in BUCKETS:
+        sel = [i for i in range(pairs) if lo < logN[i] <= hi]
+        if not sel:
+            continue
+
+        def bb():
+            g.batch_mul_device([c_ptr[i] for i in sel], [a_ptr[i] for i in sel], [na_l[i] for i in sel],
+                               [b_ptr[i] for i in sel], [nb_l[i] for i in sel], None)
+
+        def pp():
+            for i in sel:
+                g.mul_device(p_ptr[i], a_ptr[i], na_l[i], b_ptr[i], nb_l[i], None)
+
+        t = {}
+        for nm, fn in (("batched", bb), ("plain", pp)):
+            fn()
+            cudart.stream_sync(stream)
+            e0, e1 = cudart.Event(), cudart.Event()
+            e0.record(stream)
+            for _ in range(args.batch_reps):
+                fn()
+            e1.record(stream)
+            e1.synchronize()
+            t[nm] = e0.elapsed_ms(e1) / args.batch_reps
+        by_size[name] = {"pairs": len(sel), "batched_ms": t["batched"], "plain_ms": t["plain"],
+                         "batched_products_per_s": len(sel) / (t["batched"] * 1e-3),
+                         "plain_products_per_s": len(sel) / (t["plain"] * 1e-3),
+                         "speedup": t["plain"] / t["batched"]}
     for b in bufs:
         b.free()
     out = {"pairs": pairs, "sizes": "log2(n) uniform in [10, 22] per operand, seed 4242",
@@ -335,6 +372,7 @@ def run_batched_leg(g, cudart, args, stream):
            "plain_host_ms": res["plain"]["host_ms"],
            "bytes_model": bm, "batched_GBps_model": bm / (res["batched"]["ms"] * 1e-3) / 1e9,
            "batched_equals_plain_on_sample": same, "sample_pairs": len(sample), "device_error_flags": flags,
+           "by_size": by_size,
            "plain_path": "gbntt_mul_u32 per pair, device pointers, one stream, no host sync per pair"}
     return out
 
@@ -401,6 +439,31 @@ def run_serving_leg(g, cudart, args, stream):
         sat_n = min(nreq, args.serve_saturation)
         sat_wall, sat_lat = run(list(range(sat_n)), None)
         st2 = srv.stats()
+        # saturation and serial plain capacity per transform-length bucket:
+        # requests of the same size distribution restricted to the bucket
+        by_size = {}
+        logN = np.maximum(5, np.ceil(np.log2(na + nb - 1))).astype(int)
+        for name, lo, hi in BUCKETS:
+            idx = [int(i) for i in np.flatnonzero((logN > lo) & (logN <= hi))]
+            if not idx:
+                continue
+            sub = idx[:{"N<=2^16": 3000, "2^16<N<=2^20": 1500}.get(name, 400)]
+            tp = []
+            for i in sub[:200]:
+                t0 = time.perf_counter()
+                g.mul_device(arena.ptr, a_ptr, int(na[i]), b_ptr, int(nb[i]), None)
+                cudart.stream_sync(stream)
+                tp.append(time.perf_counter() - t0)
+            cap_b = 1.0 / float(np.mean(tp[10:] if len(tp) > 20 else tp))
+            w0 = srv.stats()
+            bw, blat = run(sub, None)
+            w1 = srv.stats()
+            by_size[name] = {"requests": len(sub), "served_products_per_s": len(sub) / bw,
+                             "serial_plain_products_per_s": cap_b, "vs_serial_plain": (len(sub) / bw) / cap_b,
+                             "latency_ms_p50": float(np.percentile(blat, 50)),
+                             "latency_ms_p99": float(np.percentile(blat, 99)),
+                             "products_per_wave": (w1["wave_products"] - w0["wave_products"])
+                             / max(1, w1["waves"] - w0["waves"])}
     finally:
         srv.stop()
     pool.free()
@@ -416,6 +479,10 @@ def run_serving_leg(g, cudart, args, stream):
                            "latency_ms_p99": float(np.percentile(sat_lat, 99))},
             "slots": args.serve_slots, "slot_coefficients": 1 << 26,
             "waves": st2["waves"], "products_per_wave": st2["wave_products"] / max(1, st2["waves"]),
+            "by_size": by_size,
+            "admission": "a free slot takes pending requests in arrival order while the sum of their transform "
+                         "lengths fits the slot workspace; they run as one sub-wave per transform length, "
+                         "shortest first, back to back on the slot stream",
             "device_error_flags": st2["device_errors"],
             "latency": "submit -> completion observed by the server thread (host clock)",
             "load": "0.7 x serial capacity of the plain path (gbntt_mul_u32 + sync per request)"}

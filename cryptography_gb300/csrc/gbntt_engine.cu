@@ -302,7 +302,7 @@ static int choose_log(size_t na, size_t nb)
 // limb pointers and lengths of A and B, output pointers and lengths,
 // carry tile starts (W + 1).
 constexpr int kMaxBatch = 16384;
-constexpr size_t kBtabWords = 7 * (size_t)kMaxBatch + 8;
+constexpr size_t kBtabWords = 7 * (size_t)kMaxBatch + 64;   // + one end entry per sub-wave of a serving activation
 
 // Carry tile status words for a workspace of n coefficients per prime: one
 // product of n coefficients (64-bit limbs: n / 1024 tiles), or a batched
@@ -1253,8 +1253,7 @@ struct SrvSlot {
     int tab_slot = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
-    bool busy = false;
-    std::vector<uint64_t> ids;
+    bool busy = false;   // an activation is in flight (guarded by Server::mu)
 };
 
 struct Server {
@@ -1267,68 +1266,181 @@ struct Server {
     size_t cap = 0;
     int slot_log = 0;
     bool stop = false;
-    std::atomic<uint64_t> completed{0}, waves{0}, wave_products{0};
+    std::atomic<uint64_t> completed{0}, waves{0}, wave_products{0}, activations{0};
     int error = 0;
 };
 
 Server *g_srv = nullptr;
 
+// Completion of one sub-wave, reported by a host function enqueued after it
+// on the slot's stream (no CUDA calls in here): its requests are done; the
+// last sub-wave of an activation frees the slot.
+struct SrvDone {
+    Server *S;
+    SrvSlot *sl;
+    std::vector<uint64_t> ids;
+    bool last;
+};
+
+void CUDART_CB srv_done_cb(void *p)
+{
+    SrvDone *d = (SrvDone *)p;
+    Server *S = d->S;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        const auto now = std::chrono::steady_clock::now();
+        for (uint64_t id : d->ids) { S->reqs[id].state = 2; S->reqs[id].t_done = now; }
+        S->completed += d->ids.size();
+        if (d->last) d->sl->busy = false;
+    }
+    S->cv.notify_all();
+    delete d;
+}
+
+// One activation of a slot: the admitted requests grouped by transform
+// length (ascending), each group one sub-wave through the batched pass
+// chain, back to back on the slot's stream (each sub-wave may use the whole
+// slot workspace: they run one after the other). The tables of all
+// sub-waves are filled into one host table slot and go up in one copy.
+// Launches directly (no wave graphs: group layouts rarely repeat).
+int srv_activation(Server *S, SrvSlot &sl, const std::vector<int> &gL,
+                   const std::vector<std::vector<BatchItem>> &gitems, std::vector<std::vector<uint64_t>> &gids)
+{
+    BatchCtx &x = sl.ctx;
+    const int slot = *x.slot;
+    CK(cudaEventSynchronize(x.btab_ev[slot]));   // the previous upload from this table slot has been read
+    uint64_t *h = x.h_btab + slot * kBtabWords;
+    uint64_t *dtab = x.d_btab + slot * kBtabWords;
+    const size_t ng = gL.size();
+    std::vector<size_t> off(ng);
+    std::vector<long long> tiles(ng);
+    std::vector<char> shared(ng);
+    size_t pos = 0;
+    for (size_t gi = 0; gi < ng; gi++) {
+        const std::vector<BatchItem> &items = gitems[gi];
+        const long long W = (long long)items.size();
+        if (pos + 7 * (size_t)W + 1 > kBtabWords) { set_err("server activation tables overflow"); return GBNTT_ERR_SIZE; }
+        uint64_t *hg = h + pos;
+        uint64_t *hA = hg, *hLA = hg + W, *hB = hg + 2 * W, *hLB = hg + 3 * W, *hC = hg + 4 * W, *hNC = hg + 5 * W,
+                 *hTS = hg + 6 * W;
+        long long t = 0;
+        bool sb = W > 1;
+        for (long long k = 0; k < W; k++) {
+            const BatchItem &it = items[k];
+            if (it.b != items[0].b || it.nb != items[0].nb || it.a == it.b) sb = false;
+            hA[k] = (uint64_t)(uintptr_t)it.a;
+            hLA[k] = (uint64_t)it.na;
+            hB[k] = (uint64_t)(uintptr_t)it.b;
+            hLB[k] = (uint64_t)it.nb;
+            hC[k] = (uint64_t)(uintptr_t)it.c;
+            hNC[k] = (uint64_t)(it.na + it.nb);
+            hTS[k] = (uint64_t)t;
+            t += carry_tiles((long long)(it.na + it.nb));
+        }
+        hTS[W] = (uint64_t)t;
+        if ((size_t)t > x.n_status) { set_err("server sub-wave needs %lld carry tiles", t); return GBNTT_ERR_SIZE; }
+        off[gi] = pos;
+        tiles[gi] = t;
+        shared[gi] = sb ? 1 : 0;
+        pos += 7 * (size_t)W + 1;
+    }
+    CK(cudaMemcpyAsync(dtab, h, pos * sizeof(uint64_t), cudaMemcpyHostToDevice, sl.stream));
+    CK(cudaEventRecord(x.btab_ev[slot], sl.stream));
+    *x.slot = slot ^ 1;
+    for (size_t gi = 0; gi < ng; gi++) {
+        const int rc = wave_launches(x, dtab + off[gi], (long long)gitems[gi].size(), gL[gi], sl.stream, nullptr,
+                                     tiles[gi], shared[gi] != 0);
+        if (rc) return rc;
+        SrvDone *d = new SrvDone{S, &sl, std::move(gids[gi]), gi + 1 == ng};
+        const cudaError_t e = cudaLaunchHostFunc(sl.stream, srv_done_cb, d);
+        if (e != cudaSuccess) { delete d; CK(e); }
+    }
+    S->waves += ng;
+    return GBNTT_OK;
+}
+
+// The server thread: sleeps on the condition variable until a request is
+// pending and a slot is free (submissions and sub-wave completions notify
+// it), then admits pending requests in arrival order while their transform
+// lengths fit one slot workspace (the sum of 2^L over the admitted
+// requests, HBM-footprint admission; at least the oldest request; at most
+// kMaxBatch requests) and starts them as one activation of that slot.
 void server_loop(Server *S)
 {
-    std::vector<BatchItem> items;
-    std::vector<uint64_t> ids;
+    std::vector<int> gL;
+    std::vector<std::vector<BatchItem>> gitems;
+    std::vector<std::vector<uint64_t>> gids;
     for (;;) {
-        bool did = false;
-        for (auto &sl : S->slots) {
-            if (sl.busy && cudaEventQuery(sl.done) == cudaSuccess) {
-                const auto now = std::chrono::steady_clock::now();
-                std::lock_guard<std::mutex> lk(S->mu);
-                for (uint64_t id : sl.ids) { S->reqs[id].state = 2; S->reqs[id].t_done = now; }
-                S->completed += sl.ids.size();
-                sl.ids.clear();
-                sl.busy = false;
-                did = true;
-                S->cv.notify_all();
-            }
-        }
-        for (auto &sl : S->slots) {
-            if (sl.busy) continue;
-            ids.clear();
-            int L = 0;
-            {
-                std::lock_guard<std::mutex> lk(S->mu);
-                if (S->pending.empty()) break;
-                L = S->reqs[S->pending.front()].L;
-                const size_t wmax = std::min<size_t>(kMaxBatch, S->cap >> L);
-                std::deque<uint64_t> rest;
-                for (uint64_t id : S->pending) {
-                    if (ids.size() < wmax && S->reqs[id].L == L) { ids.push_back(id); S->reqs[id].state = 1; }
-                    else rest.push_back(id);
-                }
-                S->pending.swap(rest);
-                items.clear();
-                for (uint64_t id : ids) items.push_back(S->reqs[id].item);
-            }
-            const int rc = batch_wave(sl.ctx, items.data(), (long long)items.size(), L, sl.stream);
-            if (rc) S->error = rc;
-            cudaEventRecord(sl.done, sl.stream);
-            sl.ids = ids;
-            sl.busy = true;
-            S->waves++;
-            S->wave_products += ids.size();
-            did = true;
-        }
-        if (!did) {
+        SrvSlot *sl = nullptr;
+        size_t count = 0;
+        {
             std::unique_lock<std::mutex> lk(S->mu);
-            bool any_busy = false;
-            for (auto &sl : S->slots) any_busy |= sl.busy;
-            if (S->stop && S->pending.empty() && !any_busy) return;
-            if (any_busy) {
-                lk.unlock();
-                std::this_thread::sleep_for(std::chrono::microseconds(5));
-            } else {
-                S->cv.wait_for(lk, std::chrono::milliseconds(2));
+            auto free_slot = [&]() -> SrvSlot * {
+                for (auto &x : S->slots)
+                    if (!x.busy) return &x;
+                return nullptr;
+            };
+            auto any_busy = [&]() {
+                for (auto &x : S->slots)
+                    if (x.busy) return true;
+                return false;
+            };
+            S->cv.wait(lk, [&] {
+                return S->error || (!S->pending.empty() && free_slot()) || (S->stop && S->pending.empty() && !any_busy());
+            });
+            if (S->error) return;
+            if (S->pending.empty()) return;   // stop requested and everything has completed
+            sl = free_slot();
+            std::map<int, size_t> group_of;
+            gL.clear();
+            gitems.clear();
+            gids.clear();
+            size_t used = 0;
+            while (!S->pending.empty() && count < (size_t)kMaxBatch) {
+                const uint64_t id = S->pending.front();
+                SrvRequest &r = S->reqs[id];
+                const size_t need = (size_t)1 << r.L;
+                if (count > 0 && used + need > S->cap) break;
+                used += need;
+                count++;
+                r.state = 1;
+                auto it = group_of.find(r.L);
+                size_t gi;
+                if (it == group_of.end()) {
+                    gi = gL.size();
+                    group_of[r.L] = gi;
+                    gL.push_back(r.L);
+                    gitems.emplace_back();
+                    gids.emplace_back();
+                } else {
+                    gi = it->second;
+                }
+                gitems[gi].push_back(r.item);
+                gids[gi].push_back(id);
+                S->pending.pop_front();
             }
+            sl->busy = true;
+        }
+        // shortest transforms first: their requests complete earliest
+        std::vector<size_t> order(gL.size());
+        for (size_t i = 0; i < order.size(); i++) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return gL[a] < gL[b]; });
+        std::vector<int> sL;
+        std::vector<std::vector<BatchItem>> sitems;
+        std::vector<std::vector<uint64_t>> sids;
+        for (size_t i : order) {
+            sL.push_back(gL[i]);
+            sitems.push_back(std::move(gitems[i]));
+            sids.push_back(std::move(gids[i]));
+        }
+        const int rc = srv_activation(S, *sl, sL, sitems, sids);
+        S->activations++;
+        S->wave_products += count;
+        if (rc) {
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->error = rc;
+            S->cv.notify_all();
+            return;
         }
     }
 }
