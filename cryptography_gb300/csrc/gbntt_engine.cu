@@ -1548,6 +1548,24 @@ static void *pinned_device_ptr(const void *p)
     return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
+// Device address under which kernels may read the limbs of a BigInt flagged
+// managed: managed or device memory in place, page-locked host memory through
+// its mapped address; nullptr for anything else (the caller stages it). A
+// reference build linked against this library dynamically keeps its own weak
+// bigint_alloc_managed (ntt/lib/arith/bigint.c:61-68: calloc with managed = 1),
+// so the flag alone does not mean the GPU can reach the memory.
+static const void *managed_device_ptr(const void *p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type == cudaMemoryTypeManaged || at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeHost)
+        return at.devicePointer;
+    return nullptr;
+}
+
 static int mul_host(uint32_t *c, const uint32_t *a, size_t na, const uint32_t *b, size_t nb,
                     const uint32_t *dev_a, const uint32_t *dev_b)
 {
@@ -1721,11 +1739,13 @@ static int bigint_mul_impl(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_b
         // one 64-bit limb per coefficient
         const uint64_t *pa = a->limbs, *pb = b->limbs;
         rc = mul_host64((uint64_t *)outp, pa, (size_t)na64, square ? pa : pb, square ? (size_t)na64 : (size_t)nb64,
-                        a->managed ? pa : nullptr, (!square && b->managed) ? pb : nullptr);
+                        a->managed ? (const uint64_t *)managed_device_ptr(pa) : nullptr,
+                        (!square && b->managed) ? (const uint64_t *)managed_device_ptr(pb) : nullptr);
     } else {
         const uint32_t *pa = (const uint32_t *)a->limbs, *pb = (const uint32_t *)b->limbs;
-        rc = mul_host(outp, pa, na, square ? pa : pb, square ? na : nb, a->managed ? pa : nullptr,
-                      (!square && b->managed) ? pb : nullptr);
+        rc = mul_host(outp, pa, na, square ? pa : pb, square ? na : nb,
+                      a->managed ? (const uint32_t *)managed_device_ptr(pa) : nullptr,
+                      (!square && b->managed) ? (const uint32_t *)managed_device_ptr(pb) : nullptr);
     }
     if (rc) { free(tmp); return rc; }
     if (c->cap < newcap) {

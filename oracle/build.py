@@ -111,6 +111,50 @@ def build_ref_compute_e(force=False):
     return REF_E
 
 
+# The reference's own callers of the engine, linked against libgbntt.so
+# instead of the HIP engine (or ntt_stub.c): compute_e, test_gmp_oracle and
+# test_wrap_guard (ntt/app/compute_e/Makefile builds the same objects).
+DROPIN_BINARIES = {
+    "compute_e_gb300": (["app/compute_e/main.c", "app/compute_e/binary_split.c", "app/compute_e/mem_pool.c",
+                         "lib/arith/bigint.c", "lib/arith/multiply.c", "lib/arith/newton.c",
+                         "lib/arith/base_convert.c"], ["-lm", "-fopenmp"]),
+    "test_gmp_oracle_gb300": (["app/compute_e/test_gmp_oracle.c", "lib/arith/bigint.c", "lib/arith/multiply.c"],
+                              ["-l:libgmp.so.10"]),
+    "test_wrap_guard_gb300": (["app/compute_e/test_wrap_guard.c", "lib/arith/bigint.c"], []),
+}
+
+
+def build_ref_dropin(gbntt_dir, force=False):
+    """Compile the reference's callers by path (the GPU build: no
+    COMPUTE_E_HOST, no stub) and link them against gbntt_dir/libgbntt.so.
+    Returns {binary: path} and the object files per binary, or None when the
+    reference checkout is absent. The binaries run on a machine with a GPU,
+    the reference sources and a compiler for that machine."""
+    if not reference_available():
+        return None
+    ntt = os.path.join(REFERENCE_ROOT, "ntt")
+    inc = ["-I", os.path.join(ntt, "lib"), "-I", os.path.join(ntt, "lib", "arith"),
+           "-I", os.path.join(ntt, "app", "compute_e")]
+    so = os.path.join(gbntt_dir, "libgbntt.so")
+    out, objs_of = {}, {}
+    os.makedirs(REF_DIR, exist_ok=True)
+    for name, (srcs, libs) in DROPIN_BINARIES.items():
+        exe = os.path.join(REF_DIR, name)
+        paths = [os.path.join(ntt, s_) for s_ in srcs]
+        objs = [os.path.join(REF_DIR, "dropin_" + os.path.basename(s_)[:-2] + ".o") for s_ in srcs]
+        if force or _stale(exe, paths + [so, __file__]):
+            for src, obj in zip(paths, objs):
+                subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-fopenmp"] + inc + ["-c", src, "-o", obj])
+            tmp = exe + ".tmp"
+            subprocess.check_call(["gcc"] + objs + ["-L", gbntt_dir, "-l:libgbntt.so",
+                                                    "-Wl,-rpath," + gbntt_dir, "-Wl,--no-undefined"] + libs +
+                                  ["-o", tmp])
+            os.replace(tmp, exe)
+        out[name] = exe
+        objs_of[name] = objs
+    return out, objs_of
+
+
 REF_NEGA_SO = os.path.join(REF_DIR, "libref_nega.so")
 
 

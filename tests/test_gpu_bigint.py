@@ -93,6 +93,35 @@ def test_alias_square_and_managed():
     assert json.loads(r.stdout.strip().splitlines()[-1]) == [True] * 5
 
 
+def test_managed_flag_on_host_heap_memory():
+    # A reference build linked against the library dynamically keeps its own
+    # weak bigint_alloc_managed (ntt/lib/arith/bigint.c:61-68): calloc'd host
+    # memory with managed = 1. The engine must check what the memory is and
+    # stage it, not hand it to the kernels as device-readable.
+    r = run("""
+        L.ntt_mul_init_impl(16)
+        rng = random.Random(12)
+        x, y = rnd(rng, 3000), rnd(rng, 2500)
+        a = g.bigint_from_int(x, 3000)
+        a.managed = 1                                 # calloc'd, flagged managed
+        b = g.bigint_from_int(y, 2500)
+        b.managed = 1
+        c = g.bigint_alloc(5600)
+        c.managed = 1                                 # managed output with room
+        L.ntt_bigint_mul(B(c), B(a), B(b))
+        r1 = g.bigint_to_int(c) == x * y
+        L.ntt_bigint_mul(B(c), B(a), B(a))            # square of a flagged operand
+        r2 = g.bigint_to_int(c) == x * x
+        print(json.dumps([r1, r2]))
+        for v in (a, b, c):
+            v.managed = 0
+            g.bigint_free(v)
+        L.ntt_mul_teardown_impl()
+    """)
+    assert r.returncode == 0, r.stderr
+    assert json.loads(r.stdout.strip().splitlines()[-1]) == [True, True]
+
+
 def test_wrap_guard_death():
     # ntt/app/compute_e/test_wrap_guard.c: log_n = 12 (N = 4096 64-bit
     # coefficients); 3000 + 3000 - 1 > N must exit(1) before any kernel runs,
