@@ -135,7 +135,9 @@ __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b)
 // m1 = t1 + t0, the high half of m q0 is m - m1 - [m1 < m0], so
 //   u = T_hi - m + m1 + [m1 < m0]   in (-q0, q0), minus EPS when negative.
 #ifndef GBNTT_Q0_ALU
-// bit 0: add/sub corrections (measured slower: the ALU pipe fills up),
+// bit 0: add/sub as pure borrow chains (fewer instructions: a butterfly of
+// 13.4 instead of 17.4, a 16-point register DFT of 683 instead of 856, but
+// all on the ALU pipe, which binds: 2^28-limb multiply 52.9 against 51.9 ms),
 // bit 1: multiply-free Montgomery reduction, bit 2: power-of-two reduction;
 // 2^29 transform pairs: 65.4 ms with none, 61.6 ms with bits 1 and 2.
 // bit 3: the 64 x 64 product as 32-bit multiply-add carry chains instead of
@@ -146,22 +148,23 @@ __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b)
 template <>
 __device__ __forceinline__ uint64_t add_mod<0>(uint64_t a, uint64_t b)
 {
-    // s = a + b; x = s + EPS; x when a + b >= 2^64 or s >= q0, else s
+    // a + b = a - (q0 - b): q0 - b = (0xFFFFFFFF : 1) - b needs no borrow out
+    // (b < q0); a borrow of a - (q0 - b) means a + b < q0, and adding q0
+    // back is subtracting EPS = 2^64 - q0 with the borrow mask (bw = EPS).
+    // Borrow chains only: the multiply-add corrections of the generic form
+    // cost negated moves besides the multiply-adds.
     uint64_t r;
     asm("{\n\t"
-        ".reg .u32 a0, a1, b0, b1, s0, s1, c, x0, x1, c2, r0, r1;\n\t"
-        ".reg .pred p;\n\t"
+        ".reg .u32 a0, a1, b0, b1, n0, n1, d0, d1, bw, r0, r1;\n\t"
         "mov.b64 {a0, a1}, %1;\n\t"
         "mov.b64 {b0, b1}, %2;\n\t"
-        "add.cc.u32 s0, a0, b0;\n\t"
-        "addc.cc.u32 s1, a1, b1;\n\t"
-        "addc.u32 c, 0, 0;\n\t"
-        "add.cc.u32 x0, s0, 0xFFFFFFFF;\n\t"
-        "addc.cc.u32 x1, s1, 0;\n\t"
-        "addc.u32 c2, c, 0;\n\t"
-        "setp.ne.u32 p, c2, 0;\n\t"
-        "selp.u32 r0, x0, s0, p;\n\t"
-        "selp.u32 r1, x1, s1, p;\n\t"
+        "sub.cc.u32 n0, 1, b0;\n\t"
+        "subc.u32 n1, 0xFFFFFFFF, b1;\n\t"
+        "sub.cc.u32 d0, a0, n0;\n\t"
+        "subc.cc.u32 d1, a1, n1;\n\t"
+        "subc.u32 bw, 0, 0;\n\t"
+        "sub.cc.u32 r0, d0, bw;\n\t"
+        "subc.u32 r1, d1, 0;\n\t"
         "mov.b64 %0, {r0, r1};\n\t"
         "}"
         : "=l"(r) : "l"(a), "l"(b));

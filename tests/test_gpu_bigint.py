@@ -106,8 +106,8 @@ def test_managed_flag_on_host_heap_memory():
         a.managed = 1                                 # calloc'd, flagged managed
         b = g.bigint_from_int(y, 2500)
         b.managed = 1
-        c = g.bigint_alloc(5600)
-        c.managed = 1                                 # managed output with room
+        c = g.bigint_alloc(6100)
+        c.managed = 1                                 # managed output with room for both products
         L.ntt_bigint_mul(B(c), B(a), B(b))
         r1 = g.bigint_to_int(c) == x * y
         L.ntt_bigint_mul(B(c), B(a), B(a))            # square of a flagged operand
