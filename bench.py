@@ -750,6 +750,24 @@ def run_gpu(args, dist):
                              "three_prime_64bit_bytes_per_launch")
         except (ValueError, OSError):
             traffic = None
+    issue = None
+    ip = os.path.join(ROOT, "profiles", "ncu_issue.json")
+    if os.path.exists(ip) and g.prime_set() == 2:
+        try:
+            ij = json.load(open(ip))
+            scale = float(1 << (lg + 1)) / float(1 << 27)   # the capture's transform length is 2^27
+            inst = ij["multiply_2pow27_warp_instructions"] * scale
+            alu = ij["multiply_2pow27_alu_warp_instructions"] * scale
+            sms = cudart.sm_count()
+            sm_hz = float((clk or {}).get("sm_mhz") or 2070.0) * 1e6   # SM clock sampled in the timed region
+            cap = sms * 4 * sm_hz * ms * 1e-3          # warp-instruction issue slots in one multiply
+            issue = {"bound": "integer issue", "instructions_per_multiply": inst,
+                     "achieved": inst / (ms * 1e-3), "peak": sms * 4 * sm_hz, "unit": "warp instructions/s",
+                     "frac": inst / cap, "alu_pipe_frac": 2.0 * alu / cap,
+                     "sm_mhz": sm_hz / 1e6, "source": "profiles/ncu_issue.json (ncu instruction counts of one "
+                                                    "2^27-point multiply, scaled to this transform length)"}
+        except (ValueError, OSError, KeyError):
+            issue = None
     bm = bytes_model(lg)
     res_bytes = 12 if g.prime_set() == 2 else 24
     bm_own = 10 * (1 << (lg + 1)) * res_bytes + 8 * (2 * n)
@@ -816,6 +834,7 @@ def run_gpu(args, dist):
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "kernel": "ntt_pass_kernel (%d launches per multiply)" % pass_launches,
                      "algorithmic_bytes_per_launch": pass_bytes / max(1, pass_launches)},
+        "issue_roofline": issue,
         "multiply_roofline": {"bytes_model": bm, "achieved_GBps": bm / (ms * 1e-3) / 1e9,
                               "frac": bm / (ms * 1e-3) / 1e9 / peak,
                               "model": "10*k*N*8 + 8*(n_a+n_b), k=3 (2-pass four-step with fused decomposition, "
