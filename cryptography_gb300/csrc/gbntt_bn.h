@@ -149,5 +149,57 @@ inline uint32_t divmod_small(Num &a, uint32_t d)
     return (uint32_t)rem;
 }
 
+// floor(u / v) for v != 0: long division with a two-limb quotient estimate
+// on the normalised divisor, corrected by at most one add-back per limb
+// (Knuth, TAOCP vol. 2, 4.3.1, Algorithm D).
+inline Num div_floor(const Num &u, const Num &v)
+{
+    if (cmp(u, v) < 0) return Num();
+    if (v.size() == 1) {
+        Num q = u;
+        divmod_small(q, v[0]);
+        return q;
+    }
+    const size_t n = v.size(), m = u.size() - n;
+    const int s = __builtin_clz(v.back());
+    Num vn = shl(v, s);
+    Num un = shl(u, s);
+    un.resize(u.size() + 1, 0);
+    Num q(m + 1, 0);
+    for (size_t j = m + 1; j-- > 0;) {
+        const uint64_t num = ((uint64_t)un[j + n] << 32) | un[j + n - 1];
+        uint64_t qh = num / vn[n - 1], rh = num % vn[n - 1];
+        while ((qh >> 32) || qh * vn[n - 2] > ((rh << 32) | un[j + n - 2])) {
+            qh--;
+            rh += vn[n - 1];
+            if (rh >> 32) break;
+        }
+        uint64_t k = 0;
+        uint32_t br = 0;
+        for (size_t i = 0; i < n; i++) {
+            const uint64_t p = qh * vn[i] + k;
+            k = p >> 32;
+            const uint64_t t = (uint64_t)un[i + j] - (uint32_t)p - br;
+            un[i + j] = (uint32_t)t;
+            br = (t >> 32) ? 1u : 0u;
+        }
+        const uint64_t t = (uint64_t)un[j + n] - k - br;
+        un[j + n] = (uint32_t)t;
+        if (t >> 32) {   // qh was one too large: add v back
+            qh--;
+            uint64_t c = 0;
+            for (size_t i = 0; i < n; i++) {
+                c += (uint64_t)un[i + j] + vn[i];
+                un[i + j] = (uint32_t)c;
+                c >>= 32;
+            }
+            un[j + n] += (uint32_t)c;
+        }
+        q[j] = (uint32_t)qh;
+    }
+    trim(q);
+    return q;
+}
+
 }  // namespace bn
 }  // namespace gbntt

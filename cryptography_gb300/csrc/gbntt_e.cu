@@ -28,15 +28,18 @@
 //  * Decimal conversion (reference base_convert.c, divide and conquer on
 //    powers of ten): pieces are split by d_j = 10^(9 2^j) level by level; a
 //    level's pieces are divided together (batched products against one
-//    reciprocal), leading pieces known to be zero are skipped, and pieces of
-//    576 digits are written out by one thread each (dec_leaf_kernel).
+//    reciprocal) and leading pieces known to be zero are skipped, down to
+//    pieces of 9 2^12 digits; below that one CTA per piece finishes the
+//    splits in shared memory and prints the digits (dec_block_kernel).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 #include <algorithm>
 #include <chrono>
+#include <mutex>
 #include <vector>
 
 #include "gbntt.h"
@@ -243,32 +246,232 @@ __global__ void bs_leaf_kernel(unsigned long long a, unsigned long long b, int G
     lens[2 * i + 1] = nq;
 }
 
-// Decimal leaves: piece i (i >= first), `stride` limbs at pieces + i stride,
-// holds a value below 10^(9 groups); its 9 groups digits (zero padded) go to
-// digits + 9 groups i, by repeated division by 10^9.
-__global__ void dec_leaf_kernel(const uint32_t *pieces, int stride, long long first, long long npieces, int groups,
-                                char *digits)
+// ---------------------------------------------------------------------------
+// Decimal conversion of the lower levels in one kernel (dec_block_kernel).
+//
+// d_j = 10^(9 2^j) has n_j 32-bit limbs; a piece of level j is below d_j^2
+// and is stored in 2 n_j + 1 limbs (level -1: 2 limbs). Splitting a level-j
+// piece x gives its two level-(j-1) pieces q = floor(x / d_j) (the leading
+// digits) and r = x - q d_j. One CTA takes one piece of level `top` and
+// splits it level by level down to `low`, all in shared memory, then prints
+// the pieces of level low - 1 (9 2^low digits each, one thread per piece).
+//
+// A split is Barrett's reduction with mu_j = floor(beta^(2n) / d_j) (n + 1
+// limbs, beta = 2^32; HAC algorithm 14.42): q^ = floor(floor(x / beta^(n-1))
+// mu / beta^(n+1)) satisfies q - 2 <= q^ <= q for x < beta^(2n). The product
+// is summed from column n - 1 up only; the columns left out add less than
+// beta^(n+1) (a column is below (n + 1) beta^2), so the estimate q' from the
+// partial sum is q^ or q^ - 1 and r' = x - q' d_j lies in [0, 4 d_j): it is
+// exact modulo beta^(n+1), and at most three subtractions of d_j finish it.
+// The products are schoolbook column sums (4 adjacent columns per thread,
+// 96-bit accumulators, the d_j or mu_j operand slid through registers); one
+// thread per piece then carries the column blocks into limbs, subtracts and
+// corrects.
+// ---------------------------------------------------------------------------
+constexpr int kDecThreads = 128;
+constexpr int kDecCols = 4;          // product columns per thread item
+constexpr int kDecPad = kDecCols;    // zero limbs on either side of d_j and mu_j in the table
+constexpr int kDecMaxTop = 12;       // highest level whose constants exist
+constexpr int kDecLeafLog = 7;       // at most 2^7 = kDecThreads printed pieces per CTA
+constexpr unsigned ERR_E_DECIMAL = 8u;   // a split's quotient or correction out of bounds
+
+struct DecLevel {
+    int n;             // limbs of d_j
+    int stride;        // limbs per stored piece of level j
+    int nblk;          // column blocks per piece of the quotient product, ceil((n + 3) / kDecCols)
+    long long off_d;   // d_j at ctab + off_d (kDecPad zeros before and after)
+    long long off_mu;  // mu_j at ctab + off_mu, n + 1 limbs (padded likewise)
+};
+
+struct DecArgs {
+    const uint32_t *pieces;   // pieces of level `top`, stride lv[top].stride
+    long long first;          // CTA b converts piece first + b
+    int top, low;
+    int leaf_stride;          // stride of a level low - 1 piece
+    int buf_limbs;            // limbs of each of the two piece buffers
+    int blk_items;            // column blocks of the largest level (limbs / kDecCols of the block area)
+    const uint32_t *ctab;
+    DecLevel lv[kDecMaxTop + 1];
+    char *digits;             // piece i's 9 2^(top+1) digits at digits + i 9 2^(top+1)
+    unsigned *err;
+};
+
+// (s0, s1, s2) += x y as one carry chain
+__device__ __forceinline__ void dec_mac(uint32_t &s0, uint32_t &s1, uint32_t &s2, uint32_t x, uint32_t y)
 {
-    const long long i = first + blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= npieces) return;
-    uint32_t x[kLeafLimbs];
-    const uint32_t *src = pieces + i * stride;
-    int n = stride;
-    for (int j = 0; j < n; j++) x[j] = src[j];
-    while (n > 0 && x[n - 1] == 0) n--;
-    char *o = digits + i * (long long)groups * 9;
-    for (int g = groups - 1; g >= 0; g--) {
-        uint64_t rem = 0;
-        for (int j = n - 1; j >= 0; j--) {
-            const uint64_t cur = (rem << 32) | x[j];
-            x[j] = (uint32_t)(cur / 1000000000u);
-            rem = cur % 1000000000u;
+    asm("mad.lo.cc.u32 %0, %3, %4, %0;\n\t"
+        "madc.hi.cc.u32 %1, %3, %4, %1;\n\t"
+        "addc.u32 %2, %2, 0;"
+        : "+r"(s0), "+r"(s1), "+r"(s2)
+        : "r"(x), "r"(y));
+}
+
+// Columns c0 .. c0 + kDecCols - 1 of a (na limbs, shared memory) times b (nb
+// limbs, global, zero padded by kDecPad on both sides): their sum
+// sum_k col_k beta^k as kDecCols limbs at L and a two-limb carry at K
+// (below beta^2 for na < 2^30).
+__device__ __forceinline__ void dec_colblock(const uint32_t *a, int na, const uint32_t *__restrict__ b, int nb, int c0,
+                                             uint32_t *L, uint32_t *K)
+{
+    uint32_t s0[kDecCols], s1[kDecCols], s2[kDecCols];
+#pragma unroll
+    for (int k = 0; k < kDecCols; k++) s0[k] = s1[k] = s2[k] = 0;
+    const int ihi = min(c0 + kDecCols - 1, na - 1), ilo = max(0, c0 - nb + 1);
+    if (ihi >= ilo) {
+        uint32_t w[kDecCols];   // w[k] = b[c0 + k - i]
+#pragma unroll
+        for (int k = 0; k < kDecCols; k++) w[k] = __ldg(b + (c0 + k - ihi));
+        for (int i = ihi; i >= ilo; --i) {
+            const uint32_t ai = a[i];
+#pragma unroll
+            for (int k = 0; k < kDecCols; k++) dec_mac(s0[k], s1[k], s2[k], ai, w[k]);
+#pragma unroll
+            for (int k = 0; k + 1 < kDecCols; k++) w[k] = w[k + 1];
+            w[kDecCols - 1] = __ldg(b + (c0 + kDecCols - i));
         }
-        while (n > 0 && x[n - 1] == 0) n--;
-        uint32_t r = (uint32_t)rem;
-        for (int d = 8; d >= 0; d--) {
-            o[g * 9 + d] = (char)('0' + r % 10u);
-            r /= 10u;
+    }
+    uint64_t cy = 0;   // carry into the current column, below 2^64
+#pragma unroll
+    for (int k = 0; k < kDecCols; k++) {
+        // v = col_k + cy < 2^96; limb = low word, carry = v >> 32
+        const uint64_t lo = (uint64_t)s0[k] + (uint32_t)cy;
+        const uint64_t hi = ((uint64_t)s2[k] << 32 | s1[k]) + (cy >> 32) + (lo >> 32);
+        L[k] = (uint32_t)lo;
+        cy = hi;
+    }
+    K[0] = (uint32_t)cy;
+    K[1] = (uint32_t)(cy >> 32);
+}
+
+// Carry a piece's column blocks into limbs, in place: block t holds
+// kDecCols limbs at L + t kDecCols and its carry at K + 2 t.
+__device__ __forceinline__ uint64_t dec_resolve(uint32_t *L, const uint32_t *K, int nblk)
+{
+    uint64_t cy = 0;
+    for (int t = 0; t < nblk; t++) {
+        uint32_t *l = L + t * kDecCols;
+        uint64_t c = cy;
+#pragma unroll
+        for (int k = 0; k < kDecCols; k++) {
+            const uint64_t v = (uint64_t)l[k] + (uint32_t)c;
+            l[k] = (uint32_t)v;
+            c = (c >> 32) + (v >> 32);
+        }
+        cy = ((uint64_t)K[2 * t + 1] << 32 | K[2 * t]) + c;
+    }
+    return cy;
+}
+
+__global__ void __launch_bounds__(kDecThreads) dec_block_kernel(const DecArgs A)
+{
+    extern __shared__ uint32_t dsm[];
+    uint32_t *cur = dsm, *nxt = dsm + A.buf_limbs;
+    uint32_t *BL = dsm + 2 * A.buf_limbs;                 // column block limbs
+    uint32_t *BK = BL + (size_t)A.blk_items * kDecCols;   // column block carries
+    const int tid = threadIdx.x;
+    const long long piece = A.first + blockIdx.x;
+    {
+        const int S = A.lv[A.top].stride;
+        const uint32_t *src = A.pieces + piece * S;
+        for (int i = tid; i < S; i += kDecThreads) cur[i] = src[i];
+    }
+    __syncthreads();
+    for (int j = A.top; j >= A.low; j--) {
+        const DecLevel lv = A.lv[j];
+        const int n = lv.n, S = lv.stride, Sc = j > 0 ? A.lv[j - 1].stride : 2, nb = lv.nblk;
+        const int m = 1 << (A.top - j);
+        const uint32_t *d = A.ctab + lv.off_d, *mu = A.ctab + lv.off_mu;
+        // quotient estimate: columns n - 1 .. of floor(x / beta^(n-1)) mu
+        for (int it = tid; it < m * nb; it += kDecThreads) {
+            const int p = it / nb, t = it - p * nb;
+            dec_colblock(cur + p * S + (n - 1), n + 1, mu, n + 1, n - 1 + t * kDecCols, BL + (size_t)it * kDecCols,
+                         BK + 2 * (size_t)it);
+        }
+        __syncthreads();
+        for (int p = tid; p < m; p += kDecThreads) {
+            uint32_t *L = BL + (size_t)p * nb * kDecCols;
+            const uint64_t over = dec_resolve(L, BK + 2 * (size_t)p * nb, nb);
+            uint32_t *q = nxt + (2 * p) * Sc;   // limb u of q' is column n + 1 + u
+            for (int u = 0; u < n; u++) q[u] = L[u + 2];
+            for (int u = n; u < Sc; u++) q[u] = 0;
+            if (over || L[n + 2]) atomicOr(A.err, ERR_E_DECIMAL);
+        }
+        __syncthreads();
+        // r' = x - q' d_j modulo beta^(n+1): columns 0 .. n of q' d_j
+        const int nbr = (n + 1 + kDecCols - 1) / kDecCols;
+        for (int it = tid; it < m * nbr; it += kDecThreads) {
+            const int p = it / nbr, t = it - p * nbr;
+            const int o = p * nb + t;
+            dec_colblock(nxt + (2 * p) * Sc, n, d, n, t * kDecCols, BL + (size_t)o * kDecCols, BK + 2 * (size_t)o);
+        }
+        __syncthreads();
+        for (int p = tid; p < m; p += kDecThreads) {
+            uint32_t *L = BL + (size_t)p * nb * kDecCols;
+            dec_resolve(L, BK + 2 * (size_t)p * nb, nbr);
+            const uint32_t *x = cur + p * S;
+            uint32_t *r = nxt + (2 * p + 1) * Sc, *q = nxt + (2 * p) * Sc;
+            uint32_t br = 0;
+            for (int u = 0; u <= n; u++) {
+                const uint64_t v = (uint64_t)x[u] - L[u] - br;
+                r[u] = (uint32_t)v;
+                br = (uint32_t)(v >> 63);
+            }
+            for (int u = n + 1; u < Sc; u++) r[u] = 0;
+            int t = 0;
+            for (;;) {   // while r' >= d_j: r' -= d_j, q' += 1
+                bool ge = r[n] != 0;
+                if (!ge) {
+                    int u = n - 1;
+                    while (u >= 0 && r[u] == __ldg(d + u)) u--;
+                    ge = u < 0 || r[u] > __ldg(d + u);
+                }
+                if (!ge) break;
+                if (t == 3) {
+                    atomicOr(A.err, ERR_E_DECIMAL);
+                    break;
+                }
+                br = 0;
+                for (int u = 0; u < n; u++) {
+                    const uint64_t v = (uint64_t)r[u] - __ldg(d + u) - br;
+                    r[u] = (uint32_t)v;
+                    br = (uint32_t)(v >> 63);
+                }
+                r[n] -= br;
+                t++;
+            }
+            for (int u = 0; t && u < n; u++) {
+                const uint64_t v = (uint64_t)q[u] + (uint32_t)t;
+                q[u] = (uint32_t)v;
+                t = (int)(v >> 32);
+            }
+        }
+        __syncthreads();
+        uint32_t *sw = cur;
+        cur = nxt;
+        nxt = sw;
+    }
+    // print the level low - 1 pieces: 9 2^low digits each, by repeated
+    // division by 10^9 in place
+    const int groups = 1 << A.low, npr = 1 << (A.top - A.low + 1), W = A.leaf_stride;
+    char *out = A.digits + piece * (9LL << (A.top + 1));
+    for (int p = tid; p < npr; p += kDecThreads) {
+        uint32_t *x = cur + p * W;
+        int nl = W;
+        while (nl > 0 && x[nl - 1] == 0) nl--;
+        char *o = out + (long long)p * groups * 9;
+        for (int g = groups - 1; g >= 0; g--) {
+            uint64_t rem = 0;
+            for (int u = nl - 1; u >= 0; u--) {
+                const uint64_t c = (rem << 32) | x[u];
+                x[u] = (uint32_t)(c / 1000000000u);
+                rem = c % 1000000000u;
+            }
+            while (nl > 0 && x[nl - 1] == 0) nl--;
+            uint32_t v = (uint32_t)rem;
+            for (int k = 8; k >= 0; k--) {
+                o[g * 9 + k] = (char)('0' + v % 10u);
+                v /= 10u;
+            }
         }
     }
 }
@@ -313,6 +516,17 @@ int batch_add_limbs(const uint32_t *const *x, const uint32_t *const *y, uint32_t
 // Host orchestration
 // ---------------------------------------------------------------------------
 namespace {
+
+struct Stopwatch {
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    double lap()
+    {
+        const auto t = std::chrono::steady_clock::now();
+        const double s = std::chrono::duration<double>(t - t0).count();
+        t0 = t;
+        return s;
+    }
+};
 
 struct EFail {
     int code;
@@ -406,6 +620,58 @@ struct DTab {
         if (p) cudaFreeAsync(p, g_st);
     }
 };
+
+// d_j = 10^(9 2^j) and mu_j = floor(beta^(2 n_j) / d_j) for j = 0 ..
+// kDecMaxTop, laid out for dec_block_kernel. They depend on nothing but j:
+// computed once per process on the host (long division, checked by
+// multiplication), uploaded per call.
+struct DecConst {
+    std::vector<uint32_t> tab;
+    DecLevel lv[kDecMaxTop + 1];
+    bn::Num d[kDecMaxTop + 1];
+};
+
+const DecConst &dec_constants()
+{
+    static DecConst C;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        bn::Num d = bn::from_u64(1000000000u);
+        for (int j = 0; j <= kDecMaxTop; j++) {
+            if (j) d = bn::mul_school(d, d);
+            const size_t n = d.size();
+            bn::Num b(2 * n + 1, 0);
+            b[2 * n] = 1;
+            const bn::Num mu = bn::div_floor(b, d);
+            const bn::Num lo = bn::mul_school(mu, d), hi = bn::add(lo, d);
+            if (mu.size() != n + 1 || bn::cmp(lo, b) > 0 || bn::cmp(hi, b) <= 0) {
+                fprintf(stderr, "gbntt: reciprocal of 10^(9 2^%d) failed its check\n", j);
+                abort();
+            }
+            DecLevel &L = C.lv[j];
+            L.n = (int)n;
+            L.stride = (int)(2 * n + 1);
+            L.nblk = (int)((n + 3 + kDecCols - 1) / kDecCols);
+            C.tab.insert(C.tab.end(), kDecPad, 0u);
+            L.off_d = (long long)C.tab.size();
+            C.tab.insert(C.tab.end(), d.begin(), d.end());
+            C.tab.insert(C.tab.end(), 2 * kDecPad, 0u);
+            L.off_mu = (long long)C.tab.size();
+            C.tab.insert(C.tab.end(), mu.begin(), mu.end());
+            C.tab.insert(C.tab.end(), kDecPad, 0u);
+            C.d[j] = d;
+        }
+    });
+    return C;
+}
+
+// Highest level dec_block_kernel takes (GBNTT_DEC_TOP, 0 .. kDecMaxTop).
+int dec_top_level()
+{
+    const char *e = getenv("GBNTT_DEC_TOP");
+    const int v = e ? atoi(e) : 11;
+    return std::max(0, std::min(kDecMaxTop, v));
+}
 
 struct Pipe {
     unsigned *d_err = nullptr;   // sticky device error bits of this call
@@ -868,6 +1134,9 @@ struct Pipe {
 
     // ---- decimal conversion (reference base_convert.c) ----
     // Decimal digits of x (no leading zeros; "0" for zero) into digits.
+    // Levels above `top` are split here, a level at a time, with batched
+    // engine products against one reciprocal; dec_block_kernel splits the
+    // levels top .. low of each piece and prints the digits.
     void to_decimal(const uint32_t *x, size_t nx, std::vector<char> &digits)
     {
         nx = trim_top(x, nx);
@@ -875,66 +1144,95 @@ struct Pipe {
             digits.assign(1, '0');
             return;
         }
-        const uint32_t top = read_limb(x + nx - 1);
-        const double bits = 32.0 * (double)(nx - 1) + (32 - __builtin_clz(top));
+        const uint32_t topl = read_limb(x + nx - 1);
+        const double bits = 32.0 * (double)(nx - 1) + (32 - __builtin_clz(topl));
         const long long dub = (long long)floor(bits * 0.30102999566398120) + 2;   // digit count upper bound
         int J = 0;
         while (9LL << (J + 1) < dub) J++;
-        const int jl = std::min(J + 1, 6);        // leaf pieces: 9 * 2^jl digits
         const long long TD = 9LL << (J + 1);      // padded digit count
         const long long Z = TD - dub;             // leading digits known to be zero
-        const long long LD = 9LL << jl;
-        const long long nleaf = 1LL << (J + 1 - jl);
+        const int top = std::min(J, dec_top_level());
+        const int low = std::max(0, top - (kDecLeafLog - 1));
+        const DecConst &K = dec_constants();
         DTab<char> dig((size_t)TD);
-        if (jl == J + 1) {   // one leaf: x itself
-            if (nx > (size_t)kLeafLimbs) efail(GBNTT_ERR_SIZE, "decimal leaf too large");
-            dec_leaf_kernel<<<1, 32, 0, g_st>>>(x, (int)nx, 0, 1, (int)(1 << jl), dig.p);
+        // d_j = 10^(9 2^j), nd_j limbs; pieces of level j are below d_j^2 and
+        // stored at stride 2 nd_j + 1
+        std::vector<DBuf> pw(J + 1);
+        std::vector<size_t> nd(J + 1, 0);
+        nd[top] = K.d[top].size();
+        pw[top] = upload(K.d[top], nd[top]);
+        for (int j = top + 1; j <= J; j++) {
+            pw[j].alloc(2 * nd[j - 1]);
+            mul(pw[j].p, pw[j - 1].p, nd[j - 1], pw[j - 1].p, nd[j - 1]);
+            nd[j] = trim_top(pw[j].p, 2 * nd[j - 1]);
+        }
+        auto stride = [&](int j) -> size_t { return 2 * nd[j] + 1; };
+        DBuf lev(stride(J));
+        extract1(lev.p, stride(J), x, nx, 0);
+        const bool prof = getenv("GBNTT_E_PROFILE") != nullptr;
+        for (int j = J; j > top; j--) {
+            Stopwatch sw;
+            Divisor D;
+            make_divisor(D, pw[j].p, nd[j], nd[j]);
+            double t_recip = 0;
+            if (prof) {
+                sync();
+                t_recip = sw.lap();
+            }
+            const long long cnt = 1LL << (J - j);
+            const size_t W = stride(j), Wc = stride(j - 1);
+            DBuf child((size_t)(2 * cnt) * Wc);
+            const long long i0 = Z / (9LL << (j + 1));
+            std::vector<DivItem> items;
+            items.reserve((size_t)(cnt - i0));
+            for (long long i = i0; i < cnt; i++)
+                items.push_back({lev.p + i * W, W, child.p + 2 * i * Wc, Wc, child.p + (2 * i + 1) * Wc, Wc});
+            divide(items, D);
+            if (prof) {
+                sync();
+                fprintf(stderr, "to_decimal level %d: divisor %zu limbs, %zu pieces, reciprocal %.2f ms, "
+                        "division %.2f ms\n", j, nd[j], items.size(), t_recip * 1e3, sw.lap() * 1e3);
+            }
+            lev = std::move(child);
+            pw[j].release();
+        }
+        {
+            Stopwatch sw;
+            DBuf ct(K.tab.size());
+            ECK(cudaMemcpyAsync(ct.p, K.tab.data(), K.tab.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, g_st));
+            DecArgs a{};
+            a.pieces = lev.p;
+            a.first = Z / (9LL << (top + 1));
+            a.top = top;
+            a.low = low;
+            a.leaf_stride = low > 0 ? K.lv[low - 1].stride : 2;
+            a.ctab = ct.p;
+            for (int j = 0; j <= kDecMaxTop; j++) a.lv[j] = K.lv[j];
+            a.digits = dig.p;
+            a.err = d_err;
+            long long buf = 0, blk = 0;
+            for (int j = low - 1; j <= top; j++)
+                buf = std::max(buf, (1LL << (top - j)) * (j >= 0 ? K.lv[j].stride : 2));
+            for (int j = low; j <= top; j++) blk = std::max(blk, (1LL << (top - j)) * K.lv[j].nblk);
+            a.buf_limbs = (int)buf;
+            a.blk_items = (int)blk;
+            const size_t smem = (size_t)(2 * buf + blk * (kDecCols + 2)) * sizeof(uint32_t);
+            if (smem > 48 * 1024) {
+                int dev = 0, cap = 0;
+                ECK(cudaGetDevice(&dev));
+                ECK(cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+                if (smem > (size_t)cap) efail(GBNTT_ERR_SIZE, "decimal block of level %d needs %zu bytes of shared "
+                                              "memory (%d available)", top, smem, cap);
+                ECK(cudaFuncSetAttribute(dec_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            }
+            const long long ncta = (1LL << (J - top)) - a.first;
+            dec_block_kernel<<<(unsigned)ncta, kDecThreads, smem, g_st>>>(a);
             ECK(cudaGetLastError());
-        } else {
-            // d_j = 10^(9 2^j) for j = jl .. J; nd_j limbs; pieces of level j
-            // are below d_j^2 and stored at stride W_j = 2 nd_j + 1
-            bn::Num half, low;
-            {
-                bn::Num v = bn::from_u64(1);
-                for (int g = 0; g < (1 << (jl - 1)); g++) bn::mul_small_add(v, 1000000000u, 0);
-                half = v;
-                for (int g = 0; g < (1 << (jl - 1)); g++) bn::mul_small_add(v, 1000000000u, 0);
-                low = v;
+            if (prof) {
+                sync();
+                fprintf(stderr, "to_decimal levels %d..%d in one kernel: %lld pieces, %zu bytes shared, %.2f ms\n",
+                        top, low, ncta, smem, sw.lap() * 1e3);
             }
-            const size_t w_leaf = 2 * half.size() + 1;
-            if (w_leaf > (size_t)kLeafLimbs) efail(GBNTT_ERR_SIZE, "decimal leaf stride too large");
-            std::vector<DBuf> pw(J + 1);
-            std::vector<size_t> nd(J + 1, 0);
-            pw[jl] = upload(low, low.size());
-            nd[jl] = low.size();
-            for (int j = jl + 1; j <= J; j++) {
-                pw[j].alloc(2 * nd[j - 1]);
-                mul(pw[j].p, pw[j - 1].p, nd[j - 1], pw[j - 1].p, nd[j - 1]);
-                nd[j] = trim_top(pw[j].p, 2 * nd[j - 1]);
-            }
-            auto stride = [&](int j) -> size_t { return j >= jl ? 2 * nd[j] + 1 : w_leaf; };
-            DBuf lev(stride(J));
-            extract1(lev.p, stride(J), x, nx, 0);
-            for (int j = J; j >= jl; j--) {
-                Divisor D;
-                make_divisor(D, pw[j].p, nd[j], nd[j]);
-                const long long cnt = 1LL << (J - j);
-                const size_t W = stride(j), Wc = stride(j - 1);
-                DBuf child((size_t)(2 * cnt) * Wc);
-                const long long i0 = Z / (9LL << (j + 1));
-                std::vector<DivItem> items;
-                items.reserve((size_t)(cnt - i0));
-                for (long long i = i0; i < cnt; i++)
-                    items.push_back({lev.p + i * W, W, child.p + 2 * i * Wc, Wc, child.p + (2 * i + 1) * Wc, Wc});
-                divide(items, D);
-                lev = std::move(child);
-                pw[j].release();
-            }
-            const long long first = Z / LD;
-            const long long np = nleaf - first;
-            dec_leaf_kernel<<<(unsigned)((np + 127) / 128), 128, 0, g_st>>>(lev.p, (int)w_leaf, first, nleaf,
-                                                                              (int)(1 << jl), dig.p);
-            ECK(cudaGetLastError());
         }
         std::vector<char> all((size_t)(TD - Z));
         ECK(cudaMemcpyAsync(all.data(), dig.p + Z, all.size(), cudaMemcpyDeviceToHost, g_st));
@@ -1002,17 +1300,6 @@ struct EngineUse {
             cudaMemPoolTrimTo(pool, 0);
         if (owned) gbntt_teardown();
         g_st = nullptr;
-    }
-};
-
-struct Stopwatch {
-    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
-    double lap()
-    {
-        const auto t = std::chrono::steady_clock::now();
-        const double s = std::chrono::duration<double>(t - t0).count();
-        t0 = t;
-        return s;
     }
 };
 

@@ -94,6 +94,24 @@ def test_to_decimal(arith):
         assert arith.to_decimal(v) == str(v), v.bit_length()
 
 
+@pytest.mark.parametrize("top", ["0", "1", "4", "6", "7", "9", "11", "12"])
+def test_to_decimal_block_levels(arith, top, monkeypatch):
+    # The levels at and below GBNTT_DEC_TOP are split in shared memory by
+    # Barrett steps against 10^(9 2^j); values at the level boundaries
+    # (10^(9 2^k) +- 1), all-ones limbs (long carry and borrow chains) and
+    # multiples of the divisors (remainders of zero) at every split.
+    monkeypatch.setenv("GBNTT_DEC_TOP", top)
+    rng = random.Random(int(top) + 100)
+    vals = [1, 10 ** 9 - 1, 10 ** 18 - 1, 10 ** 18, 2 ** 64 - 1]
+    for k in [9 << 1, 9 << 4, 9 << 7, 9 << 11, 9 << 12]:
+        vals += [10 ** k - 1, 10 ** k, 10 ** k + 1, 10 ** k - 10 ** (k // 2), 7 * 10 ** (k - 1)]
+    for nl in [2, 4, 8, 15, 30, 60, 120, 240, 479, 957, 1914, 3828, 3829, 7654]:
+        vals.append((1 << (32 * nl)) - 1)
+        vals.append(_rand(rng, nl))
+    for v in vals:
+        assert arith.to_decimal(v) == str(v), (top, v.bit_length())
+
+
 def test_compute_e_small(arith, e_gold):
     head = e_gold["1000"]["head"]
     for D in [1, 2, 3, 5, 10, 39]:
