@@ -93,7 +93,26 @@ def to_decimal(v):
     buf = ctypes.create_string_buffer(cap)
     n = ctypes.c_size_t(0)
     engine._check(engine.lib().gbntt_to_decimal_u32(buf, cap, ctypes.byref(n), a.ctypes.data_as(_u32p), len(a)))
-    return buf.raw[:n.value].decode()
+    return str(memoryview(buf)[:n.value], "ascii")
+
+
+_e_buf = [None]   # output buffer reused across calls (a fresh 10^8-byte buffer costs a zero fill)
+
+
+def e_buffer(digits):
+    """A host buffer of at least digits + 2 bytes for gbntt_compute_e, kept
+    between calls."""
+    if _e_buf[0] is None or len(_e_buf[0]) < int(digits) + 2:
+        _e_buf[0] = ctypes.create_string_buffer(int(digits) + 2)
+    return _e_buf[0]
+
+
+def compute_e_raw(digits, buf):
+    """gbntt_compute_e into buf (from e_buffer); returns the 5 phase wall
+    times (tree, numerator x 10^(D-1), division, decimal, total)."""
+    ph = (ctypes.c_double * 5)()
+    engine._check(engine.lib().gbntt_compute_e(int(digits), buf, len(buf), ph))
+    return list(ph)
 
 
 def compute_e(digits, phases=False):
@@ -101,8 +120,7 @@ def compute_e(digits, phases=False):
     compute_e prints it after "e = " (main.c:340-345). With phases=True also
     returns the wall seconds (tree, numerator x 10^(D-1), division, decimal,
     total)."""
-    buf = ctypes.create_string_buffer(int(digits) + 2)
-    ph = (ctypes.c_double * 5)()
-    engine._check(engine.lib().gbntt_compute_e(int(digits), buf, int(digits) + 2, ph))
-    s = buf.raw[:int(digits) + 1].decode()
-    return (s, list(ph)) if phases else s
+    buf = e_buffer(digits)
+    ph = compute_e_raw(digits, buf)
+    s = str(memoryview(buf)[:int(digits) + 1], "ascii")
+    return (s, ph) if phases else s

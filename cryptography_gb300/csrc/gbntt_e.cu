@@ -665,6 +665,14 @@ const DecConst &dec_constants()
     return C;
 }
 
+// Reciprocals of the lower powers of ten from the one above (default), or
+// each by its own Newton iteration (GBNTT_E_DERIVE_RECIP=0).
+bool derive_reciprocals()
+{
+    const char *e = getenv("GBNTT_E_DERIVE_RECIP");
+    return !e || atoi(e) != 0;
+}
+
 // Highest level dec_block_kernel takes (GBNTT_DEC_TOP, 0 .. kDecMaxTop).
 int dec_top_level()
 {
@@ -1016,6 +1024,29 @@ struct Pipe {
         D.Y = recip_exact(T.p, k);
     }
 
+    // Divisor for d = 10^(9 2^j) from the one of d^2 = 10^(9 2^(j+1)) (k = nd
+    // on both): beta^(2n) / (d 2^s) = [beta^(2n') / (d^2 2^s')] d 2^(s'-s) /
+    // beta^(2n'-2n), so Y = floor(Y' d / 2^(32 (2n' - 2n) - s' + s)). With Y'
+    // at most two below beta^(2n') / (d^2 2^s'), the dropped part is below
+    // 2 beta^(n+1) / beta^(2n-2) < 1 (n' >= 2n - 1, n >= 4): Y is exact or
+    // one below, which leaves the quotient estimate of divide() at most two
+    // below the quotient, within its two correction rounds.
+    void derive_divisor(Divisor &D, const uint32_t *d, size_t nd, const Divisor &up)
+    {
+        if (nd < 4 || up.k != up.nd || up.nd + 1 < 2 * nd) efail(GBNTT_ERR_ARG, "divisor derivation out of range");
+        D.d = d;
+        D.nd = nd;
+        D.k = nd;
+        const uint32_t top = read_limb(d + nd - 1);
+        if (!top) efail(GBNTT_ERR_ARG, "divisor not trimmed");
+        D.s = __builtin_clz(top);
+        const size_t na = up.nd + 1 + nd;
+        DBuf A(na);
+        mul(A.p, up.Y.p, up.nd + 1, d, nd);
+        D.Y.alloc(nd + 1);
+        extract1(D.Y.p, nd + 1, A.p, na, 32LL * (long long)(2 * up.nd - 2 * nd) - up.s + D.s);
+    }
+
     struct DivItem {
         const uint32_t *x;
         size_t nx;
@@ -1133,16 +1164,23 @@ struct Pipe {
     }
 
     // ---- decimal conversion (reference base_convert.c) ----
-    // Decimal digits of x (no leading zeros; "0" for zero) into digits.
+    // Decimal digits of x (no leading zeros; "0" for zero), copied from the
+    // device straight to host memory: the leading digit to *first, the
+    // others to rest[0 ..]. Returns the digit count; fails with
+    // GBNTT_ERR_SIZE before copying when it exceeds max_digits (the count is
+    // stored in *count_out first when count_out is given).
     // Levels above `top` are split here, a level at a time, with batched
     // engine products against one reciprocal; dec_block_kernel splits the
     // levels top .. low of each piece and prints the digits.
-    void to_decimal(const uint32_t *x, size_t nx, std::vector<char> &digits)
+    size_t to_decimal(const uint32_t *x, size_t nx, char *first, char *rest, size_t max_digits,
+                      size_t *count_out = nullptr)
     {
         nx = trim_top(x, nx);
         if (nx == 0) {
-            digits.assign(1, '0');
-            return;
+            if (count_out) *count_out = 1;
+            if (max_digits < 1) efail(GBNTT_ERR_SIZE, "decimal string needs 1 digit");
+            *first = '0';
+            return 1;
         }
         const uint32_t topl = read_limb(x + nx - 1);
         const double bits = 32.0 * (double)(nx - 1) + (32 - __builtin_clz(topl));
@@ -1170,10 +1208,12 @@ struct Pipe {
         DBuf lev(stride(J));
         extract1(lev.p, stride(J), x, nx, 0);
         const bool prof = getenv("GBNTT_E_PROFILE") != nullptr;
+        Divisor up;   // the level above's divisor: its reciprocal seeds this level's
         for (int j = J; j > top; j--) {
             Stopwatch sw;
             Divisor D;
-            make_divisor(D, pw[j].p, nd[j], nd[j]);
+            if (j < J && nd[j] >= 4 && derive_reciprocals()) derive_divisor(D, pw[j].p, nd[j], up);
+            else make_divisor(D, pw[j].p, nd[j], nd[j]);
             double t_recip = 0;
             if (prof) {
                 sync();
@@ -1194,8 +1234,11 @@ struct Pipe {
                         "division %.2f ms\n", j, nd[j], items.size(), t_recip * 1e3, sw.lap() * 1e3);
             }
             lev = std::move(child);
+            up = std::move(D);
+            up.d = nullptr;   // d_j is released; Y, s and nd stay
             pw[j].release();
         }
+        up.Y.release();
         {
             Stopwatch sw;
             DBuf ct(K.tab.size());
@@ -1234,12 +1277,25 @@ struct Pipe {
                         top, low, ncta, smem, sw.lap() * 1e3);
             }
         }
-        std::vector<char> all((size_t)(TD - Z));
-        ECK(cudaMemcpyAsync(all.data(), dig.p + Z, all.size(), cudaMemcpyDeviceToHost, g_st));
+        // Z under-counts the leading zeros by at most two (the digit bound
+        // from the bit length): read a short head to find the first digit
+        const size_t avail = (size_t)(TD - Z);
+        char head[64];
+        const size_t hn = std::min(avail, sizeof head);
+        ECK(cudaMemcpyAsync(head, dig.p + Z, hn, cudaMemcpyDeviceToHost, g_st));
         sync();
         size_t lead = 0;
-        while (lead + 1 < all.size() && all[lead] == '0') lead++;
-        digits.assign(all.begin() + lead, all.end());
+        while (lead + 1 < hn && head[lead] == '0') lead++;
+        if (head[lead] == '0' && hn < avail) efail(GBNTT_ERR_DEVICE, "decimal digits start with %zu zeros", hn);
+        const size_t count = avail - lead;
+        if (count_out) *count_out = count;
+        if (count > max_digits) efail(GBNTT_ERR_SIZE, "decimal string has %zu digits, room for %zu", count, max_digits);
+        *first = head[lead];
+        if (count > 1) {
+            ECK(cudaMemcpyAsync(rest, dig.p + Z + lead + 1, count - 1, cudaMemcpyDeviceToHost, g_st));
+            sync();
+        }
+        return count;
     }
 };
 
@@ -1432,13 +1488,12 @@ int gbntt_to_decimal_u32(char *out, size_t cap, size_t *len, const uint32_t *x, 
         EngineUse eu(gbntt_max_log());
         Pipe pp;
         DBuf dx = pp.upload(bn::Num(x, x + nx), std::max<size_t>(nx, 1));
-        std::vector<char> dig;
-        pp.to_decimal(dx.p, nx, dig);
+        if (!out || cap < 2) efail(GBNTT_ERR_ARG, "output buffer needs at least 2 bytes");
+        size_t count = 0;
+        pp.to_decimal(dx.p, nx, out, out + 1, cap - 1, &count);
+        if (len) *len = count;
         pp.check_errors();
-        if (len) *len = dig.size();
-        if (dig.size() + 1 > cap) efail(GBNTT_ERR_SIZE, "decimal string needs %zu bytes", dig.size() + 1);
-        memcpy(out, dig.data(), dig.size());
-        out[dig.size()] = 0;
+        out[count] = 0;
         return GBNTT_OK;
     } catch (const EFail &f) {
         return f.code;
@@ -1491,15 +1546,14 @@ int gbntt_compute_e(long digits, char *out, size_t cap, double *phase_seconds)
         D.Y.release();
         const size_t nQ = pp.trim_top(Q.p, cq);
         ph[2] = sw.lap();
-        std::vector<char> dig;
-        pp.to_decimal(Q.p, nQ, dig);
+        // "2.718...": the leading digit, the point, then the others, copied
+        // from the device into out
+        const size_t count = pp.to_decimal(Q.p, nQ, out, out + 2, (size_t)digits);
         pp.check_errors();
         ph[3] = sw.lap();
-        if ((long)dig.size() != digits)
-            efail(GBNTT_ERR_DEVICE, "quotient has %zu decimal digits, expected %ld", dig.size(), digits);
-        out[0] = dig[0];
+        if ((long)count != digits)
+            efail(GBNTT_ERR_DEVICE, "quotient has %zu decimal digits, expected %ld", count, digits);
         out[1] = '.';
-        if (digits > 1) memcpy(out + 2, dig.data() + 1, (size_t)digits - 1);
         out[digits + 1] = 0;
         ph[4] = total.lap();
         if (phase_seconds) memcpy(phase_seconds, ph, sizeof ph);

@@ -112,6 +112,20 @@ def test_to_decimal_block_levels(arith, top, monkeypatch):
         assert arith.to_decimal(v) == str(v), (top, v.bit_length())
 
 
+@pytest.mark.parametrize("derive", ["0", "1"])
+def test_to_decimal_reciprocals(arith, derive, monkeypatch):
+    # Levels above the block kernel divide by reciprocals of 10^(9 2^j),
+    # each from its own Newton iteration (0) or derived from the level
+    # above's (1); low tops put many levels on that path.
+    monkeypatch.setenv("GBNTT_E_DERIVE_RECIP", derive)
+    rng = random.Random(31)
+    vals = [_rand(rng, 9000), (1 << (32 * 9000)) - 1, 10 ** 80000 - 1, 10 ** 73728, 10 ** 73728 - 1]
+    for top in ["2", "5", "11"]:
+        monkeypatch.setenv("GBNTT_DEC_TOP", top)
+        for v in vals:
+            assert arith.to_decimal(v) == str(v), (derive, top, v.bit_length())
+
+
 def test_compute_e_small(arith, e_gold):
     head = e_gold["1000"]["head"]
     for D in [1, 2, 3, 5, 10, 39]:
