@@ -12,10 +12,12 @@
 // GB300 design. All integers stay in HBM as 32-bit limbs; the host only
 // plans, launches and reads lengths and flags.
 //  * Product tree: leaf groups of up to 64 consecutive terms are folded by
-//    one thread each (bs_leaf_kernel: P = P k + 1, B = B k); then the tree
-//    is merged level by level, each level's 2 m products (B_L B_R and
-//    P_L B_R) going to the engine as ONE batch (gbntt_batch_mul_u32: waves
-//    of equal-length transforms), P_L B_R + P_R as one batched add kernel.
+//    one thread each (P = P k + 1, B = B k) and the first six levels of 64
+//    groups merged in shared memory by one CTA (bs_block_kernel); above
+//    that the tree is merged level by level, each level's 2 m products
+//    (B_L B_R and P_L B_R) going to the engine as ONE batch
+//    (gbntt_batch_mul_u32: waves of equal-length transforms), P_L B_R + P_R
+//    as one batched add kernel.
 //    Any tree shape gives the same P and B: P / B = sum_{k=a}^{b-1}
 //    (a-1)!/k! with B = (b-1)!/(a-1)!.
 //  * 10^(D-1) = 5^(D-1) 2^(D-1): 5^(D-1) by GPU squarings; the power of two
@@ -204,47 +206,11 @@ __global__ void cond_inc_kernel(const IncItem *items, int nitems, unsigned *erro
     if (j == it.n) atomicOr(error, ERR_E_OVERFLOW);
 }
 
-// Leaf groups of the product tree: thread i folds the terms
+// Leaf groups of the product tree: group i folds the terms
 // [a + i G, min(a + (i+1) G, b)) as P <- P k + 1, B <- B k (the reference's
-// leaf P = 1, B = a merged term by term, binary_split.c:44-51 and :60-71),
-// writing P at out + 2 i S and B at out + (2 i + 1) S (S = kLeafLimbs) and
-// their limb counts to lens[2 i], lens[2 i + 1]. The host picks G so that B
-// stays below 2^(32 (kLeafLimbs - 2)).
+// leaf P = 1, B = a merged term by term, binary_split.c:44-51 and :60-71);
+// G is picked so that a group's B stays below 2^(32 (kLeafLimbs - 2)).
 constexpr int kLeafLimbs = 64;
-
-__global__ void bs_leaf_kernel(unsigned long long a, unsigned long long b, int G, long long nleaf, uint32_t *out,
-                               long long *lens)
-{
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= nleaf) return;
-    const unsigned long long lo = a + (unsigned long long)i * (unsigned long long)G;
-    const unsigned long long hi = lo + G < b ? lo + G : b;
-    uint32_t p[kLeafLimbs], q[kLeafLimbs];
-    int np = 0, nq = 1;
-    q[0] = 1;
-    for (unsigned long long k = lo; k < hi; k++) {
-        const uint32_t m = (uint32_t)k;
-        uint64_t c = 1;
-        for (int j = 0; j < np; j++) {
-            c += (uint64_t)p[j] * m;
-            p[j] = (uint32_t)c;
-            c >>= 32;
-        }
-        if (c && np < kLeafLimbs) p[np++] = (uint32_t)c;
-        c = 0;
-        for (int j = 0; j < nq; j++) {
-            c += (uint64_t)q[j] * m;
-            q[j] = (uint32_t)c;
-            c >>= 32;
-        }
-        if (c && nq < kLeafLimbs) q[nq++] = (uint32_t)c;
-    }
-    uint32_t *P = out + 2 * i * kLeafLimbs, *B = P + kLeafLimbs;
-    for (int j = 0; j < np; j++) P[j] = p[j];
-    for (int j = 0; j < nq; j++) B[j] = q[j];
-    lens[2 * i] = np;
-    lens[2 * i + 1] = nq;
-}
 
 // ---------------------------------------------------------------------------
 // Decimal conversion of the lower levels in one kernel (dec_block_kernel).
@@ -307,9 +273,11 @@ __device__ __forceinline__ void dec_mac(uint32_t &s0, uint32_t &s1, uint32_t &s2
 }
 
 // Columns c0 .. c0 + kDecCols - 1 of a (na limbs, shared memory) times b (nb
-// limbs, global, zero padded by kDecPad on both sides): their sum
+// limbs, zero padded by kDecPad on both sides; global memory when
+// B_GLOBAL, else shared): their sum
 // sum_k col_k beta^k as kDecCols limbs at L and a two-limb carry at K
 // (below beta^2 for na < 2^30).
+template <bool B_GLOBAL = true>
 __device__ __forceinline__ void dec_colblock(const uint32_t *a, int na, const uint32_t *__restrict__ b, int nb, int c0,
                                              uint32_t *L, uint32_t *K)
 {
@@ -320,14 +288,14 @@ __device__ __forceinline__ void dec_colblock(const uint32_t *a, int na, const ui
     if (ihi >= ilo) {
         uint32_t w[kDecCols];   // w[k] = b[c0 + k - i]
 #pragma unroll
-        for (int k = 0; k < kDecCols; k++) w[k] = __ldg(b + (c0 + k - ihi));
+        for (int k = 0; k < kDecCols; k++) w[k] = B_GLOBAL ? __ldg(b + (c0 + k - ihi)) : b[c0 + k - ihi];
         for (int i = ihi; i >= ilo; --i) {
             const uint32_t ai = a[i];
 #pragma unroll
             for (int k = 0; k < kDecCols; k++) dec_mac(s0[k], s1[k], s2[k], ai, w[k]);
 #pragma unroll
             for (int k = 0; k + 1 < kDecCols; k++) w[k] = w[k + 1];
-            w[kDecCols - 1] = __ldg(b + (c0 + kDecCols - i));
+            w[kDecCols - 1] = B_GLOBAL ? __ldg(b + (c0 + kDecCols - i)) : b[c0 + kDecCols - i];
         }
     }
     uint64_t cy = 0;   // carry into the current column, below 2^64
@@ -473,6 +441,121 @@ __global__ void __launch_bounds__(kDecThreads) dec_block_kernel(const DecArgs A)
                 v /= 10u;
             }
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Product tree bottom in one kernel (bs_block_kernel). CTA c folds the leaf
+// groups c 2^t .. c 2^t + 2^t - 1 (G terms each; groups past the end are
+// empty: P = 0, B = 1) and merges them t levels up in
+// shared memory, P = P_L B_R + P_R, B = B_L B_R (binary_split.c:73-84),
+// with schoolbook column blocks (dec_colblock) and one thread per product
+// carrying them into limbs. A node of level l spans G 2^l terms below
+// 2^kbits, so B < 2^(kbits G 2^l) and P < 2 B: cap[l] limbs hold either.
+// Layout of a level: the P of its nodes, then their B, each node's cap[l]
+// limbs preceded by kDecCols zeros, and kDecCols zeros at the end; the
+// zeros are the padding dec_colblock reads past an operand.
+// ---------------------------------------------------------------------------
+constexpr int kBsThreads = 128;
+constexpr int kBsMaxLevels = 8;
+
+struct BsArgs {
+    unsigned long long a, b;       // terms [a, b)
+    int G, t;
+    int cap[kBsMaxLevels + 1];     // limbs of a node's P or B at level l
+    int region;                    // limbs of one level's node area
+    uint32_t *out;                 // node c: P at out + 2 c cap[t], B at out + (2 c + 1) cap[t]
+    long long *lens;               // limb counts of P and B of node c at lens[2 c], lens[2 c + 1]
+    unsigned *err;
+};
+
+__global__ void __launch_bounds__(kBsThreads) bs_block_kernel(const BsArgs A)
+{
+    extern __shared__ uint32_t bsm[];
+    uint32_t *cur = bsm, *nxt = bsm + A.region;
+    uint32_t *BK = bsm + 2 * A.region;
+    const int tid = threadIdx.x, t = A.t, n0 = 1 << t;
+    for (int i = tid; i < A.region; i += kBsThreads) cur[i] = 0;
+    __syncthreads();
+    {   // leaves: thread 2u folds P of group u, thread 2u + 1 its B
+        const int cap = A.cap[0], s0 = cap + kDecCols;
+        for (int w = tid; w < 2 * n0; w += kBsThreads) {
+            const int u = w >> 1, isB = w & 1;
+            uint32_t *x = cur + (isB ? n0 * s0 : 0) + kDecCols + u * s0;
+            const unsigned long long lo = A.a + ((unsigned long long)blockIdx.x * n0 + u) * (unsigned long long)A.G;
+            const unsigned long long hi = lo + A.G < A.b ? lo + A.G : A.b;
+            int n = 0;
+            if (isB) x[n++] = 1;
+            for (unsigned long long k = lo; k < hi; k++) {
+                const uint32_t m = (uint32_t)k;
+                uint64_t c = isB ? 0 : 1;
+                for (int j = 0; j < n; j++) {
+                    c += (uint64_t)x[j] * m;
+                    x[j] = (uint32_t)c;
+                    c >>= 32;
+                }
+                if (c) {
+                    if (n < cap) x[n++] = (uint32_t)c;
+                    else atomicOr(A.err, ERR_E_OVERFLOW);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int l = 1; l <= t; l++) {
+        const int N = 1 << (t - l);
+        const int cp = A.cap[l - 1], sp = cp + kDecCols, cl = A.cap[l], sl = cl + kDecCols;
+        const int nb = (cl + kDecCols - 1) / kDecCols;
+        for (int i = tid; i < A.region; i += kBsThreads) nxt[i] = 0;
+        __syncthreads();
+        const uint32_t *Pp = cur + kDecCols, *Bp = cur + 2 * N * sp + kDecCols;
+        uint32_t *Pn = nxt + kDecCols, *Bn = nxt + N * sl + kDecCols;
+        // product e of pair v: e = 0 B_L B_R, e = 1 P_L B_R; block t2 of it
+        for (int it = tid; it < 2 * N * nb; it += kBsThreads) {
+            const int pe = it / nb, t2 = it - pe * nb, v = pe >> 1, e = pe & 1;
+            const uint32_t *x = (e ? Pp : Bp) + (2 * v) * sp;
+            uint32_t *o = (e ? Pn : Bn) + v * sl;
+            dec_colblock<false>(x, cp, Bp + (2 * v + 1) * sp, cp, t2 * kDecCols, o + t2 * kDecCols,
+                                BK + 2 * (size_t)it);
+        }
+        __syncthreads();
+        for (int pe = tid; pe < 2 * N; pe += kBsThreads) {
+            const int v = pe >> 1, e = pe & 1;
+            uint32_t *o = (e ? Pn : Bn) + v * sl;
+            bool bad = dec_resolve(o, BK + 2 * (size_t)pe * nb, nb) != 0;
+            if (e) {   // + P_R
+                const uint32_t *r = Pp + (2 * v + 1) * sp;
+                uint32_t c = 0;
+                for (int j = 0; j < cl; j++) {
+                    const uint64_t y = (uint64_t)o[j] + (j < cp ? r[j] : 0u) + c;
+                    o[j] = (uint32_t)y;
+                    c = (uint32_t)(y >> 32);
+                }
+                bad |= c != 0;
+            }
+            for (int j = cl; j < nb * kDecCols; j++) {   // the overhang is the next node's zero padding
+                bad |= o[j] != 0;
+                o[j] = 0;
+            }
+            if (bad) atomicOr(A.err, ERR_E_OVERFLOW);
+        }
+        __syncthreads();
+        uint32_t *sw = cur;
+        cur = nxt;
+        nxt = sw;
+    }
+    const int ct = A.cap[t];
+    const uint32_t *P = cur + kDecCols, *B = cur + ct + 2 * kDecCols;
+    uint32_t *oP = A.out + 2 * (size_t)blockIdx.x * ct, *oB = oP + ct;
+    for (int i = tid; i < ct; i += kBsThreads) {
+        oP[i] = P[i];
+        oB[i] = B[i];
+    }
+    if (tid < 2) {
+        const uint32_t *x = tid ? B : P;
+        int n = ct;
+        while (n > 0 && x[n - 1] == 0) n--;
+        A.lens[2 * (size_t)blockIdx.x + tid] = n;
     }
 }
 
@@ -673,6 +756,15 @@ bool derive_reciprocals()
     return !e || atoi(e) != 0;
 }
 
+// Product tree levels merged inside bs_block_kernel (GBNTT_BS_BLOCK_LEVELS,
+// 0 .. kBsMaxLevels).
+int bs_block_levels()
+{
+    const char *e = getenv("GBNTT_BS_BLOCK_LEVELS");
+    const int v = e ? atoi(e) : 6;
+    return std::max(0, std::min(kBsMaxLevels, v));
+}
+
 // Highest level dec_block_kernel takes (GBNTT_DEC_TOP, 0 .. kDecMaxTop).
 int dec_top_level()
 {
@@ -843,24 +935,59 @@ struct Pipe {
         const int kbits = 64 - __builtin_clzll(b - 1);
         const int G = std::max(1, std::min(64, (kLeafLimbs - 2) * 32 / kbits));
         const long long nleaf = (long long)((b - a + G - 1) / G);
-        DBuf lev((size_t)nleaf * 2 * kLeafLimbs);
-        std::vector<long long> lens((size_t)nleaf * 2);
+        // the first t levels in shared memory (bs_block_kernel), 2^t groups per CTA
+        int t = 0;
+        while (t < bs_block_levels() && (1LL << t) < nleaf) t++;
+        BsArgs ba{};
+        ba.a = a;
+        ba.b = b;
+        ba.G = G;
+        ba.t = t;
+        long long region = 0, items = 0;
+        for (int l = 0; l <= t; l++) {
+            ba.cap[l] = (int)(((long long)kbits * G << l) / 32 + 3) | 1;   // >= 2 spare limbs, odd node stride
+            const long long nodes = 1LL << (t - l), sl = ba.cap[l] + kDecCols;
+            region = std::max(region, 2 * nodes * sl + kDecCols);
+            if (l) items = std::max(items, 2 * nodes * ((ba.cap[l] + kDecCols - 1) / kDecCols));
+        }
+        ba.region = (int)region;
+        const size_t smem = (size_t)(2 * region + 2 * items) * sizeof(uint32_t);
+        if (smem > 48 * 1024) {
+            int dev = 0, cap = 0;
+            ECK(cudaGetDevice(&dev));
+            ECK(cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+            if (smem > (size_t)cap) efail(GBNTT_ERR_SIZE, "product tree block needs %zu bytes of shared memory", smem);
+            ECK(cudaFuncSetAttribute(bs_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        }
+        const long long ncta = (nleaf + (1LL << t) - 1) >> t;
+        const size_t ct = (size_t)ba.cap[t];
+        DBuf lev((size_t)ncta * 2 * ct);
+        std::vector<long long> lens((size_t)ncta * 2);
         {
-            DTab<long long> dl((size_t)nleaf * 2);
-            bs_leaf_kernel<<<(unsigned)((nleaf + 127) / 128), 128, 0, g_st>>>(a, b, G, nleaf, lev.p, dl.p);
+            Stopwatch sw;
+            DTab<long long> dl((size_t)ncta * 2);
+            ba.out = lev.p;
+            ba.lens = dl.p;
+            ba.err = d_err;
+            bs_block_kernel<<<(unsigned)ncta, kBsThreads, smem, g_st>>>(ba);
             ECK(cudaGetLastError());
             ECK(cudaMemcpyAsync(lens.data(), dl.p, lens.size() * sizeof(long long), cudaMemcpyDeviceToHost, g_st));
             sync();
+            if (getenv("GBNTT_E_PROFILE"))
+                fprintf(stderr, "binary_split leaves and levels 1..%d in one kernel: %lld CTAs, %zu bytes shared, "
+                        "%.2f ms\n", t, ncta, smem, sw.lap() * 1e3);
         }
         struct Node {
             uint32_t *P, *B;
             size_t nP, nB;
         };
-        std::vector<Node> nodes((size_t)nleaf);
-        for (long long i = 0; i < nleaf; i++)
-            nodes[i] = {lev.p + 2 * i * kLeafLimbs, lev.p + (2 * i + 1) * kLeafLimbs, (size_t)lens[2 * i],
-                        (size_t)lens[2 * i + 1]};
+        std::vector<Node> nodes((size_t)ncta);
+        for (long long i = 0; i < ncta; i++)
+            nodes[i] = {lev.p + 2 * i * ct, lev.p + (2 * i + 1) * ct, (size_t)lens[2 * i], (size_t)lens[2 * i + 1]};
+        const bool prof = getenv("GBNTT_E_PROFILE") != nullptr;
+        int level = 0;
         while (nodes.size() > 1) {
+            Stopwatch sw;
             const size_t m = nodes.size() / 2;
             const bool odd = nodes.size() & 1;
             std::vector<size_t> capB(m), capP(m);
@@ -922,6 +1049,11 @@ struct Pipe {
             }
             nodes.swap(out);
             lev = std::move(next);
+            if (prof) {
+                sync();
+                fprintf(stderr, "binary_split level %d: %zu products, B limbs %zu, %.2f ms\n", t + ++level, 2 * m,
+                        nodes[0].nB, sw.lap() * 1e3);
+            }
         }
         const Node &r = nodes[0];
         nP = r.nP;

@@ -50,6 +50,18 @@ def test_binary_split_matches_oracle(arith, engine):
     assert engine.device_errors() == 0
 
 
+@pytest.mark.parametrize("levels", ["0", "1", "3", "6", "8"])
+def test_binary_split_block_levels(arith, engine, levels, monkeypatch):
+    # GBNTT_BS_BLOCK_LEVELS levels of the tree are merged in shared memory
+    # (groups of 64 terms, 2^levels per CTA, empty groups past the end);
+    # ranges that end mid-group, mid-CTA, and terms near 2^32.
+    monkeypatch.setenv("GBNTT_BS_BLOCK_LEVELS", levels)
+    for a, b in [(1, 2), (1, 64), (1, 65), (1, 4097), (7, 70000), (1, 300001), (123456, 123456 + 8191),
+                 ((1 << 32) - 5000, 1 << 32)]:
+        assert arith.binary_split(a, b) == eo.binary_split(a, b), (levels, a, b)
+    assert engine.device_errors() == 0
+
+
 def test_newton_reciprocal(arith):
     rng = random.Random(5)
     vals = [1, 2, 3, 5, 2 ** 31, 2 ** 32 - 1, 2 ** 32, 2 ** 32 + 1, 2 ** 64 - 1, 2 ** 64, 2 ** 95 + 12345,
