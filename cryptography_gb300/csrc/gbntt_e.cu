@@ -12,7 +12,7 @@
 // GB300 design. All integers stay in HBM as 32-bit limbs; the host only
 // plans, launches and reads lengths and flags.
 //  * Product tree: leaf groups of up to 64 consecutive terms are folded by
-//    one thread each (P = P k + 1, B = B k) and the first six levels of 64
+//    one thread each (P = P k + 1, B = B k) and the first five levels of 32
 //    groups merged in shared memory by one CTA (bs_block_kernel); above
 //    that the tree is merged level by level, each level's 2 m products
 //    (B_L B_R and P_L B_R) going to the engine as ONE batch
@@ -761,7 +761,7 @@ bool derive_reciprocals()
 int bs_block_levels()
 {
     const char *e = getenv("GBNTT_BS_BLOCK_LEVELS");
-    const int v = e ? atoi(e) : 6;
+    const int v = e ? atoi(e) : 5;
     return std::max(0, std::min(kBsMaxLevels, v));
 }
 
@@ -1187,13 +1187,21 @@ struct Pipe {
         uint32_t *r;   // nr limbs, nr >= nd + 1 (remainders before correction are below 2 d)
         size_t nr;
     };
+    // q_i = floor(x_i / d), r_i = x_i - q_i d for every item. The estimate
+    // q' = floor(floor(x / beta^(nd-1)) Y / 2^(32 (k + 1) - s)) multiplies
+    // only the dividend's top limbs (a product of about half the length).
+    // With M = 2^(32 (k + nd) - s) and M / d - 2 <= Y <= M / d (an exact or
+    // a derived reciprocal), x < M, and the dropped limbs costing less than
+    // beta^(nd-1) Y / M <= beta^(nd-1) / d <= 1: x / d - 3 < q' <= x / d.
+    // Three rounds of "if r >= d: r -= d, q += 1" finish it; a fourth
+    // comparison checks.
     void divide(const std::vector<DivItem> &items, const Divisor &D)
     {
         const size_t n = items.size();
         if (!n) return;
         size_t t1 = 0, t2 = 0, tr = 0;
         for (auto &it : items) {
-            t1 += it.nx + D.k + 1;
+            t1 += it.nx - std::min(D.nd - 1, it.nx) + D.k + 1;
             t2 += it.nq + D.nd;
             tr += it.nr;
         }
@@ -1203,11 +1211,12 @@ struct Pipe {
         std::vector<ExtractItem> ex;
         ex.reserve(n);
         size_t o = 0;
-        for (auto &it : items) {   // q' = floor(x Y / 2^(32 (k + nd) - s))
-            pr.push_back({T1.p + o, it.x, D.Y.p, it.nx, D.k + 1});
-            ex.push_back({T1.p + o, it.q, nullptr, (long long)(it.nx + D.k + 1), (long long)it.nq,
-                          32LL * (long long)(D.k + D.nd) - D.s, 0});
-            o += it.nx + D.k + 1;
+        for (auto &it : items) {   // q' = floor(floor(x / beta^(nd-1)) Y / 2^(32 (k + 1) - s))
+            const size_t drop = std::min(D.nd - 1, it.nx), nh = it.nx - drop;
+            pr.push_back({T1.p + o, it.x + drop, D.Y.p, nh, D.k + 1});
+            ex.push_back({T1.p + o, it.q, nullptr, (long long)(nh + D.k + 1), (long long)it.nq,
+                          32LL * (long long)(D.k + D.nd - drop) - D.s, 0});
+            o += nh + D.k + 1;
         }
         batch_mul(pr);
         extract(ex);
@@ -1239,7 +1248,7 @@ struct Pipe {
             inc.push_back({it.q, flags.p + i, (long long)it.nq});
             o += it.nr;
         }
-        for (int round = 0; round < 2; round++) {
+        for (int round = 0; round < 3; round++) {
             addsub(sb, true);
             extract(cp);
             cond_inc(inc);
