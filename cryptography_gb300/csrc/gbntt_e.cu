@@ -229,13 +229,15 @@ constexpr int kLeafLimbs = 64;
 // beta^(n+1) (a column is below (n + 1) beta^2), so the estimate q' from the
 // partial sum is q^ or q^ - 1 and r' = x - q' d_j lies in [0, 4 d_j): it is
 // exact modulo beta^(n+1), and at most three subtractions of d_j finish it.
-// The products are schoolbook column sums (4 adjacent columns per thread,
+// The products are schoolbook column sums (5 adjacent columns per thread,
 // 96-bit accumulators, the d_j or mu_j operand slid through registers); one
-// thread per piece then carries the column blocks into limbs, subtracts and
-// corrects.
+// warp per piece then carries the column blocks into limbs, subtracts and
+// corrects (warp_resolve, warp_addsub).
 // ---------------------------------------------------------------------------
 constexpr int kDecThreads = 128;
-constexpr int kDecCols = 4;          // product columns per thread item
+constexpr int kDecWarps = kDecThreads / 32;
+constexpr int kDecCols = 5;          // product columns per thread item; odd, so that the
+                                     // lanes' operand reads (stride kDecCols) hit distinct banks
 constexpr int kDecPad = kDecCols;    // zero limbs on either side of d_j and mu_j in the table
 constexpr int kDecMaxTop = 12;       // highest level whose constants exist
 constexpr int kDecLeafLog = 7;       // at most 2^7 = kDecThreads printed pieces per CTA
@@ -311,23 +313,100 @@ __device__ __forceinline__ void dec_colblock(const uint32_t *a, int na, const ui
     K[1] = (uint32_t)(cy >> 32);
 }
 
-// Carry a piece's column blocks into limbs, in place: block t holds
-// kDecCols limbs at L + t kDecCols and its carry at K + 2 t.
-__device__ __forceinline__ uint64_t dec_resolve(uint32_t *L, const uint32_t *K, int nblk)
+// Warp-wide carry propagation. Lane i of a chunk owns one block of limbs;
+// with G = lanes whose block generates a carry (with no carry in) and X = G
+// or lanes whose block passes a carry on (all ones, or all zeros for a
+// borrow), the carries into the lanes are (X + G) ^ X ^ G: the carry chain
+// of the sum X + G is exactly "generate, or propagate a carry from below".
+// A carry into the chunk enters as a generating lane below lane 0.
+// Returns the carries into lanes 0 .. 31 (bits 1 .. 32) and out of the
+// chunk's lane `last` (bit last + 2).
+__device__ __forceinline__ uint64_t warp_carries(bool g, bool p, uint32_t cin)
 {
-    uint64_t cy = 0;
-    for (int t = 0; t < nblk; t++) {
-        uint32_t *l = L + t * kDecCols;
-        uint64_t c = cy;
+    const uint64_t G = (uint64_t)__ballot_sync(0xffffffffu, g) << 1 | cin;
+    const uint64_t X = (uint64_t)__ballot_sync(0xffffffffu, g || p) << 1 | cin;
+    return (X + G) ^ X ^ G;
+}
+
+// Carry a product's column blocks into limbs, in place (one warp): block t
+// holds kDecCols limbs at L + t kDecCols and a carry below beta^2 into block
+// t + 1 at K + 2 t. Returns the carry out of the last block (its K plus the
+// propagated bit).
+__device__ __forceinline__ uint64_t warp_resolve(uint32_t *L, const uint32_t *K, int nblk, int lane)
+{
+    uint64_t cin = 0;   // into the chunk's first block
+    for (int b0 = 0; b0 < nblk; b0 += 32) {
+        const int b = b0 + lane, last = min(31, nblk - 1 - b0);
+        const bool act = b < nblk;
+        uint32_t v[kDecCols];
+        bool g = false, p = false;
+        if (act) {
+            uint64_t c = lane ? ((uint64_t)K[2 * (b - 1) + 1] << 32 | K[2 * (b - 1)]) : cin;
+            p = true;
+#pragma unroll
+            for (int k = 0; k < kDecCols; k++) {   // L_b + K_(b-1): a carry of 0 or 1 leaves the block
+                const uint64_t s = (uint64_t)L[b * kDecCols + k] + (uint32_t)c;
+                v[k] = (uint32_t)s;
+                c = (c >> 32) + (s >> 32);
+                p = p && v[k] == 0xffffffffu;
+            }
+            g = c != 0;
+        }
+        const uint64_t cv = warp_carries(g, p, 0);
+        if (act) {
+            uint32_t c = (uint32_t)(cv >> (lane + 1)) & 1u;
+#pragma unroll
+            for (int k = 0; k < kDecCols; k++) {
+                const uint64_t s = (uint64_t)v[k] + c;
+                L[b * kDecCols + k] = (uint32_t)s;
+                c = (uint32_t)(s >> 32);
+            }
+        }
+        const int bl = b0 + last;
+        cin = ((uint64_t)K[2 * bl + 1] << 32 | K[2 * bl]) + ((cv >> (last + 2)) & 1);
+    }
+    return cin;
+}
+
+// dst[0 .. n) = x + y or x - y modulo beta^n (one warp), x and y read as 0 at
+// or beyond nx, ny; lane i of a chunk owns limbs i kDecCols .. + kDecCols.
+// In-place use (dst == x or dst == y) is safe. Returns the carry (borrow)
+// out of limb n - 1.
+__device__ __forceinline__ uint32_t warp_addsub(uint32_t *dst, const uint32_t *x, int nx, const uint32_t *y, int ny,
+                                                int n, bool sub, int lane)
+{
+    uint32_t cin = 0;
+    for (int i0 = 0; i0 < n; i0 += 32 * kDecCols) {
+        const int i = i0 + lane * kDecCols, last = min(31, (n - 1 - i0) / kDecCols);
+        uint32_t v[kDecCols];
+        bool g = false, p = i < n;
+        uint32_t c = 0;
 #pragma unroll
         for (int k = 0; k < kDecCols; k++) {
-            const uint64_t v = (uint64_t)l[k] + (uint32_t)c;
-            l[k] = (uint32_t)v;
-            c = (c >> 32) + (v >> 32);
+            const int j = i + k;
+            if (j < n) {
+                const uint32_t a = j < nx ? x[j] : 0u, e = j < ny ? y[j] : 0u;
+                const uint64_t s = sub ? (uint64_t)a - e - c : (uint64_t)a + e + c;
+                v[k] = (uint32_t)s;
+                c = sub ? (uint32_t)(s >> 63) : (uint32_t)(s >> 32);
+                p = p && v[k] == (sub ? 0u : 0xffffffffu);
+            }
         }
-        cy = ((uint64_t)K[2 * t + 1] << 32 | K[2 * t]) + c;
+        g = c != 0;
+        const uint64_t cv = warp_carries(g, p, cin);
+        c = (uint32_t)(cv >> (lane + 1)) & 1u;
+#pragma unroll
+        for (int k = 0; k < kDecCols; k++) {
+            const int j = i + k;
+            if (j < n) {
+                const uint64_t s = sub ? (uint64_t)v[k] - c : (uint64_t)v[k] + c;
+                dst[j] = (uint32_t)s;
+                c = sub ? (uint32_t)(s >> 63) : (uint32_t)(s >> 32);
+            }
+        }
+        cin = (uint32_t)(cv >> (last + 2)) & 1u;
     }
-    return cy;
+    return cin;
 }
 
 __global__ void __launch_bounds__(kDecThreads) dec_block_kernel(const DecArgs A)
@@ -336,7 +415,7 @@ __global__ void __launch_bounds__(kDecThreads) dec_block_kernel(const DecArgs A)
     uint32_t *cur = dsm, *nxt = dsm + A.buf_limbs;
     uint32_t *BL = dsm + 2 * A.buf_limbs;                 // column block limbs
     uint32_t *BK = BL + (size_t)A.blk_items * kDecCols;   // column block carries
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long piece = A.first + blockIdx.x;
     {
         const int S = A.lv[A.top].stride;
@@ -356,13 +435,12 @@ __global__ void __launch_bounds__(kDecThreads) dec_block_kernel(const DecArgs A)
                          BK + 2 * (size_t)it);
         }
         __syncthreads();
-        for (int p = tid; p < m; p += kDecThreads) {
+        for (int p = warp; p < m; p += kDecWarps) {   // one warp per piece
             uint32_t *L = BL + (size_t)p * nb * kDecCols;
-            const uint64_t over = dec_resolve(L, BK + 2 * (size_t)p * nb, nb);
+            const uint64_t over = warp_resolve(L, BK + 2 * (size_t)p * nb, nb, lane);
             uint32_t *q = nxt + (2 * p) * Sc;   // limb u of q' is column n + 1 + u
-            for (int u = 0; u < n; u++) q[u] = L[u + 2];
-            for (int u = n; u < Sc; u++) q[u] = 0;
-            if (over || L[n + 2]) atomicOr(A.err, ERR_E_DECIMAL);
+            for (int u = lane; u < Sc; u += 32) q[u] = u < n ? L[u + 2] : 0u;
+            if (lane == 0 && (over || L[n + 2])) atomicOr(A.err, ERR_E_DECIMAL);
         }
         __syncthreads();
         // r' = x - q' d_j modulo beta^(n+1): columns 0 .. n of q' d_j
@@ -373,44 +451,31 @@ __global__ void __launch_bounds__(kDecThreads) dec_block_kernel(const DecArgs A)
             dec_colblock(nxt + (2 * p) * Sc, n, d, n, t * kDecCols, BL + (size_t)o * kDecCols, BK + 2 * (size_t)o);
         }
         __syncthreads();
-        for (int p = tid; p < m; p += kDecThreads) {
+        for (int p = warp; p < m; p += kDecWarps) {
             uint32_t *L = BL + (size_t)p * nb * kDecCols;
-            dec_resolve(L, BK + 2 * (size_t)p * nb, nbr);
+            warp_resolve(L, BK + 2 * (size_t)p * nb, nbr, lane);
             const uint32_t *x = cur + p * S;
             uint32_t *r = nxt + (2 * p + 1) * Sc, *q = nxt + (2 * p) * Sc;
-            uint32_t br = 0;
-            for (int u = 0; u <= n; u++) {
-                const uint64_t v = (uint64_t)x[u] - L[u] - br;
-                r[u] = (uint32_t)v;
-                br = (uint32_t)(v >> 63);
-            }
-            for (int u = n + 1; u < Sc; u++) r[u] = 0;
+            warp_addsub(r, x, n + 1, L, n + 1, n + 1, true, lane);   // r' = x - q' d_j mod beta^(n+1)
+            for (int u = n + 1 + lane; u < Sc; u += 32) r[u] = 0;
+            __syncwarp();
             int t = 0;
-            for (;;) {   // while r' >= d_j: r' -= d_j, q' += 1
-                bool ge = r[n] != 0;
-                if (!ge) {
-                    int u = n - 1;
-                    while (u >= 0 && r[u] == __ldg(d + u)) u--;
-                    ge = u < 0 || r[u] > __ldg(d + u);
-                }
-                if (!ge) break;
+            for (;;) {   // while r' >= d_j: r' -= d_j, q' += 1 (r' - d_j goes to the block area first)
+                const uint32_t br = warp_addsub(L, r, n + 1, d, n, n + 1, true, lane);
+                if (br) break;
                 if (t == 3) {
-                    atomicOr(A.err, ERR_E_DECIMAL);
+                    if (lane == 0) atomicOr(A.err, ERR_E_DECIMAL);
                     break;
                 }
-                br = 0;
-                for (int u = 0; u < n; u++) {
-                    const uint64_t v = (uint64_t)r[u] - __ldg(d + u) - br;
-                    r[u] = (uint32_t)v;
-                    br = (uint32_t)(v >> 63);
-                }
-                r[n] -= br;
+                __syncwarp();
+                for (int u = lane; u <= n; u += 32) r[u] = L[u];
+                __syncwarp();
                 t++;
             }
-            for (int u = 0; t && u < n; u++) {
-                const uint64_t v = (uint64_t)q[u] + (uint32_t)t;
-                q[u] = (uint32_t)v;
-                t = (int)(v >> 32);
+            if (t) {
+                if (lane == 0) L[0] = (uint32_t)t;
+                __syncwarp();
+                warp_addsub(q, q, n, L, 1, n, false, lane);
             }
         }
         __syncthreads();
@@ -449,8 +514,8 @@ __global__ void __launch_bounds__(kDecThreads) dec_block_kernel(const DecArgs A)
 // groups c 2^t .. c 2^t + 2^t - 1 (G terms each; groups past the end are
 // empty: P = 0, B = 1) and merges them t levels up in
 // shared memory, P = P_L B_R + P_R, B = B_L B_R (binary_split.c:73-84),
-// with schoolbook column blocks (dec_colblock) and one thread per product
-// carrying them into limbs. A node of level l spans G 2^l terms below
+// with schoolbook column blocks (dec_colblock) and one warp per product
+// carrying them into limbs (warp_resolve). A node of level l spans G 2^l terms below
 // 2^kbits, so B < 2^(kbits G 2^l) and P < 2 B: cap[l] limbs hold either.
 // Layout of a level: the P of its nodes, then their B, each node's cap[l]
 // limbs preceded by kDecCols zeros, and kDecCols zeros at the end; the
@@ -474,7 +539,7 @@ __global__ void __launch_bounds__(kBsThreads) bs_block_kernel(const BsArgs A)
     extern __shared__ uint32_t bsm[];
     uint32_t *cur = bsm, *nxt = bsm + A.region;
     uint32_t *BK = bsm + 2 * A.region;
-    const int tid = threadIdx.x, t = A.t, n0 = 1 << t;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, t = A.t, n0 = 1 << t;
     for (int i = tid; i < A.region; i += kBsThreads) cur[i] = 0;
     __syncthreads();
     {   // leaves: thread 2u folds P of group u, thread 2u + 1 its B
@@ -519,25 +584,16 @@ __global__ void __launch_bounds__(kBsThreads) bs_block_kernel(const BsArgs A)
                                 BK + 2 * (size_t)it);
         }
         __syncthreads();
-        for (int pe = tid; pe < 2 * N; pe += kBsThreads) {
+        for (int pe = warp; pe < 2 * N; pe += kBsThreads / 32) {   // one warp per product
             const int v = pe >> 1, e = pe & 1;
             uint32_t *o = (e ? Pn : Bn) + v * sl;
-            bool bad = dec_resolve(o, BK + 2 * (size_t)pe * nb, nb) != 0;
-            if (e) {   // + P_R
-                const uint32_t *r = Pp + (2 * v + 1) * sp;
-                uint32_t c = 0;
-                for (int j = 0; j < cl; j++) {
-                    const uint64_t y = (uint64_t)o[j] + (j < cp ? r[j] : 0u) + c;
-                    o[j] = (uint32_t)y;
-                    c = (uint32_t)(y >> 32);
-                }
-                bad |= c != 0;
-            }
-            for (int j = cl; j < nb * kDecCols; j++) {   // the overhang is the next node's zero padding
+            bool bad = warp_resolve(o, BK + 2 * (size_t)pe * nb, nb, lane) != 0;
+            if (e) bad |= warp_addsub(o, o, cl, Pp + (2 * v + 1) * sp, cp, cl, false, lane) != 0;   // + P_R
+            for (int j = cl + lane; j < nb * kDecCols; j += 32) {   // the overhang is the next node's zero padding
                 bad |= o[j] != 0;
                 o[j] = 0;
             }
-            if (bad) atomicOr(A.err, ERR_E_OVERFLOW);
+            if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(A.err, ERR_E_OVERFLOW);
         }
         __syncthreads();
         uint32_t *sw = cur;
