@@ -52,13 +52,15 @@
 namespace gbntt {
 
 constexpr unsigned ERR_E_OVERFLOW = 4u;   // conditional increment ran off the top
+constexpr unsigned ERR_E_WRAP = 16u;      // a cyclic remainder out of its bound
 
 // ---------------------------------------------------------------------------
 // Device kernels
 // ---------------------------------------------------------------------------
 
-// out = x + y or x - y (mod beta^nout) for a batch of items. Limb i of the
-// operands reads as 0 at or beyond nx / ny. Subtraction adds the complement
+// out = x + y or x - y (mod beta^nout) for a batch of items (the launch
+// picks one, or an item's sel word on the device). Limb i of the operands
+// reads as 0 at or beyond nx / ny. Subtraction adds the complement
 // of y plus one, so the carry out of the top limb is 1 exactly when x >= y;
 // that carry is stored in *flag. In-place use (out == x or out == y) is safe:
 // a limb is read and written by the same thread.
@@ -68,6 +70,8 @@ struct AddItem {
     unsigned *flag;
     long long nx, ny, nout;
     long long tile_start;
+    const uint32_t *sel = nullptr;   // when set: subtract iff (*sel != 0) == sub_if_nonzero (else the launch's mode)
+    int sub_if_nonzero = 1;
 };
 
 constexpr int kAddThreads = 256, kAddPer = 8, kAddTile = kAddThreads * kAddPer;
@@ -93,6 +97,7 @@ __global__ void __launch_bounds__(kAddThreads)
     }
     __syncthreads();
     const AddItem it = items[s_item];
+    if (it.sel) sub = ((*it.sel != 0u) ? 1 : 0) == it.sub_if_nonzero;
     const long long tile = s_t - it.tile_start;
     const long long base = tile * kAddTile + (long long)tid * K;
     uint64_t s[K];
@@ -206,11 +211,82 @@ __global__ void cond_inc_kernel(const IncItem *items, int nitems, unsigned *erro
     if (j == it.n) atomicOr(error, ERR_E_OVERFLOW);
 }
 
+// Remainders from cyclic products (Pipe::wrap_remainders). With M = beta^W
+// - 1, r = x - P (mod M) is assembled from S1 = x_lo + x_hi (carry f1),
+// S2 = P_lo + P_top (carry f2, in place in P) and D = S1 - S2 (f3 = 1 when
+// S1 >= S2, no borrow): r == D + e (mod M) with e = f1 - f2 - (1 - f3) in
+// -2 .. 1. For a remainder below beta^(W-1), D + e >= 0 (a value in
+// [-2, 0) would be congruent to one in [M - 2, M)), and D + e is r itself
+// unless it reached M or M + 1, for r = 0 or 1.
+struct WrapFix {
+    uint32_t *D;
+    const unsigned *f;   // f1, f2, f3
+    long long W;
+};
+
+// D += e, one thread per item (the carry or borrow rarely passes a limb);
+// D + 1 = beta^W is stored as 1, D = M stays (the copy reads it as 0).
+__global__ void wrap_fix_kernel(const WrapFix *items, int nitems, unsigned *error)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nitems) return;
+    const WrapFix it = items[i];
+    const int e = (int)it.f[0] - (int)it.f[1] - (1 - (int)it.f[2]);
+    if (e > 0) {
+        long long j = 0;
+        for (; j < it.W; j++)
+            if (++it.D[j] != 0) break;
+        if (j == it.W) it.D[0] = 1;
+    } else if (e < 0) {
+        uint32_t b = (uint32_t)(-e);
+        for (long long j = 0; j < it.W && b; j++) {
+            const uint32_t v = it.D[j];
+            it.D[j] = v - b;
+            b = v < b ? 1u : 0u;
+        }
+        if (b) atomicOr(error, ERR_E_WRAP);
+    }
+}
+
+struct WrapCopy {
+    const uint32_t *D;
+    uint32_t *r;
+    long long W, nr;
+    long long tile_start;   // first tile of the item; tiles of kWrapTile limbs cover [0, W)
+};
+constexpr int kWrapThreads = 256, kWrapTile = 4 * kWrapThreads;
+
+// r = D (0 when D = M, all ones), nr limbs; the limbs of D from nr up must
+// be zero.
+__global__ void __launch_bounds__(kWrapThreads)
+    wrap_copy_kernel(const WrapCopy *items, int nitems, unsigned *error)
+{
+    int lo = 0, hi = nitems - 1;
+    while (lo < hi) {   // the item whose tiles hold this block
+        const int mid = (lo + hi + 1) >> 1;
+        if (items[mid].tile_start <= (long long)blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    const WrapCopy it = items[lo];
+    const long long j0 = ((long long)blockIdx.x - it.tile_start) * kWrapTile;
+    const bool all_ones = it.D[it.W - 1] == 0xffffffffu;
+    bool bad = false;
+    for (long long j = j0 + threadIdx.x; j < j0 + kWrapTile && j < it.W; j += kWrapThreads) {
+        if (j < it.nr) it.r[j] = all_ones ? 0u : it.D[j];
+        else bad |= !all_ones && it.D[j] != 0;
+    }
+    if (bad) atomicOr(error, ERR_E_WRAP);
+}
+
 // Leaf groups of the product tree: group i folds the terms
 // [a + i G, min(a + (i+1) G, b)) as P <- P k + 1, B <- B k (the reference's
 // leaf P = 1, B = a merged term by term, binary_split.c:44-51 and :60-71);
 // G is picked so that a group's B stays below 2^(32 (kLeafLimbs - 2)).
 constexpr int kLeafLimbs = 64;
+
+// Newton reciprocals of at most this many limbs are computed exactly on the
+// host (long division) instead of by further GPU steps.
+constexpr size_t kRecipHostLimbs = 64;
 
 // ---------------------------------------------------------------------------
 // Decimal conversion of the lower levels in one kernel (dec_block_kernel).
@@ -821,6 +897,14 @@ int bs_block_levels()
     return std::max(0, std::min(kBsMaxLevels, v));
 }
 
+// Division remainders from cyclic products where their transform is shorter
+// (default), or always from full products (GBNTT_E_WRAP=0).
+bool wrap_remainders_enabled()
+{
+    const char *e = getenv("GBNTT_E_WRAP");
+    return !e || atoi(e) != 0;
+}
+
 // Highest level dec_block_kernel takes (GBNTT_DEC_TOP, 0 .. kDecMaxTop).
 int dec_top_level()
 {
@@ -976,6 +1060,79 @@ struct Pipe {
         ERC(gbntt_batch_mul_u32(c.data(), a.data(), na.data(), b.data(), nb.data(), (int)v.size(), (void *)g_st));
     }
 
+    // Products with cyclic items (wl[i] > 0: c = a b mod (beta^(2^wl) - 1),
+    // 2^wl + 3 limbs, the top 3 unfolded).
+    void batch_mul_wrap(const std::vector<Prod> &v, const std::vector<int> &wl)
+    {
+        if (v.empty()) return;
+        std::vector<uint32_t *> c(v.size());
+        std::vector<const uint32_t *> a(v.size()), b(v.size());
+        std::vector<size_t> na(v.size()), nb(v.size());
+        for (size_t i = 0; i < v.size(); i++) {
+            c[i] = v[i].c;
+            a[i] = v[i].a;
+            b[i] = v[i].b;
+            na[i] = v[i].na;
+            nb[i] = v[i].nb;
+        }
+        ERC(gbntt::batch_mul_wrap(c.data(), a.data(), na.data(), b.data(), nb.data(), wl.data(), (int)v.size(), g_st));
+    }
+
+    // r_i = x_i - P_i (mod beta^W_i - 1) for remainders known to be below
+    // beta^(W_i - 1), where P_i (W_i + 3 limbs, overwritten) is a cyclic
+    // product; x_i has at most 2 W_i limbs. r_i gets nr_i limbs (nr_i <= W_i;
+    // the remainder must fit them).
+    struct WrapItem {
+        const uint32_t *x;
+        size_t nx;
+        uint32_t *P;
+        size_t W;
+        uint32_t *r;
+        size_t nr;
+    };
+    void wrap_remainders(const std::vector<WrapItem> &v)
+    {
+        const size_t n = v.size();
+        if (!n) return;
+        size_t tot = 0;
+        for (auto &w : v) {
+            if (w.nx > 2 * w.W || w.nr > w.W) efail(GBNTT_ERR_ARG, "cyclic remainder operands out of range");
+            tot += w.W;
+        }
+        DBuf S(tot);
+        DTab<unsigned> f(3 * n);
+        std::vector<AddItem> a1, a2, a3;
+        std::vector<WrapFix> fx;
+        std::vector<WrapCopy> cp;
+        size_t o = 0;
+        long long tiles = 0;
+        for (size_t i = 0; i < n; i++) {
+            const WrapItem &w = v[i];
+            const long long W = (long long)w.W;
+            uint32_t *s1 = S.p + o;
+            a1.push_back({w.x, w.x + std::min(w.nx, w.W), s1, f.p + 3 * i, (long long)std::min(w.nx, w.W),
+                          (long long)(w.nx > w.W ? w.nx - w.W : 0), W, 0});
+            a2.push_back({w.P, w.P + w.W, w.P, f.p + 3 * i + 1, W, 3, W, 0});
+            a3.push_back({s1, w.P, s1, f.p + 3 * i + 2, W, W, W, 0});
+            fx.push_back({s1, f.p + 3 * i, W});
+            cp.push_back({s1, w.r, W, (long long)w.nr, tiles});
+            tiles += (W + kWrapTile - 1) / kWrapTile;
+            o += w.W;
+        }
+        addsub(a1, false);
+        addsub(a2, false);
+        addsub(a3, true);
+        {
+            DTab<WrapFix> d(fx);
+            wrap_fix_kernel<<<(unsigned)((n + 127) / 128), 128, 0, g_st>>>(d.p, (int)n, d_err);
+            ECK(cudaGetLastError());
+        }
+        if (tiles > 0x7fffffffLL) efail(GBNTT_ERR_SIZE, "cyclic remainders too long");
+        DTab<WrapCopy> d(cp);
+        wrap_copy_kernel<<<(unsigned)tiles, kWrapThreads, 0, g_st>>>(d.p, (int)n, d_err);
+        ECK(cudaGetLastError());
+    }
+
     // ---- binary splitting (reference binary_split.c) ----
     // P and B of [a, b) on the device, exact limb counts.
     void binary_split(unsigned long long a, unsigned long long b, DBuf &P, size_t &nP, DBuf &B, size_t &nB)
@@ -1127,38 +1284,38 @@ struct Pipe {
     //   U = T Yh, E = |beta^(k+h) - U| (< 6 beta^k), Y = Yh beta^(k-h) +- floor(Yh E / beta^(2h)).
     DBuf recip_approx(const uint32_t *T, size_t k)
     {
-        DBuf Y(k + 1);
-        if (k <= 2) {
-            uint32_t t[2] = {0, 0};
-            ECK(cudaMemcpyAsync(t, T, k * sizeof(uint32_t), cudaMemcpyDeviceToHost, g_st));
+        if (k <= kRecipHostLimbs) {   // exact on the host: floor(beta^(2k) / T)
+            bn::Num t(k), b(2 * k + 1, 0);
+            ECK(cudaMemcpyAsync(t.data(), T, k * sizeof(uint32_t), cudaMemcpyDeviceToHost, g_st));
             sync();
-            unsigned __int128 q;
-            if (k == 1) {
-                q = ((unsigned __int128)1 << 64) / t[0];
-            } else {
-                const uint64_t t64 = (uint64_t)t[0] | ((uint64_t)t[1] << 32);
-                q = (~(unsigned __int128)0) / t64;
-                if ((unsigned __int128)((q + 1) * t64) == 0) q += 1;   // t64 divides 2^128
-            }
-            uint32_t y[3] = {(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)(q >> 64)};
-            ECK(cudaMemcpyAsync(Y.p, y, (k + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, g_st));
-            sync();
-            return Y;
+            bn::trim(t);
+            if (t.empty()) efail(GBNTT_ERR_ARG, "reciprocal of zero");
+            b[2 * k] = 1;
+            return upload(bn::div_floor(b, t), k + 1);
         }
         const size_t h = k / 2 + 1;
         DBuf Yh = recip_approx(T + (k - h), h);
         DBuf U(k + h + 1);
         mul(U.p, T, k, Yh.p, h + 1);
-        const bool neg = read_limb(U.p + k + h) != 0;
+        // U >= beta^(k+h) exactly when its top limb is set; the sign picks
+        // on the device between E = U - beta^(k+h) = U mod beta^(k+1) and
+        // E = beta^(k+h) - U = -U mod beta^(k+1) (both below 6 beta^k)
+        const uint32_t *neg = U.p + k + h;
         DBuf E(k + 1);
-        if (neg) extract1(E.p, k + 1, U.p, k + h + 1, 0);              // U - beta^(k+h)
-        else add1(E.p, k + 1, nullptr, 0, U.p, k + 1, true);           // beta^(k+h) - U
-        U.release();
+        {
+            std::vector<AddItem> v{{nullptr, U.p, E.p, nullptr, 0, (long long)k + 1, (long long)k + 1, 0, neg, 0}};
+            addsub(v, true);
+        }
         DBuf M(k + h + 2);
         mul(M.p, Yh.p, h + 1, E.p, k + 1);
         E.release();
+        DBuf Y(k + 1);
         extract1(Y.p, k + 1, Yh.p, h + 1, -32LL * (long long)(k - h));   // Yh beta^(k-h)
-        add1(Y.p, k + 1, Y.p, k + 1, M.p + 2 * h, k + 2 - h, neg);
+        {   // Y -+ floor(Yh E / beta^(2h)): subtract when U was above beta^(k+h)
+            std::vector<AddItem> v{{Y.p, M.p + 2 * h, Y.p, nullptr, (long long)k + 1, (long long)(k + 2 - h),
+                                    (long long)k + 1, 0, neg, 1}};
+            addsub(v, false);
+        }
         return Y;
     }
 
@@ -1170,11 +1327,26 @@ struct Pipe {
         const bn::Num eight = bn::from_u64(8);
         DBuf c8 = upload(eight, 1);
         add1(Y.p, k + 1, Y.p, k + 1, c8.p, 1, true);                 // Y -= 8
-        DBuf Z(2 * k + 1);
-        mul(Z.p, Y.p, k + 1, T, k);
         DBuf R(k + 1), t(k + 1);
-        add1(R.p, k + 1, nullptr, 0, Z.p, k + 1, true);               // beta^(2k) - Z < 16 T
-        Z.release();
+        int lw = kMinLog, ll = kMinLog;
+        while (((size_t)1 << lw) < k + 2) lw++;
+        while (((size_t)1 << ll) < 2 * k) ll++;
+        if (wrap_remainders_enabled() && lw < ll) {
+            // beta^(2k) - Y T < 16 T < beta^(W-1) from the cyclic product
+            // Y T mod (beta^W - 1), with beta^(2k) == beta^(2k - W)
+            const size_t W = (size_t)1 << lw;
+            DBuf Z(W + 3), X(W);
+            batch_mul_wrap({{Z.p, Y.p, T, k + 1, k}}, {lw});
+            ECK(cudaMemsetAsync(X.p, 0, W * sizeof(uint32_t), g_st));
+            static const uint32_t one = 1;
+            ECK(cudaMemcpyAsync(X.p + (2 * k >= W ? 2 * k - W : 2 * k), &one, sizeof one, cudaMemcpyHostToDevice,
+                                g_st));
+            wrap_remainders({{X.p, W, Z.p, W, R.p, k + 1}});
+        } else {
+            DBuf Z(2 * k + 1);
+            mul(Z.p, Y.p, k + 1, T, k);
+            add1(R.p, k + 1, nullptr, 0, Z.p, k + 1, true);           // beta^(2k) - Z < 16 T
+        }
         DTab<unsigned> flag(1);
         for (int it = 0; it < 16; it++) {
             add1(t.p, k + 1, R.p, k + 1, T, k, true, flag.p);         // flag: R >= T
@@ -1277,19 +1449,47 @@ struct Pipe {
         batch_mul(pr);
         extract(ex);
         T1.release();
+        // r = x - q' d: modulo beta^nr from the full product, or modulo
+        // beta^W - 1 from a cyclic one (W >= nd + 2, so that the remainder,
+        // below 4 d, stays below beta^(W-1)) when that transform is shorter
+        int lw = kMinLog;
+        while (((size_t)1 << lw) < D.nd + 2) lw++;
+        const size_t W = (size_t)1 << lw;
+        std::vector<char> wrap(n);
+        t2 = 0;
+        for (size_t i = 0; i < n; i++) {
+            const DivItem &it = items[i];
+            int ll = kMinLog;
+            while (((size_t)1 << ll) < it.nq + D.nd - 1) ll++;
+            wrap[i] = wrap_remainders_enabled() && lw < ll && it.nq <= W && it.nx <= 2 * W && it.nr <= W;
+            t2 += wrap[i] ? W + 3 : it.nq + D.nd;
+        }
         DBuf T2(t2);
         pr.clear();
+        std::vector<Prod> pw;
+        std::vector<int> wl;
+        std::vector<WrapItem> wr;
         std::vector<AddItem> ad;
         ad.reserve(n);
         o = 0;
-        for (auto &it : items) {   // r = x - q' d (mod beta^nr)
-            pr.push_back({T2.p + o, it.q, D.d, it.nq, D.nd});
-            ad.push_back({it.x, T2.p + o, it.r, nullptr, (long long)it.nx, (long long)(it.nq + D.nd),
-                          (long long)it.nr, 0});
-            o += it.nq + D.nd;
+        for (size_t i = 0; i < n; i++) {
+            const DivItem &it = items[i];
+            if (wrap[i]) {
+                pw.push_back({T2.p + o, it.q, D.d, it.nq, D.nd});
+                wl.push_back(lw);
+                wr.push_back({it.x, it.nx, T2.p + o, W, it.r, it.nr});
+                o += W + 3;
+            } else {
+                pr.push_back({T2.p + o, it.q, D.d, it.nq, D.nd});
+                ad.push_back({it.x, T2.p + o, it.r, nullptr, (long long)it.nx, (long long)(it.nq + D.nd),
+                              (long long)it.nr, 0});
+                o += it.nq + D.nd;
+            }
         }
         batch_mul(pr);
+        batch_mul_wrap(pw, wl);
         addsub(ad, true);
+        wrap_remainders(wr);
         T2.release();
         DBuf Tt(tr);
         DTab<unsigned> flags(n);

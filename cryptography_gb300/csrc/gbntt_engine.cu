@@ -926,7 +926,10 @@ struct BatchItem {
     uint32_t *c;
     const uint32_t *a, *b;
     size_t na, nb;
+    size_t nc = 0;   // limbs written to c: na + nb when 0 (a cyclic product writes 2^L + 3)
 };
+
+static inline size_t out_limbs(const BatchItem &it) { return it.nc ? it.nc : it.na + it.nb; }
 
 static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
                          long long tiles, bool shared_b);
@@ -955,9 +958,9 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
         hB[k] = (uint64_t)(uintptr_t)it.b;
         hLB[k] = (uint64_t)it.nb;
         hC[k] = (uint64_t)(uintptr_t)it.c;
-        hNC[k] = (uint64_t)(it.na + it.nb);
+        hNC[k] = (uint64_t)out_limbs(it);
         hTS[k] = (uint64_t)tiles;
-        tiles += carry_tiles((long long)(it.na + it.nb));
+        tiles += carry_tiles((long long)out_limbs(it));
     }
     hTS[W] = (uint64_t)tiles;
     if ((size_t)tiles > x.n_status) {
@@ -1120,8 +1123,13 @@ static int g_batch_slot = 0;
 // product is E + O by one batched carry-propagating addition.
 constexpr size_t kSplitMinShort = 64;
 
+// wrap_log (optional): items with wrap_log[i] > 0 are cyclic products,
+// c = a b mod (beta^(2^L) - 1) at transform length 2^L = 2^wrap_log[i] (na,
+// nb <= 2^L): the transform's cyclic convolution carried into 2^L + 3
+// limbs, the top 3 limbs being the carry past limb 2^L - 1 (not folded).
 static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const size_t *na,
-                     const uint32_t *const *d_b, const size_t *nb, int count, cudaStream_t st)
+                     const uint32_t *const *d_b, const size_t *nb, int count, cudaStream_t st,
+                     const int *wrap_log = nullptr)
 {
     if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
     if (count < 0 || (count > 0 && (!d_c || !d_a || !na || !d_b || !nb))) { set_err("bad batch arguments"); return GBNTT_ERR_ARG; }
@@ -1140,6 +1148,24 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
     all.reserve(count);
     int rc = GBNTT_OK;
     for (int i = 0; i < count && rc == GBNTT_OK; i++) {
+        const int wl = wrap_log ? wrap_log[i] : 0;
+        if (wl) {
+            if (wl < kMinLog || wl > g.max_log || na[i] > ((size_t)1 << wl) || nb[i] > ((size_t)1 << wl)) {
+                set_err("cyclic batch product %d: operands of %zu and %zu limbs at 2^%d (engine 2^%d..2^%d)", i,
+                        na[i], nb[i], wl, kMinLog, g.max_log);
+                rc = GBNTT_ERR_SIZE;
+                break;
+            }
+            const size_t nc = ((size_t)1 << wl) + 3;
+            if (na[i] == 0 || nb[i] == 0) {
+                CK(cudaMemsetAsync(d_c[i], 0, nc * sizeof(uint32_t), st));
+                continue;
+            }
+            BatchItem it{d_c[i], d_a[i], d_b[i], na[i], nb[i]};
+            it.nc = nc;
+            all.push_back({wl, (long long)i, it});
+            continue;
+        }
         if (na[i] == 0 || nb[i] == 0) {
             if (na[i] + nb[i]) CK(cudaMemsetAsync(d_c[i], 0, (na[i] + nb[i]) * sizeof(uint32_t), st));
             continue;
@@ -1220,6 +1246,13 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
         }
     }
     return rc;
+}
+
+int batch_mul_wrap(uint32_t *const *d_c, const uint32_t *const *d_a, const size_t *na, const uint32_t *const *d_b,
+                   const size_t *nb, const int *wrap_log, int count, cudaStream_t st)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    return batch_mul(d_c, d_a, na, d_b, nb, count, st, wrap_log);
 }
 
 // ---------------------------------------------------------------------------
@@ -1333,9 +1366,9 @@ int srv_activation(Server *S, SrvSlot &sl, const std::vector<int> &gL,
             hB[k] = (uint64_t)(uintptr_t)it.b;
             hLB[k] = (uint64_t)it.nb;
             hC[k] = (uint64_t)(uintptr_t)it.c;
-            hNC[k] = (uint64_t)(it.na + it.nb);
+            hNC[k] = (uint64_t)out_limbs(it);
             hTS[k] = (uint64_t)t;
-            t += carry_tiles((long long)(it.na + it.nb));
+            t += carry_tiles((long long)out_limbs(it));
         }
         hTS[W] = (uint64_t)t;
         if ((size_t)t > x.n_status) { set_err("server sub-wave needs %lld carry tiles", t); return GBNTT_ERR_SIZE; }

@@ -148,6 +148,13 @@ struct NegaArgs {
 cudaError_t launch_nega_twist(const NegaArgs &a, cudaStream_t st);
 cudaError_t launch_nega_finish(const NegaArgs &a, cudaStream_t st);
 
+// Batched products as gbntt_batch_mul_u32, with cyclic items: wrap_log[i] >
+// 0 makes item i c = a b mod (beta^(2^L) - 1), L = wrap_log[i], written as
+// 2^L + 3 limbs whose top 3 are the carry past limb 2^L - 1, unfolded
+// (gbntt_engine.cu).
+int batch_mul_wrap(uint32_t *const *d_c, const uint32_t *const *d_a, const size_t *na, const uint32_t *const *d_b,
+                   const size_t *nb, const int *wrap_log, int count, cudaStream_t st);
+
 // Batched limb additions out_i = x_i + y_i over n_i limbs (gbntt_e.cu).
 int batch_add_limbs(const uint32_t *const *x, const uint32_t *const *y, uint32_t *const *out, const long long *n,
                     int count, cudaStream_t st, unsigned *err);

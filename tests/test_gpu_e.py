@@ -62,7 +62,10 @@ def test_binary_split_block_levels(arith, engine, levels, monkeypatch):
     assert engine.device_errors() == 0
 
 
-def test_newton_reciprocal(arith):
+@pytest.mark.parametrize("wrap", ["0", "1"])
+def test_newton_reciprocal(arith, wrap, monkeypatch):
+    # wrap 1: the exactness check takes beta^(2k) - Y T from a cyclic product
+    monkeypatch.setenv("GBNTT_E_WRAP", wrap)
     rng = random.Random(5)
     vals = [1, 2, 3, 5, 2 ** 31, 2 ** 32 - 1, 2 ** 32, 2 ** 32 + 1, 2 ** 64 - 1, 2 ** 64, 2 ** 95 + 12345,
             2 ** (32 * 7), 2 ** (32 * 7) - 1, 3 ** 500, 10 ** 1000, 2 ** 4095, 2 ** 4096 - 1]
@@ -74,7 +77,10 @@ def test_newton_reciprocal(arith):
         assert arith.newton_reciprocal(q) == eo.newton_reciprocal(q), q.bit_length()
 
 
-def test_div_newton(arith):
+@pytest.mark.parametrize("wrap", ["0", "1"])
+def test_div_newton(arith, wrap, monkeypatch):
+    # wrap 1: remainders from cyclic products mod beta^W - 1 where shorter
+    monkeypatch.setenv("GBNTT_E_WRAP", wrap)
     rng = random.Random(6)
     cases = [(0, 7), (5, 7), (7, 7), (8, 7), (2 ** 64, 1), (10 ** 50, 2 ** 40), (2 ** 1000 - 1, 2 ** 500)]
     for nn, nd in [(1, 1), (2, 1), (3, 2), (10, 3), (100, 50), (100, 99), (101, 51), (1000, 10), (5000, 1000),
@@ -124,12 +130,14 @@ def test_to_decimal_block_levels(arith, top, monkeypatch):
         assert arith.to_decimal(v) == str(v), (top, v.bit_length())
 
 
-@pytest.mark.parametrize("derive", ["0", "1"])
-def test_to_decimal_reciprocals(arith, derive, monkeypatch):
+@pytest.mark.parametrize("derive,wrap", [("0", "0"), ("0", "1"), ("1", "0"), ("1", "1")])
+def test_to_decimal_reciprocals(arith, derive, wrap, monkeypatch):
     # Levels above the block kernel divide by reciprocals of 10^(9 2^j),
     # each from its own Newton iteration (0) or derived from the level
-    # above's (1); low tops put many levels on that path.
+    # above's (1), with remainders from full or cyclic products; low tops
+    # put many levels on that path.
     monkeypatch.setenv("GBNTT_E_DERIVE_RECIP", derive)
+    monkeypatch.setenv("GBNTT_E_WRAP", wrap)
     rng = random.Random(31)
     vals = [_rand(rng, 9000), (1 << (32 * 9000)) - 1, 10 ** 80000 - 1, 10 ** 73728, 10 ** 73728 - 1]
     for top in ["2", "5", "11"]:
