@@ -1259,14 +1259,16 @@ int batch_mul_wrap(uint32_t *const *d_c, const uint32_t *const *d_a, const size_
 // Serving loop (continuous batching). A server thread owns K workspace
 // slots, each with its own stream, carry control words and batch tables.
 // Requests (device pointers) queue in arrival order; whenever a slot is
-// free, the server takes the oldest pending request's transform length and
-// admits, in arrival order, every pending request of that length whose
-// spectra still fit the slot (the HBM-footprint admission: 48 N bytes per
-// product against the slot's 48 cap bytes), and launches them as one wave on
-// the slot's stream. Waves in different slots overlap on the device;
-// requests that arrive meanwhile are admitted as slots free up. A request is
-// done when the server observes its wave's completion event; latency is
-// submit -> that observation. Results are bit-identical to gbntt_mul_u32.
+// free, the server admits pending requests in arrival order, of any
+// transform length, while the sum of their transform lengths fits the slot
+// (the HBM-footprint admission: 48 N bytes per product against the slot's
+// 48 cap bytes; at most kMaxBatch), and runs them as one sub-wave per
+// length, shortest first, back to back on the slot's stream
+// (srv_activation). Waves in different slots overlap on the device. The
+// server thread sleeps on a condition variable: a host callback enqueued
+// after each sub-wave (srv_done_cb) marks its requests done, the one after
+// the last sub-wave also frees the slot, and a submit wakes it. Latency is
+// submit -> that callback. Results are bit-identical to gbntt_mul_u32.
 // ---------------------------------------------------------------------------
 namespace {
 
