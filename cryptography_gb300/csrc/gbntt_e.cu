@@ -24,15 +24,18 @@
 //    is a bit shift (extract_kernel).
 //  * Division (reference newton.c): reciprocal Y = floor(beta^2k / T) of the
 //    normalised divisor by Newton iteration with precision doubling (two
-//    GPU products per step), made exact by a bounded correction; quotient
-//    q' = top bits of x Y is exact or one below, fixed by a conditional
-//    subtract (add/subtract kernel with decoupled look-back carry).
+//    GPU products per step, from an exact host division at 64 limbs), made
+//    exact by a bounded correction; the quotient estimate multiplies only
+//    the dividend's top limbs by Y and is at most three below, fixed by
+//    conditional subtracts (add/subtract kernel with decoupled look-back
+//    carry); remainders come from cyclic products where those are shorter.
 //  * Decimal conversion (reference base_convert.c, divide and conquer on
 //    powers of ten): pieces are split by d_j = 10^(9 2^j) level by level; a
 //    level's pieces are divided together (batched products against one
-//    reciprocal) and leading pieces known to be zero are skipped, down to
-//    pieces of 9 2^12 digits; below that one CTA per piece finishes the
-//    splits in shared memory and prints the digits (dec_block_kernel).
+//    reciprocal, each level's derived from the level above's) and leading
+//    pieces known to be zero are skipped, down to pieces of 9 2^12 digits;
+//    below that one CTA per piece finishes the splits in shared memory and
+//    prints the digits (dec_block_kernel).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
