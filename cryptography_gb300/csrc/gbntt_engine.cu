@@ -650,10 +650,11 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
 
 // Pointwise product of the spectra and inverse transform, in place in specA.
 // shared_b: specB holds one spectrum (2^L points) that every product of
-// the wave multiplies by.
+// the wave multiplies by; pair_b: specB holds W / 2 spectra, spectrum i
+// for products 2i and 2i + 1.
 static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, size_t stride, int L,
                    cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr, bool shared_b = false,
-                   bool skip_first = false)
+                   bool skip_first = false, bool pair_b = false)
 {
     // skip_first: the pointwise product and the innermost inverse pass were
     // done by the fused kernel (inner_fused); start at the next pass
@@ -662,6 +663,7 @@ static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, s
     PassArgs a;
     memset(&a, 0, sizeof a);
     a.other_log = shared_b ? L : 0;
+    a.other_pair_log = !shared_b && pair_b ? L : 0;
     for (int k = 0; k < ps.n; k++) {
         const int pi = ps.pi[k];
         a.data[k] = specA + k * stride;
@@ -710,7 +712,7 @@ static bool fuse_inner(int L)
 // prime, in place in specA (see ntt_inner_fused_kernel). Runs between
 // forward(..., skip_last) of both operands and inverse(..., skip_first).
 static int inner_fused(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, size_t stride, int L,
-                       cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr)
+                       cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr, bool pair_b = false)
 {
     int pl[kMaxPasses];
     const int np = plan_passes(L, pl);
@@ -727,6 +729,7 @@ static int inner_fused(const PrimeSet &ps, uint64_t *specA, const uint64_t *spec
     a.log_m = l;
     a.log_s = 0;
     a.ncols = W << (L - l);
+    a.other_pair_log = pair_b ? L : 0;   // products 2i and 2i + 1 read specB's spectrum i
     for (int k = 0; k < ps.n; k++) {
         const int pi = ps.pi[k];
         const double nbw = word_bytes(pi) * (double)((size_t)1 << L) * (double)W;
@@ -932,9 +935,9 @@ struct BatchItem {
 static inline size_t out_limbs(const BatchItem &it) { return it.nc ? it.nc : it.na + it.nb; }
 
 static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                         long long tiles, bool shared_b);
+                         long long tiles, bool shared_b, bool pair_b = false);
 static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                      long long tiles, bool shared_b);
+                      long long tiles, bool shared_b, bool pair_b = false);
 
 // One wave of W products, all of transform length 2^L, on stream st.
 static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, cudaStream_t st,
@@ -948,10 +951,15 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
              *hTS = h + 6 * W;
     long long tiles = 0;
     // every product multiplying by the same right operand (a division by a
-    // shared divisor or reciprocal): its transform is computed once
+    // shared divisor or reciprocal): its transform is computed once; products
+    // 2i and 2i + 1 multiplying by the same one (a product tree's B_L B_R and
+    // P_L B_R): one transform per pair
     bool shared_b = W > 1;
+    bool pair_b = W > 1 && W % 2 == 0;
     for (long long k = 0; k < W; k++) {
         const BatchItem &it = items[k];
+        const BatchItem &mate = items[k ^ 1];
+        if (pair_b && (it.b != mate.b || it.nb != mate.nb || it.a == it.b)) pair_b = false;
         if (it.b != items[0].b || it.nb != items[0].nb || it.a == it.b) shared_b = false;
         hA[k] = (uint64_t)(uintptr_t)it.a;
         hLA[k] = (uint64_t)it.na;
@@ -967,18 +975,24 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
         set_err("batched wave needs %lld carry tiles; workspace holds %zu", tiles, x.n_status);
         return GBNTT_ERR_SIZE;
     }
+    if (shared_b) pair_b = false;
+    if (pair_b)   // the right operands of the pairs, one table entry each
+        for (long long k = 0; k < W / 2; k++) {
+            hB[k] = (uint64_t)(uintptr_t)items[2 * k].b;
+            hLB[k] = (uint64_t)items[2 * k].nb;
+        }
     CK(cudaMemcpyAsync(dtab, h, (7 * (size_t)W + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(x.btab_ev[slot], st));
     *x.slot = slot ^ 1;
-    if (g.graphs && !g_rec_on) return wave_graph(x, dtab, W, L, st, aux_stream, tiles, shared_b);
-    return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b);
+    if (g.graphs && !g_rec_on) return wave_graph(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b);
+    return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b);
 }
 
 // The launches of one wave after its table upload: both operands' forward
 // transforms, the fused pointwise product and inverse, the batched carry
 // kernel over `tiles` carry tiles.
 static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                         long long tiles, bool shared_b)
+                         long long tiles, bool shared_b, bool pair_b)
 {
     uint64_t *specA = x.spec, *specB = x.spec + 3 * x.cap;
     const PrimeSet &ps = coef32_set();
@@ -990,15 +1004,16 @@ static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaSt
                      (const long long *)(dtab + W), aux, nullptr, false, nullptr, fused);
     if (rc) return rc;
     // shared right operand: one transform (table entry 0), read by every
-    // product's pointwise pass
-    rc = forward(ps, specB, x.cap, nullptr, 0, L, st, false, shared_b ? 1 : W, (const uint32_t *const *)(dtab + 2 * W),
-                 (const long long *)(dtab + 3 * W), aux, nullptr, false, nullptr, fused);
+    // product's pointwise pass; pairs: W / 2 transforms (entries 0 .. W/2 - 1)
+    rc = forward(ps, specB, x.cap, nullptr, 0, L, st, false, shared_b ? 1 : pair_b ? W / 2 : W,
+                 (const uint32_t *const *)(dtab + 2 * W), (const long long *)(dtab + 3 * W), aux, nullptr, false,
+                 nullptr, fused);
     if (rc) return rc;
     if (fused) {
-        rc = inner_fused(ps, specA, specB, x.cap, L, st, false, W, aux);
+        rc = inner_fused(ps, specA, specB, x.cap, L, st, false, W, aux, pair_b);
         if (rc) return rc;
     }
-    rc = inverse(ps, specA, specB, x.cap, L, st, false, W, aux, shared_b, fused);
+    rc = inverse(ps, specA, specB, x.cap, L, st, false, W, aux, shared_b, fused, pair_b);
     if (rc) return rc;
     rc = join_aux(st, aux);
     if (rc) return rc;
@@ -1064,14 +1079,15 @@ static void invalidate_wave_graphs()
 }
 
 static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                      long long tiles, bool shared_b)
+                      long long tiles, bool shared_b, bool pair_b)
 {
     const PrimeSet &ps = coef32_set();
     const long long ub = W * carry_tiles(((long long)1 << L) + 1);
-    if ((size_t)ub > x.n_status) return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b);
+    if ((size_t)ub > x.n_status) return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b);
     const bool aux = aux_used(ps, aux_stream);
     const WaveKey key{x.spec, dtab, x.ctl, x.cap, L, W,
-                      ps.n * 16 + ps.pi[0] * 4 + ps.pi[1] + (aux ? 256 : 0) + (shared_b ? 512 : 0)};
+                      ps.n * 16 + ps.pi[0] * 4 + ps.pi[1] + (aux ? 256 : 0) + (shared_b ? 512 : 0) +
+                          (pair_b ? 1024 : 0)};
     cudaGraphExec_t exec = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_wave_graphs_mu);
@@ -1079,10 +1095,10 @@ static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStrea
         exec = wg.exec;
         if (!exec && wg.runs++ == 0) exec = (cudaGraphExec_t)-1;
     }
-    if (exec == (cudaGraphExec_t)-1) return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b);
+    if (exec == (cudaGraphExec_t)-1) return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b);
     if (!exec) {
         CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        const int rc = wave_launches(x, dtab, W, L, st, aux_stream, ub, shared_b);
+        const int rc = wave_launches(x, dtab, W, L, st, aux_stream, ub, shared_b, pair_b);
         cudaGraph_t graph = nullptr;
         const cudaError_t e = cudaStreamEndCapture(st, &graph);
         if (rc != GBNTT_OK || e != cudaSuccess) {
@@ -1138,6 +1154,7 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
         int L;
         long long group;   // items of one split stay together (shared operand per wave)
         BatchItem item;
+        int paired = 0;    // with its neighbour in the batch: the same right operand, one transform
     };
     struct Split {
         uint32_t *E, *O, *c;
@@ -1206,17 +1223,36 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
         all.push_back({L, (long long)i, {d_c[i], d_a[i], d_b[i], na[i], nb[i]}});
     }
     if (rc == GBNTT_OK) {
+        // consecutive products of the batch with the same right operand and
+        // transform length (a product tree's B_L B_R, P_L B_R) run as pairs
+        // in waves of pairs only, where each pair's right operand is
+        // transformed once
+        // (runs of three or more: a batch sharing one right operand, which
+        // its wave transforms once)
+        for (size_t i = 0; i + 1 < all.size(); i++) {
+            const Keyed &u = all[i], &v = all[i + 1];
+            const bool run3 = (i > 0 && all[i - 1].item.b == u.item.b) ||
+                              (i + 2 < all.size() && all[i + 2].item.b == u.item.b);
+            if (!run3 && u.group != v.group && u.L == v.L && u.item.b == v.item.b && u.item.nb == v.item.nb &&
+                u.item.a != u.item.b && v.item.a != v.item.b && !u.item.nc && !v.item.nc) {
+                all[i].paired = all[i + 1].paired = 1;
+                i++;
+            }
+        }
         std::stable_sort(all.begin(), all.end(), [](const Keyed &x, const Keyed &y) {
-            return x.L != y.L ? x.L < y.L : x.group < y.group;
+            if (x.L != y.L) return x.L < y.L;
+            if (x.paired != y.paired) return x.paired < y.paired;
+            return x.group < y.group;
         });
         BatchCtx x{g.d_spec, g.n_max, g.d_ctl, g.n_status, g.d_btab, g.h_btab, g.btab_ev, &g_batch_slot};
         std::vector<BatchItem> items;
         size_t pos = 0;
         while (pos < all.size() && rc == GBNTT_OK) {
-            const int L = all[pos].L;
+            const int L = all[pos].L, paired = all[pos].paired;
             size_t end = pos;
-            while (end < all.size() && all[end].L == L) end++;
-            const long long wmax = std::min<long long>(kMaxBatch, (long long)(g.n_max >> L));
+            while (end < all.size() && all[end].L == L && all[end].paired == paired) end++;
+            long long wmax = std::min<long long>(kMaxBatch, (long long)(g.n_max >> L));
+            if (paired && wmax > 1) wmax &= ~1LL;   // waves split between pairs
             for (size_t w0 = pos; w0 < end && rc == GBNTT_OK; w0 += (size_t)wmax) {
                 const long long W = std::min<long long>(wmax, (long long)(end - w0));
                 items.clear();

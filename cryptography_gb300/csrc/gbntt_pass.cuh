@@ -187,6 +187,19 @@ __device__ __forceinline__ typename Field<PI>::T tile_in(const typename Field<PI
     else return *p;
 }
 
+// Position in the second spectra of element addr of the product spectra: the
+// same, within the one shared spectrum (other_log), or within the spectrum
+// a pair of products shares (other_pair_log).
+__device__ __forceinline__ long long other_index(const PassArgs &a, long long addr)
+{
+    if (a.other_log) return addr & ((1LL << a.other_log) - 1);
+    if (a.other_pair_log) {
+        const int L = a.other_pair_log;
+        return ((addr >> (L + 1)) << L) | (addr & ((1LL << L) - 1));
+    }
+    return addr;
+}
+
 // value of tile element at address addr for the load kind LD
 template <int PI, int LD>
 __device__ __forceinline__ typename Field<PI>::T load_elem(const PassArgs &a, const typename Field<PI>::T *data,
@@ -199,8 +212,7 @@ __device__ __forceinline__ typename Field<PI>::T load_elem(const PassArgs &a, co
         if constexpr (sizeof(typename F::T) == 8) return F::from_u64(limb64_residue<PI>(a, addr));
         else return F::zero();
     } else if constexpr (LD == LD_PW) {
-        const long long oaddr = a.other_log ? (addr & ((1LL << a.other_log) - 1)) : addr;
-        return F::mul(data[addr], other[oaddr]);
+        return F::mul(data[addr], other[other_index(a, addr)]);
     } else {
         return data[addr];
     }
@@ -209,7 +221,7 @@ __device__ __forceinline__ typename Field<PI>::T load_elem(const PassArgs &a, co
 // Issue (without waiting) the cp.async copies of the residue tile whose first
 // column is col0 into sm: tile element (g, m) -> sm[g*RS + m + m/B]; rows of
 // a contiguous tile beyond the pass are zero-filled with plain stores.
-template <int PI, int LOG_L, int LAYOUT>
+template <int PI, int LOG_L, int LAYOUT, bool OTHER = false>
 __device__ __forceinline__ void issue_tile_loads_from(const PassArgs &a, const typename Field<PI>::T *data,
                                                       typename Field<PI>::T *sm, long long col0)
 {
@@ -237,7 +249,7 @@ __device__ __forceinline__ void issue_tile_loads_from(const PassArgs &a, const t
             const int e = t + it * T;
             const int g = e >> LOG_L, m = e & (L - 1);
             V *d = sm + g * RS + m + (m >> LOG_B);
-            if (g < rows_left) cp_async_word<sizeof(V)>(d, data + base + e);
+            if (g < rows_left) cp_async_word<sizeof(V)>(d, data + (OTHER ? other_index(a, base + e) : base + e));
             else *d = F::zero();
         }
     }
@@ -442,9 +454,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         // words it copied (visible to it after the wait)
         const long long rows_left = a.ncols - col0;
         const long long base = col0 << LOG_L;
-        // a shared second spectrum (one operand common to the whole batch)
-        // is read at the position within its product
-        const long long omask = a.other_log ? ((1LL << a.other_log) - 1) : -1LL;
+        // a shared second spectrum (one operand common to the whole batch,
+        // or to a pair of products) is read at the position other_index gives
         V o[A];
 #pragma unroll
         for (int it = 0; it < A; it++) {
@@ -453,7 +464,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
             V *d = sm + g * RS + m + (m >> LOG_B);
             if (g < rows_left) {
                 cp_async_word<sizeof(V)>(d, data + base + e);
-                o[it] = __ldg(other + ((base + e) & omask));
+                o[it] = __ldg(other + other_index(a, base + e));
             } else {
                 *d = F::zero();
                 o[it] = F::zero();
@@ -723,7 +734,7 @@ __global__ void __launch_bounds__(kPassThreads, FusedMinBlocks<PI, LOG_L>::value
     const int t = threadIdx.x;
     // both tiles' copies in flight at once
     issue_tile_loads_from<PI, LOG_L, LAYOUT_CONTIG>(a, (const V *)a.data[F::SLOT], smA, col0);
-    if (!square) issue_tile_loads_from<PI, LOG_L, LAYOUT_CONTIG>(a, (const V *)a.other[F::SLOT], smB, col0);
+    if (!square) issue_tile_loads_from<PI, LOG_L, LAYOUT_CONTIG, true>(a, (const V *)a.other[F::SLOT], smB, col0);
     cp_async_wait_all();
     __syncthreads();
     const V *st1f = (const V *)a.tw.st1[F::SLOT] + (L - 32);

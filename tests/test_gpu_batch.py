@@ -177,3 +177,66 @@ def test_batch_uneven_products_split(engine):
             if i % 3 == 0:
                 assert np.array_equal(c, engine.mul(a, b)), i
     assert engine.device_errors() == 0
+
+
+def _run_batch_shared(engine, A, B, bidx):
+    # product i multiplies A[i] by B[bidx[i]] (one device buffer per B)
+    da, db = _upload(A), _upload(B)
+    nb = [len(B[j]) for j in bidx]
+    dc = [cudart.DeviceBuffer(max(4, 4 * (len(a) + n))) for a, n in zip(A, nb)]
+    engine.batch_mul_device([c.ptr for c in dc], [x.ptr for x in da], [len(a) for a in A],
+                            [db[j].ptr for j in bidx], nb)
+    cudart.synchronize()
+    out = [c.download(np.uint32, len(a) + n) for c, a, n in zip(dc, A, nb)]
+    for buf in da + db + dc:
+        buf.free()
+    return out
+
+
+def test_batch_pairs_sharing_right_operand(engine):
+    # Neighbours that multiply by the same right operand (a product tree's
+    # B_L B_R and P_L B_R) run as pairs whose right operand is transformed
+    # once: pairs of equal and of different left lengths, pairs whose two
+    # products land on different transform lengths (not paired), lone
+    # products between them, and a bucket of pairs longer than one wave
+    # (waves must split between pairs).
+    rng = np.random.default_rng(77)
+
+    def rnd(n):
+        return rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+
+    A, B, bidx = [], [], []
+    for k in range(60):
+        nr = int(rng.integers(1, 30000))
+        B.append(rnd(nr))
+        na1 = int(rng.integers(1, 30000))
+        na2 = na1 + int(rng.integers(-2, 3)) if k % 3 else int(rng.integers(1, 30000))
+        A += [rnd(max(1, na1)), rnd(max(1, na2))]
+        bidx += [len(B) - 1, len(B) - 1]
+        if k % 7 == 0:   # a lone product between pairs
+            A.append(rnd(int(rng.integers(1, 5000))))
+            B.append(rnd(int(rng.integers(1, 5000))))
+            bidx.append(len(B) - 1)
+        if k % 11 == 0:  # a lone product by a copy of its own right operand
+            A.append(B[-1].copy())
+            bidx.append(len(B) - 1)
+    # straddling a power of two: 4096 + 4097 - 1 = 2^13 coefficients, 4097 + 4097 - 1 above it
+    B.append(rnd(4097))
+    A += [rnd(4096), rnd(4097)]
+    bidx += [len(B) - 1, len(B) - 1]
+    # a bucket of 40 pairs of 2^20-coefficient products (16 per wave at 2^24)
+    for k in range(40):
+        B.append(rnd((1 << 19) + 3))
+        A += [rnd((1 << 19) - 7 - k), rnd((1 << 19) - 9 - k)]
+        bidx += [len(B) - 1, len(B) - 1]
+    got = _run_batch_shared(engine, A, B, bidx)
+    for i, (a, j, c) in enumerate(zip(A, bidx, got)):
+        if len(a) > (1 << 18) and i % 5:
+            continue
+        assert np.array_equal(c, engine.mul(a, B[j])), i
+    for i in range(0, len(A), 17):
+        want = np.zeros(len(A[i]) + len(B[bidx[i]]), dtype=np.uint32)
+        r = oracle.mul(A[i], B[bidx[i]])
+        want[:len(r)] = r
+        assert np.array_equal(got[i], want), i
+    assert engine.device_errors() == 0
