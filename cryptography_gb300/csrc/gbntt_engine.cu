@@ -1762,8 +1762,8 @@ static size_t limbs32(const gbntt_bigint *x)
     return n;
 }
 
-static int bigint_mul_impl(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_bigint *b, bool *guard_fail,
-                           bool *managed_fail)
+int bigint_mul_impl(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_bigint *b, bool *guard_fail,
+                    bool *managed_fail)
 {
     *guard_fail = false;
     *managed_fail = false;
@@ -1833,6 +1833,26 @@ static int bigint_mul_impl(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_b
     while (n > 0 && c->limbs[n - 1] == 0) n--;
     c->n_limbs = (int)n;
     return GBNTT_OK;
+}
+
+// ---- engine state for the reference entry points (gbntt_refabi.cu) ----
+std::recursive_mutex &engine_mutex() { return g_mu; }
+bool engine_ready() { return g.ready; }
+int engine_init(int L) { return init_impl(L); }
+int engine_max_log() { return g.max_log; }
+const char *engine_error() { return g_err; }
+int ref_log_cap() { return g_ref_cap; }
+int ref_log() { return g_ref_log; }
+void ref_begin(int max_log_n)
+{
+    g_ref_log = max_log_n;
+    g.dispatch = 0;
+}
+unsigned long &dispatch_count() { return g.dispatch; }
+cudaStream_t engine_stream() { return g.stream; }
+int mul_dev_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb, cudaStream_t st)
+{
+    return mul_dev(d_c, d_a, na, d_b, nb, st);
 }
 
 }  // namespace gbntt
@@ -2298,83 +2318,5 @@ int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log
     cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
     return forward(kSet3, d_out, (size_t)1 << log_n, d_in, n, log_n, st);
 }
-
-// ---- reference-compatible entry points --------------------------------------
-void ntt_mul_init_impl(int max_log_n)
-{
-    std::lock_guard<std::recursive_mutex> lk(g_mu);
-    if (g.ready) return;
-    int cap = g_ref_cap;
-    const char *e = getenv("NTT_MAX_LOGN");
-    if (e) { int v = atoi(e); if (v >= 3 && v <= kMaxLog - 1) cap = v; }
-    if (max_log_n < 3 || max_log_n > cap) {
-        fprintf(stderr, "ntt_mul_init: log_n=%d out of safe range [3,%d] (set NTT_MAX_LOGN to raise)\n", max_log_n,
-                cap);
-        exit(1);
-    }
-    // 64-bit coefficients of the reference = pairs of 32-bit coefficients.
-    int L = max_log_n + 1;
-    if (L < kMinLog) L = kMinLog;
-    int rc = init_impl(L);
-    if (rc) {
-        fprintf(stderr, "ntt_mul_init: %s\n", g_err);
-        exit(1);
-    }
-    g_ref_log = max_log_n;
-    g.dispatch = 0;
-}
-
-void ntt_mul_teardown_impl(void) { gbntt_teardown(); }
-
-unsigned long ntt_get_gpu_dispatch_count(void) { return g.dispatch; }
-
-void ntt_gpu_emergency_reset(void) { (void)cudaDeviceSynchronize(); }
-
-int ntt_bigint_mul_checked(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_bigint *b)
-{
-    std::lock_guard<std::recursive_mutex> lk(g_mu);
-    if (!c || !a || !b) { set_err("null BigInt"); return GBNTT_ERR_ARG; }
-    bool gf, mf;
-    return bigint_mul_impl(c, a, b, &gf, &mf);
-}
-
-void ntt_bigint_mul(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_bigint *b)
-{
-    std::lock_guard<std::recursive_mutex> lk(g_mu);
-    if (!g.ready) {
-        fprintf(stderr, "ntt_bigint_mul: call ntt_mul_init first\n");
-        exit(1);
-    }
-    bool gf = false, mf = false;
-    int rc = bigint_mul_impl(c, a, b, &gf, &mf);
-    if (rc == GBNTT_OK) return;
-    if (mf) {
-        fprintf(stderr, "%s\n", g_err);
-        abort();
-    }
-    fprintf(stderr, "ntt_bigint_mul: %s\n", g_err);
-    fflush(stderr);
-    exit(1);
-}
-
-void ntt_bigint_sqr(gbntt_bigint *c, const gbntt_bigint *a) { ntt_bigint_mul(c, a, a); }
-
-gbntt_bigint bigint_alloc_managed(int cap)
-{
-    gbntt_bigint r;
-    memset(&r, 0, sizeof r);
-    void *p = nullptr;
-    if (cap <= 0 || cudaMallocManaged(&p, (size_t)cap * sizeof(uint64_t)) != cudaSuccess) {
-        fprintf(stderr, "bigint_alloc_managed: cudaMallocManaged(%d limbs) failed\n", cap);
-        exit(1);
-    }
-    memset(p, 0, (size_t)cap * sizeof(uint64_t));
-    r.limbs = (uint64_t *)p;
-    r.cap = cap;
-    r.managed = 1;
-    return r;
-}
-
-void hip_free_limbs(uint64_t *p) { cudaFree(p); }
 
 }  // extern "C"

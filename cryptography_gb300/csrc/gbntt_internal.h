@@ -3,6 +3,9 @@
 #pragma once
 #include <stdint.h>
 #include <cuda_runtime.h>
+#include <mutex>
+
+#include "gbntt.h"
 
 namespace gbntt {
 
@@ -169,5 +172,25 @@ void set_error_message(const char *msg);
 // device, cleared on read (gbntt_noalloc.cu); *set_up = 0 when that scratch
 // was never set up on this device.
 int noalloc_read_errors(unsigned *flags, int *set_up);
+
+// Engine state and operations behind the reference-compatible entry points
+// (gbntt_refabi.cu, built once for 64-bit and once for 112-bit BigInt
+// limbs; gbntt_engine.cu).
+std::recursive_mutex &engine_mutex();
+bool engine_ready();
+int engine_init(int L);            // size the engine for 2^L 32-bit coefficients
+int engine_max_log();
+const char *engine_error();        // message of the last failure
+int ref_log_cap();                 // default cap of ntt_mul_init_impl's max_log_n
+int ref_log();                     // max_log_n of the current ntt_mul_init_impl (0: none)
+void ref_begin(int max_log_n);     // record it and zero the dispatch count
+unsigned long &dispatch_count();
+cudaStream_t engine_stream();
+// device product of 32-bit limbs (na + nb limbs written to d_c)
+int mul_dev_u32(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb, cudaStream_t st);
+// the 64-bit BigInt product behind ntt_bigint_mul (guard and managed-capacity
+// failures flagged for the caller's exit / abort)
+int bigint_mul_impl(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_bigint *b, bool *guard_fail,
+                    bool *managed_fail);
 
 }  // namespace gbntt

@@ -48,8 +48,11 @@ typedef struct {
 #define GBNTT_ERR_ALLOC       7  /* device or host allocation failed        */
 
 /* =====================================================================
- * 1. Reference-compatible entry points
+ * 1. Reference-compatible entry points (libgbntt.so: the reference's
+ *    default 64-bit limb build; libgbntt112.so exports the same names for
+ *    its LIMB_BITS=112 build, declared in gbntt_limb112.h)
  * ===================================================================== */
+#ifndef GBNTT_LIMB112_ABI
 
 /* Replaces ntt_mul_init_impl (ntt/lib/arith/ntt_mul.hip:379), reached from
  * ntt_mul_init (ntt/lib/arith/multiply.c:97). Sizes the engine for products
@@ -91,6 +94,7 @@ void ntt_bigint_sqr(gbntt_bigint *c, const gbntt_bigint *a);
 
 /* Additive: ntt_bigint_mul returning a GBNTT_* code instead of exiting. */
 int ntt_bigint_mul_checked(gbntt_bigint *c, const gbntt_bigint *a, const gbntt_bigint *b);
+#endif /* GBNTT_LIMB112_ABI */
 
 /* =====================================================================
  * 2. Native API (32-bit limbs)

@@ -124,29 +124,40 @@ DROPIN_BINARIES = {
 }
 
 
-def build_ref_dropin(gbntt_dir, force=False):
+# the reference's LIMB_BITS=112 build of the same callers (its GMP oracle
+# imports 64-bit limbs and is left out), linked against libgbntt112.so
+DROPIN_BINARIES_112 = {k.replace("_gb300", "_limb112_gb300"): v for k, v in DROPIN_BINARIES.items()
+                       if not k.startswith("test_gmp_oracle")}
+
+
+def build_ref_dropin(gbntt_dir, force=False, limb_bits=64):
     """Compile the reference's callers by path (the GPU build: no
-    COMPUTE_E_HOST, no stub) and link them against gbntt_dir/libgbntt.so.
-    Returns {binary: path} and the object files per binary, or None when the
-    reference checkout is absent. The binaries run on a machine with a GPU,
-    the reference sources and a compiler for that machine."""
+    COMPUTE_E_HOST, no stub) and link them against gbntt_dir/libgbntt.so,
+    or with limb_bits=112 compile them with -DLIMB_BITS=112 and link them
+    against gbntt_dir/libgbntt112.so. Returns {binary: path} and the object
+    files per binary, or None when the reference checkout is absent. The
+    binaries run on a machine with a GPU, the reference sources and a
+    compiler for that machine."""
     if not reference_available():
         return None
     ntt = os.path.join(REFERENCE_ROOT, "ntt")
     inc = ["-I", os.path.join(ntt, "lib"), "-I", os.path.join(ntt, "lib", "arith"),
            "-I", os.path.join(ntt, "app", "compute_e")]
-    so = os.path.join(gbntt_dir, "libgbntt.so")
+    lib = "libgbntt112.so" if limb_bits == 112 else "libgbntt.so"
+    so = os.path.join(gbntt_dir, lib)
+    defs = ["-DLIMB_BITS=112"] if limb_bits == 112 else []
+    tag = "dropin112_" if limb_bits == 112 else "dropin_"
     out, objs_of = {}, {}
     os.makedirs(REF_DIR, exist_ok=True)
-    for name, (srcs, libs) in DROPIN_BINARIES.items():
+    for name, (srcs, libs) in (DROPIN_BINARIES_112 if limb_bits == 112 else DROPIN_BINARIES).items():
         exe = os.path.join(REF_DIR, name)
         paths = [os.path.join(ntt, s_) for s_ in srcs]
-        objs = [os.path.join(REF_DIR, "dropin_" + os.path.basename(s_)[:-2] + ".o") for s_ in srcs]
+        objs = [os.path.join(REF_DIR, tag + os.path.basename(s_)[:-2] + ".o") for s_ in srcs]
         if force or _stale(exe, paths + [so, __file__]):
             for src, obj in zip(paths, objs):
-                subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-fopenmp"] + inc + ["-c", src, "-o", obj])
+                subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-fopenmp"] + defs + inc + ["-c", src, "-o", obj])
             tmp = exe + ".tmp"
-            subprocess.check_call(["gcc"] + objs + ["-L", gbntt_dir, "-l:libgbntt.so",
+            subprocess.check_call(["gcc"] + objs + ["-L", gbntt_dir, "-l:" + lib,
                                                     "-Wl,-rpath," + gbntt_dir, "-Wl,--no-undefined"] + libs +
                                   ["-o", tmp])
             os.replace(tmp, exe)

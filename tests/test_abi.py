@@ -32,6 +32,18 @@ def test_library_exports_every_declared_symbol(built_lib):
     assert set(declared_functions()) == set(engine.EXPORTS)
 
 
+def test_limb112_library_exports_the_same_symbols(built_lib):
+    # libgbntt112.so: the reference entry points for 112-bit limbs
+    # (include/gbntt_limb112.h) plus the same native API
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(HEADER), "..", "cryptography_gb300", "libgbntt112.so"))
+    h112 = open(os.path.join(os.path.dirname(HEADER), "gbntt_limb112.h")).read()
+    h112 = re.sub(r"/\*.*?\*/", "", h112, flags=re.S)
+    names = set(re.findall(r"\b([a-z_][a-z0-9_]*)\s*\(", h112)) - {"sizeof"}
+    assert {"ntt_mul_init_impl", "ntt_bigint_mul", "bigint_alloc_managed", "ntt_bigint_mul_checked"} <= names
+    missing = [n for n in sorted(names | set(declared_functions())) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
 def test_library_is_native_sm103a(built_lib):
     # the library links the CUDA runtime; nothing of the oracle is linked in
     path = engine.lib_path()

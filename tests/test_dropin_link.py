@@ -49,3 +49,22 @@ def test_reference_callers_link_against_the_library(built_lib):
     # compute_e reaches all five engine entry points (main.c:58, :243, :325
     # and multiply.c:87, :97-98)
     assert {s for s in _imports(exes["compute_e_gb300"]) if s.startswith("ntt_")} == set(STUB_SET)
+
+
+def test_reference_limb112_build_links_against_the_112_library(built_lib):
+    # The reference's LIMB_BITS=112 BigInt build (ntt/lib/arith/bigint.h:30-43)
+    # of compute_e and test_wrap_guard, compiled by path with -DLIMB_BITS=112,
+    # links against libgbntt112.so (the same entry points for 16-byte limbs).
+    lib112 = os.path.join(ROOT, "cryptography_gb300", "libgbntt112.so")
+    assert os.path.exists(lib112)
+    r = build.build_ref_dropin(os.path.join(ROOT, "cryptography_gb300"), limb_bits=112)
+    if r is None:
+        pytest.skip("reference checkout not present")
+    exes, _ = r
+    lib = ctypes.CDLL(lib112)
+    for name, exe in exes.items():
+        imported = {s for s in _imports(exe) if s.startswith("ntt_")}
+        assert imported and imported <= set(STUB_SET), (name, imported)
+        for sym in imported:
+            assert hasattr(lib, sym), (name, sym)
+    assert {s for s in _imports(exes["compute_e_limb112_gb300"]) if s.startswith("ntt_")} == set(STUB_SET)
