@@ -200,6 +200,20 @@ __device__ __forceinline__ long long other_index(const PassArgs &a, long long ad
     return addr;
 }
 
+// The second spectra for a contiguous tile [base, base + span) of the
+// product spectra: when the tile lies within one product, other_index is a
+// constant offset off over it (returns true; off = 0 without a shared
+// spectrum), else it must be applied per element (returns false).
+__device__ __forceinline__ bool other_tile_offset(const PassArgs &a, long long base, long long span, long long &off)
+{
+    off = 0;
+    const int L = a.other_log ? a.other_log : a.other_pair_log;
+    if (!L) return true;
+    if ((base >> L) != ((base + span - 1) >> L)) return false;
+    off = other_index(a, base) - base;
+    return true;
+}
+
 // value of tile element at address addr for the load kind LD
 template <int PI, int LD>
 __device__ __forceinline__ typename Field<PI>::T load_elem(const PassArgs &a, const typename Field<PI>::T *data,
@@ -244,13 +258,26 @@ __device__ __forceinline__ void issue_tile_loads_from(const PassArgs &a, const t
     } else {
         const long long rows_left = a.ncols - col0;
         const long long base = col0 << LOG_L;
+        long long off = 0;
+        if (!OTHER || other_tile_offset(a, base, (long long)G << LOG_L, off)) {
+            const V *src = data + off + base;
 #pragma unroll
-        for (int it = 0; it < A; it++) {
-            const int e = t + it * T;
-            const int g = e >> LOG_L, m = e & (L - 1);
-            V *d = sm + g * RS + m + (m >> LOG_B);
-            if (g < rows_left) cp_async_word<sizeof(V)>(d, data + (OTHER ? other_index(a, base + e) : base + e));
-            else *d = F::zero();
+            for (int it = 0; it < A; it++) {
+                const int e = t + it * T;
+                const int g = e >> LOG_L, m = e & (L - 1);
+                V *d = sm + g * RS + m + (m >> LOG_B);
+                if (g < rows_left) cp_async_word<sizeof(V)>(d, src + e);
+                else *d = F::zero();
+            }
+        } else {   // a tile over several products sharing second spectra
+#pragma unroll
+            for (int it = 0; it < A; it++) {
+                const int e = t + it * T;
+                const int g = e >> LOG_L, m = e & (L - 1);
+                V *d = sm + g * RS + m + (m >> LOG_B);
+                if (g < rows_left) cp_async_word<sizeof(V)>(d, data + other_index(a, base + e));
+                else *d = F::zero();
+            }
         }
     }
 }
@@ -457,6 +484,9 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
         // a shared second spectrum (one operand common to the whole batch,
         // or to a pair of products) is read at the position other_index gives
         V o[A];
+        long long off = 0;
+        const bool flat = other_tile_offset(a, base, (long long)G << LOG_L, off);
+        const V *osrc = other + off + base;
 #pragma unroll
         for (int it = 0; it < A; it++) {
             const int e = t + it * T;
@@ -464,7 +494,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, typename Field<PI>:
             V *d = sm + g * RS + m + (m >> LOG_B);
             if (g < rows_left) {
                 cp_async_word<sizeof(V)>(d, data + base + e);
-                o[it] = __ldg(other + other_index(a, base + e));
+                o[it] = __ldg(flat ? osrc + e : other + other_index(a, base + e));
             } else {
                 *d = F::zero();
                 o[it] = F::zero();
@@ -718,7 +748,9 @@ struct FusedMinBlocks {
 // the product spectrum: three words of traffic per point instead of seven
 // over three launches. No pass twiddle and no scale occur in these passes
 // (plans of two or more passes). a.other == a.data: a square.
-template <int PI, int LOG_L>
+// PAIRED: products 2i and 2i + 1 share the second spectrum i (a separate
+// instantiation, so that the unpaired kernel keeps its code as it is).
+template <int PI, int LOG_L, bool PAIRED>
 __global__ void __launch_bounds__(kPassThreads, FusedMinBlocks<PI, LOG_L>::value) ntt_inner_fused_kernel(PassArgs a)
 {
     extern __shared__ uint64_t smraw[];
@@ -734,7 +766,7 @@ __global__ void __launch_bounds__(kPassThreads, FusedMinBlocks<PI, LOG_L>::value
     const int t = threadIdx.x;
     // both tiles' copies in flight at once
     issue_tile_loads_from<PI, LOG_L, LAYOUT_CONTIG>(a, (const V *)a.data[F::SLOT], smA, col0);
-    if (!square) issue_tile_loads_from<PI, LOG_L, LAYOUT_CONTIG, true>(a, (const V *)a.other[F::SLOT], smB, col0);
+    if (!square) issue_tile_loads_from<PI, LOG_L, LAYOUT_CONTIG, PAIRED>(a, (const V *)a.other[F::SLOT], smB, col0);
     cp_async_wait_all();
     __syncthreads();
     const V *st1f = (const V *)a.tw.st1[F::SLOT] + (L - 32);
@@ -763,13 +795,13 @@ __global__ void __launch_bounds__(kPassThreads, FusedMinBlocks<PI, LOG_L>::value
     }
 }
 
-template <int PI, int LOG_L>
-static cudaError_t launch_inner_fused_l(const PassArgs &a, cudaStream_t st)
+template <int PI, int LOG_L, bool PAIRED>
+static cudaError_t launch_inner_fused_lp(const PassArgs &a, cudaStream_t st)
 {
     using S_ = PassShape<LOG_L, sizeof(typename Field<PI>::T)>;
     const long long gx = (a.ncols + S_::G - 1) / S_::G;
     const size_t smem = 2 * S_::SMEM;
-    auto fn = ntt_inner_fused_kernel<PI, LOG_L>;
+    auto fn = ntt_inner_fused_kernel<PI, LOG_L, PAIRED>;
     static bool attr_set = false;   // once per instantiation (before any graph capture uses it)
     if (smem > 48 * 1024 && !attr_set) {
         const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -778,6 +810,12 @@ static cudaError_t launch_inner_fused_l(const PassArgs &a, cudaStream_t st)
     }
     fn<<<(unsigned)gx, kPassThreads, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+template <int PI, int LOG_L>
+static cudaError_t launch_inner_fused_l(const PassArgs &a, cudaStream_t st)
+{
+    return a.other_pair_log ? launch_inner_fused_lp<PI, LOG_L, true>(a, st) : launch_inner_fused_lp<PI, LOG_L, false>(a, st);
 }
 
 template <int PI>
