@@ -1535,19 +1535,31 @@ struct Pipe {
         for (unsigned long long j = 0; j < v; j++) x0 *= 5;
         DBuf x = upload(bn::from_u64(x0), 2);
         n = x0 >> 32 ? 2 : 1;
+        // 5^k has floor(k log2 5) + 1 bits: below 2^40 the double product is
+        // within 1e-6 of k log2 5, so limbs_of(k) holds 5^k and the steps
+        // need no length read back from the device (one trim at the end)
+        const bool bound = e < (1ull << 40);
+        auto limbs_of = [](unsigned long long k) -> size_t {
+            return (size_t)((floor((double)k * 2.3219280948873623478703194 + 1e-6) + 1.0) / 32.0) + 1;
+        };
+        unsigned long long k = v;
         for (; i >= 0; i--) {
+            k *= 2;
+            const size_t ns = bound ? std::min(2 * n, limbs_of(k)) : 2 * n;
             DBuf y(2 * n);
             mul(y.p, x.p, n, x.p, n);
-            n = trim_top(y.p, 2 * n);
+            n = bound ? ns : trim_top(y.p, 2 * n);
             x = std::move(y);
             if ((e >> i) & 1) {
+                k += 1;
                 DBuf z(n + 1);
                 extract1(z.p, n + 1, x.p, n, -2);
                 add1(z.p, n + 1, z.p, n + 1, x.p, n, false);
-                n = trim_top(z.p, n + 1);
+                n = bound ? std::min(n + 1, limbs_of(k)) : trim_top(z.p, n + 1);
                 x = std::move(z);
             }
         }
+        n = trim_top(x.p, n);
         return x;
     }
 
