@@ -162,8 +162,9 @@ def test_compute_e_matches_reference(arith, engine, e_gold, D):
 
 
 def test_compute_e_against_oracle_odd_sizes(arith):
-    # sizes around the decimal leaf (576 digits) and level boundaries
-    for D in [575, 576, 577, 1152, 1153, 4608, 4609, 7777]:
+    # sizes around the printed decimal pieces (288 digits) and level
+    # boundaries (9 2^j digits)
+    for D in [287, 288, 289, 575, 576, 577, 1152, 1153, 4608, 4609, 7777]:
         assert arith.compute_e(D) == eo.e_string(D), D
 
 
