@@ -900,6 +900,15 @@ int bs_block_levels()
     return std::max(0, std::min(kBsMaxLevels, v));
 }
 
+// The top decimal level's reciprocal only as precise as its quotient needs,
+// from the squared reciprocal of the level below (default), or a full-length
+// Newton reciprocal (GBNTT_E_SHORT_TOP=0).
+bool short_top_reciprocal()
+{
+    const char *e = getenv("GBNTT_E_SHORT_TOP");
+    return !e || atoi(e) != 0;
+}
+
 // Division remainders from cyclic products where their transform is shorter
 // (default), or always from full products (GBNTT_E_WRAP=0).
 bool wrap_remainders_enabled()
@@ -1410,6 +1419,35 @@ struct Pipe {
         extract1(D.Y.p, nd + 1, A.p, na, 32LL * (long long)(2 * up.nd - 2 * nd) - up.s + D.s);
     }
 
+    // Divisor of the top decimal level d = 10^(9 2^J) = d'^2 for a dividend
+    // of nx limbs with the reciprocal precision the quotient needs, k = nx -
+    // nd + 2 (x 2^s < beta^(k + nd)), from the exact reciprocal Y' of the
+    // level below (made here by Newton, returned in `below` for that level):
+    // beta^(k+nd) / (d 2^s) = (beta^(2n') / (d' 2^s'))^2 / 2^(32 (4n' - k -
+    // nd) - 2s' + s), so Y = floor(Y'^2 / 2^sh); Y' is below its value by
+    // less than 1, which costs less than 2 V' / 2^sh <= 2^64 beta^(k - n')
+    // < 1 for k <= n' - 3: Y is exact or one below. False (nothing done)
+    // when the quotient needs more precision than that.
+    bool short_top_divisor(Divisor &D, const uint32_t *d, size_t nd, size_t nx, const uint32_t *d1, size_t n1,
+                           Divisor &below)
+    {
+        if (nx + 2 <= nd || n1 < 8) return false;
+        const size_t k = nx + 2 - nd;
+        if (k + 3 > n1 || nd > 2 * n1) return false;
+        make_divisor(below, d1, n1, n1);
+        D.d = d;
+        D.nd = nd;
+        D.k = k;
+        const uint32_t topl = read_limb(d + nd - 1);
+        if (!topl) efail(GBNTT_ERR_ARG, "divisor not trimmed");
+        D.s = __builtin_clz(topl);
+        DBuf A(2 * n1 + 2);
+        mul(A.p, below.Y.p, n1 + 1, below.Y.p, n1 + 1);
+        D.Y.alloc(k + 1);
+        extract1(D.Y.p, k + 1, A.p, 2 * n1 + 2, 32LL * (long long)(4 * n1 - k - nd) - 2LL * below.s + D.s);
+        return true;
+    }
+
     struct DivItem {
         const uint32_t *x;
         size_t nx;
@@ -1620,11 +1658,17 @@ struct Pipe {
         DBuf lev(stride(J));
         extract1(lev.p, stride(J), x, nx, 0);
         const bool prof = getenv("GBNTT_E_PROFILE") != nullptr;
-        Divisor up;   // the level above's divisor: its reciprocal seeds this level's
+        Divisor up;      // the level above's divisor: its reciprocal seeds this level's
+        Divisor below;   // level J - 1's, when the top level's short reciprocal was made from it
+        bool have_below = false;
         for (int j = J; j > top; j--) {
             Stopwatch sw;
             Divisor D;
-            if (j < J && nd[j] >= 4 && derive_reciprocals()) derive_divisor(D, pw[j].p, nd[j], up);
+            if (j == J && j - 1 > top && short_top_reciprocal() &&
+                short_top_divisor(D, pw[j].p, nd[j], nx, pw[j - 1].p, nd[j - 1], below))
+                have_below = true;
+            else if (j == J - 1 && have_below) D = std::move(below);
+            else if (j < J && nd[j] >= 4 && derive_reciprocals()) derive_divisor(D, pw[j].p, nd[j], up);
             else make_divisor(D, pw[j].p, nd[j], nd[j]);
             double t_recip = 0;
             if (prof) {
@@ -1637,8 +1681,9 @@ struct Pipe {
             const long long i0 = Z / (9LL << (j + 1));
             std::vector<DivItem> items;
             items.reserve((size_t)(cnt - i0));
-            for (long long i = i0; i < cnt; i++)
-                items.push_back({lev.p + i * W, W, child.p + 2 * i * Wc, Wc, child.p + (2 * i + 1) * Wc, Wc});
+            for (long long i = i0; i < cnt; i++)   // (the top piece is x itself: nx limbs, zeros above)
+                items.push_back({lev.p + i * W, j == J ? nx : W, child.p + 2 * i * Wc, Wc, child.p + (2 * i + 1) * Wc,
+                                 Wc});
             divide(items, D);
             if (prof) {
                 sync();

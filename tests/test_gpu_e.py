@@ -130,20 +130,26 @@ def test_to_decimal_block_levels(arith, top, monkeypatch):
         assert arith.to_decimal(v) == str(v), (top, v.bit_length())
 
 
-@pytest.mark.parametrize("derive,wrap", [("0", "0"), ("0", "1"), ("1", "0"), ("1", "1")])
-def test_to_decimal_reciprocals(arith, derive, wrap, monkeypatch):
+@pytest.mark.parametrize("derive,wrap,short", [("0", "0", "0"), ("0", "1", "1"), ("1", "0", "1"), ("1", "1", "0"),
+                                               ("1", "1", "1")])
+def test_to_decimal_reciprocals(arith, derive, wrap, short, monkeypatch):
     # Levels above the block kernel divide by reciprocals of 10^(9 2^j),
     # each from its own Newton iteration (0) or derived from the level
-    # above's (1), with remainders from full or cyclic products; low tops
-    # put many levels on that path.
+    # above's (1), with remainders from full or cyclic products, and the top
+    # level's reciprocal short (from the squared one of the level below) or
+    # full; low tops put many levels on that path. 10^110000 + 7 needs a top
+    # reciprocal of 3766 limbs, at the limit (3824) of the short form;
+    # 10^147000 - 3 more than it can give (full-length fallback).
     monkeypatch.setenv("GBNTT_E_DERIVE_RECIP", derive)
     monkeypatch.setenv("GBNTT_E_WRAP", wrap)
+    monkeypatch.setenv("GBNTT_E_SHORT_TOP", short)
     rng = random.Random(31)
-    vals = [_rand(rng, 9000), (1 << (32 * 9000)) - 1, 10 ** 80000 - 1, 10 ** 73728, 10 ** 73728 - 1]
+    vals = [_rand(rng, 9000), (1 << (32 * 9000)) - 1, 10 ** 80000 - 1, 10 ** 73728, 10 ** 73728 - 1,
+            10 ** 110000 + 7, 10 ** 147000 - 3]
     for top in ["2", "5", "11"]:
         monkeypatch.setenv("GBNTT_DEC_TOP", top)
         for v in vals:
-            assert arith.to_decimal(v) == str(v), (derive, top, v.bit_length())
+            assert arith.to_decimal(v) == str(v), (derive, wrap, short, top, v.bit_length())
 
 
 def test_compute_e_small(arith, e_gold):
