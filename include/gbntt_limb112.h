@@ -25,8 +25,10 @@ typedef struct {
 
 /* Replaces ntt_mul_init_impl (ntt/lib/arith/ntt_mul.hip:379) for 112-bit
  * limbs: products of up to 2^max_log_n 112-bit coefficients
- * (n_a + n_b - 1 <= 2^max_log_n); valid range [3, cap], cap 28 unless
- * NTT_MAX_LOGN (<= 28) lowers or raises it. Out of range: message + exit(1). */
+ * (n_a + n_b - 1 <= 2^max_log_n, 3.5 32-bit limbs per coefficient, so the
+ * engine is sized for 2^(max_log_n + 2) 32-bit coefficients); valid range
+ * [3, cap], cap 28 (the engine's 2^30 limit), lowered by NTT_MAX_LOGN
+ * (3..28). Out of range: message + exit(1). */
 void ntt_mul_init_impl(int max_log_n);
 void ntt_mul_teardown_impl(void);
 
