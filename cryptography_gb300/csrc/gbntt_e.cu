@@ -1946,9 +1946,8 @@ int gbntt_to_decimal_u32(char *out, size_t cap, size_t *len, const uint32_t *x, 
         Pipe pp;
         DBuf dx = pp.upload(bn::Num(x, x + nx), std::max<size_t>(nx, 1));
         if (!out || cap < 2) efail(GBNTT_ERR_ARG, "output buffer needs at least 2 bytes");
-        size_t count = 0;
-        pp.to_decimal(dx.p, nx, out, out + 1, cap - 1, &count);
-        if (len) *len = count;
+        // *len receives the digit count also when the buffer is too small
+        const size_t count = pp.to_decimal(dx.p, nx, out, out + 1, cap - 1, len);
         pp.check_errors();
         out[count] = 0;
         return GBNTT_OK;

@@ -112,6 +112,30 @@ def test_to_decimal(arith):
         assert arith.to_decimal(v) == str(v), v.bit_length()
 
 
+def test_to_decimal_buffer_too_small(arith, engine):
+    # the digits come from the device straight into the caller's buffer: a
+    # buffer without room reports the digit count and GBNTT_ERR_SIZE and is
+    # left untouched beyond its size
+    import ctypes
+    import numpy as np
+    v = 3 ** 20000 + 12345
+    want = str(v)
+    a = np.frombuffer(v.to_bytes((v.bit_length() + 31) // 32 * 4, "little"), dtype=np.uint32).copy()
+    lib = engine.lib()
+    for cap in (1, 2, len(want), len(want) + 1):
+        buf = ctypes.create_string_buffer(b"\x7f" * (cap + 8), cap + 8)
+        n = ctypes.c_size_t(0)
+        rc = lib.gbntt_to_decimal_u32(buf, cap, ctypes.byref(n), a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                      len(a))
+        if cap >= len(want) + 1:
+            assert rc == 0 and n.value == len(want) and buf.raw[:len(want)].decode() == want and buf.raw[len(want)] == 0
+        else:
+            assert rc == (5 if cap < 2 else 2), (cap, rc)   # GBNTT_ERR_ARG below 2 bytes, else GBNTT_ERR_SIZE
+            if cap >= 2:
+                assert n.value == len(want)
+        assert buf.raw[cap:] == b"\x7f" * 8, cap
+
+
 @pytest.mark.parametrize("top", ["0", "1", "4", "6", "7", "9", "11", "12"])
 def test_to_decimal_block_levels(arith, top, monkeypatch):
     # The levels at and below GBNTT_DEC_TOP are split in shared memory by
