@@ -7,6 +7,7 @@ products run on the GPU engine. The engine must be initialised
 not.
 """
 import ctypes
+import threading
 
 import numpy as np
 
@@ -96,15 +97,16 @@ def to_decimal(v):
     return str(memoryview(buf)[:n.value], "ascii")
 
 
-_e_buf = [None]   # output buffer reused across calls (a fresh 10^8-byte buffer costs a zero fill)
+_e_buf = threading.local()   # per-thread output buffer reused across calls (a fresh 10^8-byte buffer costs a zero fill)
 
 
 def e_buffer(digits):
     """A host buffer of at least digits + 2 bytes for gbntt_compute_e, kept
-    between calls."""
-    if _e_buf[0] is None or len(_e_buf[0]) < int(digits) + 2:
-        _e_buf[0] = ctypes.create_string_buffer(int(digits) + 2)
-    return _e_buf[0]
+    between calls of the calling thread (threads do not share it)."""
+    buf = getattr(_e_buf, "buf", None)
+    if buf is None or len(buf) < int(digits) + 2:
+        buf = _e_buf.buf = ctypes.create_string_buffer(int(digits) + 2)
+    return buf
 
 
 def compute_e_raw(digits, buf):
