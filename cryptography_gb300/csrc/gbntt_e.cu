@@ -2004,7 +2004,7 @@ int gbntt_compute_e(long digits, char *out, size_t cap, double *phase_seconds)
         ph[2] = sw.lap();
         // "2.718...": the leading digit, the point, then the others, copied
         // from the device into out
-        const size_t count = pp.to_decimal(Q.p, nQ, out, out + 2, (size_t)digits);
+        const size_t count = pp.to_decimal(Q.p, nQ, out, out + 2, cap - 2);   // a wrong count is checked below
         pp.check_errors();
         ph[3] = sw.lap();
         if ((long)count != digits)
