@@ -23,7 +23,7 @@ LIB = os.path.join(HERE, "libgbntt.so")
 LIB112 = os.path.join(HERE, "libgbntt112.so")
 
 SOURCES = ["gbntt_pass_p0.cu", "gbntt_pass_p1.cu", "gbntt_pass_p2.cu", "gbntt_pass_p3.cu", "gbntt_pass_p4.cu", "gbntt_kernels.cu", "gbntt_engine.cu", "gbntt_noalloc.cu",
-           "gbntt_e.cu", "gbntt_negacyclic.cu", "gbntt_refabi.cu"]
+           "gbntt_e.cu", "gbntt_negacyclic.cu", "gbntt_refabi.cu", "gbntt_radix3.cu"]
 # (source, object name, extra flags): the reference entry points once more for 112-bit limbs
 VARIANTS = [("gbntt_refabi.cu", "gbntt_refabi112", ["-DGBNTT_LIMB_BITS=112"])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -82,6 +82,11 @@ struct Engine {
     bool fuse_inner = true;         // innermost forward passes, pointwise product and innermost inverse pass in one launch
     bool pass_tables = true;        // strided passes read their twiddles from pass tables (PassArgs::ptw)
     size_t ptw_budget = 0;          // ... up to this many bytes of tables in all
+    bool radix3 = true;             // transforms of length 3 2^k where those are shorter than the next 2^L
+    void *d_r3[5] = {};             // per prime: rho^(i 2^15) (3 2^15 words), then rho^i (2^15 words)
+    uint64_t r3c[5][5] = {};        // per prime: c, 1/2, 1/3, 1/6, c/3 in its multiply form
+    uint64_t r3rho[5] = {};         // per prime: rho (order 3 2^30), plain
+    int r3_min_log = 20;            // radix-3 for c products of 3 2^k points when c 2^k >= 2^r3_min_log
     bool batch_split = true;        // uneven batch products split into chunk products
     int split_ratio_log = 3;        // ... when the longer operand is >= 2^this x the shorter
     uint64_t garner2[2] = {0, 0};   // two-prime Garner constants (p3 Montgomery multipliers)
@@ -150,7 +155,8 @@ void set_error_message(const char *msg) { snprintf(g_err, sizeof g_err, "%s", ms
 // Optional per-launch CUDA-event records (kind, pass size, algorithmic bytes)
 // for roofline reporting; off by default and never used in timed runs.
 struct LaunchRec {
-    int kind;       // 0 fwd first pass, 1 fwd pass, 2 inv first pass, 3 inv pass, 4 garner+carry
+    int kind;       // 0 fwd first pass, 1 fwd pass, 2 inv first pass, 3 inv pass, 4 garner+carry,
+                    // 5 fused innermost passes, 6 and 7 forward and inverse radix-3 stages
     int log_l;
     double bytes;   // algorithmic bytes moved by this launch
     cudaEvent_t e0, e1;
@@ -337,6 +343,7 @@ static void free_all()
     cudaFree(g.d_tw3);
     cudaFree(g.d_st1);
     cudaFree(g.d_st13);
+    for (int i = 0; i < 5; i++) cudaFree(g.d_r3[i]);
     cudaFree(g.d_ctl);
     cudaFree(g.d_io);
     if (g.stream2) cudaStreamSynchronize(g.stream2);
@@ -483,6 +490,46 @@ static int init_impl(int max_log)
             e = cudaMemcpy(g.d_st13, st.data(), st.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
         }
         if (e != cudaSuccess) { set_err("gbntt_init: twiddle upload failed: %s", cudaGetErrorString(e)); free_all(); return GBNTT_ERR_CUDA; }
+        // radix-3 stage: rho of order 3 2^30 for Montgomery q0 (0), normal-form
+        // q0 (4) and p3 (3), two-level tables and constants in each form
+        for (const int pi : {0, 4, 3}) {
+            const uint64_t pp = prime_value(pi), gen = pi == 3 ? kGen3 : kGen[0];
+            const uint64_t rho = h_pow(gen, (pp - 1) / (3ull << kMaxLog), pp);
+            if (h_pow(rho, 3ull << kMaxLog, pp) != 1 || h_pow(rho, 1ull << kMaxLog, pp) == 1 ||
+                h_pow(rho, 3ull << (kMaxLog - 1), pp) == 1) {
+                set_err("gbntt_init: no root of order 3 2^30 for prime %d", pi);
+                free_all();
+                return GBNTT_ERR_ARG;
+            }
+            auto form = [&](uint64_t x) -> uint64_t { return pi == 3 ? h_mont3(x) : pi == 4 ? x % pp : h_mont(x, pp); };
+            const size_t nhi = 3 * (size_t)kTwSize, nw = nhi + (size_t)kTwSize;
+            std::vector<uint64_t> t(nw);
+            const uint64_t big = h_pow(rho, (uint64_t)kTwSize, pp);
+            uint64_t x = 1;
+            for (size_t i = 0; i < nhi; i++) { t[i] = form(x); x = h_mul(x, big, pp); }
+            x = 1;
+            for (size_t i = 0; i < (size_t)kTwSize; i++) { t[nhi + i] = form(x); x = h_mul(x, rho, pp); }
+            const size_t wb = pi == 3 ? 4 : 8;
+            std::vector<uint32_t> t32;
+            if (pi == 3) t32.assign(t.begin(), t.end());
+            if (cudaMalloc(&g.d_r3[pi], nw * wb) != cudaSuccess ||
+                cudaMemcpy(g.d_r3[pi], pi == 3 ? (const void *)t32.data() : (const void *)t.data(), nw * wb,
+                           cudaMemcpyHostToDevice) != cudaSuccess) {
+                set_err("gbntt_init: radix-3 table upload failed");
+                cudaGetLastError();
+                free_all();
+                return GBNTT_ERR_CUDA;
+            }
+            const uint64_t om = h_pow(rho, 1ull << kMaxLog, pp), inv2 = h_inv(2, pp), inv3 = h_inv(3, pp);
+            const uint64_t om2 = h_mul(om, om, pp);
+            const uint64_t c = h_mul(om >= om2 ? om - om2 : om + (pp - om2), inv2, pp);   // no 64-bit overflow for q0
+            g.r3rho[pi] = rho;
+            g.r3c[pi][0] = form(c);
+            g.r3c[pi][1] = form(inv2);
+            g.r3c[pi][2] = form(inv3);
+            g.r3c[pi][3] = form(h_mul(inv2, inv3, pp));
+            g.r3c[pi][4] = form(h_mul(c, inv3, pp));
+        }
         // two-prime Garner: q0^-1 mod p3 and 2^64 mod p3 as p3 Montgomery multipliers
         const uint64_t q0 = prime_value(0);
         g.garner2[0] = h_mont3(h_inv(q0 % p, p));
@@ -529,6 +576,10 @@ static int init_impl(int max_log)
         // workspace (a 2^29-point multiply needs about 12 GiB of them)
         const char *fi = getenv("GBNTT_FUSE_INNER");
         g.fuse_inner = !(fi && fi[0] == '0');
+        const char *r3 = getenv("GBNTT_RADIX3");
+        g.radix3 = !(r3 && r3[0] == '0');
+        const char *r3m = getenv("GBNTT_RADIX3_MIN_LOG");
+        g.r3_min_log = r3m ? std::max(10, std::min(30, atoi(r3m))) : 20;
         const char *pt = getenv("GBNTT_PASS_TABLES");
         g.pass_tables = !(pt && pt[0] == '0');
         const char *pb = getenv("GBNTT_PASS_TABLES_MB");
@@ -765,13 +816,14 @@ static void carry_setup(CarryArgs &c, const PrimeSet &ps, const uint64_t *specA,
 }
 
 static int carry(const PrimeSet &ps, uint32_t *d_c, size_t n_out, const uint64_t *specA, size_t stride, int L,
-                 cudaStream_t st)
+                 cudaStream_t st, long long n_coef = 0)
 {
+    // n_coef: coefficients of the transform (2^L unless given: 3 2^k)
     CarryArgs c;
     memset(&c, 0, sizeof c);
     carry_setup(c, ps, specA, stride);
     c.out = d_c;
-    c.n_coef = (long long)1 << L;
+    c.n_coef = n_coef ? n_coef : (long long)1 << L;
     c.n_out = (long long)n_out;
     c.ticket = g.d_ctl;
     c.error = g.d_ctl + 1;
@@ -798,6 +850,136 @@ struct StageJob {
     bool mapped = false;
 };
 
+// Sub-transform log k of a length-3 2^k transform for an n_a x n_b product
+// when that is shorter than the power-of-two one (the product needs at most
+// 3/4 of 2^L coefficients), else -1. Two-prime set, 2^k of at least 2^10.
+// The radix-3 stage adds six launches and a sweep over the spectrum, which
+// the quarter fewer points repay from about 2^20-point sub-transforms on
+// (measured per product: 3 2^18 points 1.11 x the time of 2^20, 3 2^20
+// points 0.875 x that of 2^22, 3 2^22 0.816 x): a product alone takes it
+// from k = r3_min_log, a batch for c products of one length when
+// c 2^k >= 2^r3_min_log (batch_mul).
+static int r3_log(size_t na, size_t nb)
+{
+    if (!g.radix3 || g.prime_set != 2 || na == 0 || nb == 0) return -1;
+    const int L = choose_log(na, nb);
+    const int k = L - 2;
+    if (k < 10 || (3ull << k) < na + nb - 1 || (3ull << k) > g.n_max) return -1;
+    return k;
+}
+
+// The outer radix-3 stage of W products on each prime (gbntt_radix3.cu),
+// on the streams the pass chain uses for them.
+static int radix3_stage(const PrimeSet &ps, uint64_t *spec, size_t stride, int k, long long W, bool inverse,
+                        const uint32_t *limbs, size_t n, const uint32_t *const *limb_tab, const long long *len_tab,
+                        cudaStream_t st, cudaStream_t aux)
+{
+    for (int q = 0; q < ps.n; q++) {
+        const int pi = ps.pi[q];
+        R3Args a;
+        memset(&a, 0, sizeof a);
+        a.spec = spec + q * stride;
+        a.M = 1LL << k;
+        a.W = W;
+        a.shift = kMaxLog - k;
+        a.limbs = limbs;
+        a.n_limbs = (long long)n;
+        a.limb_tab = limb_tab;
+        a.len_tab = len_tab;
+        const size_t wb = pi == 3 ? 4 : 8;
+        a.hi = g.d_r3[pi];
+        a.lo = (const char *)g.d_r3[pi] + 3 * (size_t)kTwSize * wb;
+        a.c = g.r3c[pi][0];
+        a.inv2 = g.r3c[pi][1];
+        a.inv3 = g.r3c[pi][2];
+        a.inv6 = g.r3c[pi][3];
+        a.c3 = g.r3c[pi][4];
+        // a thread steps through j, j + G, j + 2 G, ... (G = blocks x 256
+        // threads): its twiddle is multiplied by w^(+-G) per step
+        const long long per_block = 256LL * kR3Unroll;
+        a.blocks = (int)std::min<long long>((a.M + per_block - 1) / per_block, 8LL * g.sms);
+        const uint64_t pp = prime_value(pi), order = 3ull << kMaxLog;
+        uint64_t e = (uint64_t)(((unsigned __int128)(256ull * a.blocks) << a.shift) % order);
+        if (inverse && e) e = order - e;
+        const uint64_t step = h_pow(g.r3rho[pi], e, pp);
+        a.step = pi == 3 ? h_mont3(step) : pi == 4 ? step : h_mont(step, pp);
+        cudaStream_t sk = (aux && q == 1) ? aux : st;
+        const double nbw = word_bytes(pi) * 3.0 * (double)a.M * (double)W;
+        rec_begin(sk, inverse ? 7 : 6, 0, inverse ? 2.0 * nbw : nbw + 4.0 * (double)n);
+        CK(launch_radix3(pi, inverse, a, sk));
+        rec_end(sk);
+    }
+    return GBNTT_OK;
+}
+
+// c = a b through a transform of length 3 2^k: the radix-3 stage, three
+// 2^k-point pass chains per operand (a batch of three for the pass
+// kernels), the same fused and inverse passes, the inverse radix-3 stage,
+// and Garner + carry over the 3 2^k coefficients.
+static int r3_residues(const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb, int k, cudaStream_t st,
+                       const StageJob *stage_b, uint32_t *stage_a, int debug_mode = -1);
+
+static int mul_dev_r3(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb, int k,
+                      cudaStream_t st, const StageJob *stage_b, uint32_t *stage_a)
+{
+    const int rc = r3_residues(d_a, na, d_b, nb, k, st, stage_b, stage_a);
+    if (rc) return rc;
+    return carry(coef32_set(), d_c, na + nb, g.d_spec, g.n_max, k, st, 3LL << k);
+}
+
+// The residues of the product of length 3 2^k in the first slots of the
+// workspace (q0 at d_spec, p3 at d_spec + n_max). debug_mode 0: only the
+// forward and inverse radix-3 stages of A (the residues of A itself).
+static int r3_residues(const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb, int k, cudaStream_t st,
+                       const StageJob *stage_b, uint32_t *stage_a, int debug_mode)
+{
+    const bool square = (d_a == d_b && na == nb);
+    if (stage_a) {   // A in pinned host memory: one pass over C2C into HBM, read there by both primes
+        CK(launch_copy_words(stage_a, d_a, (long long)na, g.sms * 4, st));
+        d_a = stage_a;
+        if (square) d_b = stage_a;
+    }
+    uint64_t *specA = g.d_spec;
+    uint64_t *specB = g.d_spec + 3 * g.n_max;
+    const PrimeSet &ps = coef32_set();
+    const bool fused = fuse_inner(k);
+    cudaStream_t aux = fork_aux(ps, st, g.stream2);
+    int rc = radix3_stage(ps, specA, g.n_max, k, 1, false, d_a, na, nullptr, nullptr, st, aux);
+    if (rc) return rc;
+    if (debug_mode == 0) {
+        rc = radix3_stage(ps, specA, g.n_max, k, 1, true, nullptr, 0, nullptr, nullptr, st, aux);
+        if (rc) return rc;
+        return join_aux(st, aux);
+    }
+    if (stage_b && !square) CK(cudaEventRecord(g.ev_a, st));
+    rc = forward(ps, specA, g.n_max, nullptr, 0, k, st, false, 3, nullptr, nullptr, aux, nullptr, true, nullptr, fused);
+    if (rc) return rc;
+    if (!square) {
+        if (stage_b) {   // B's copy runs on the copy stream while A is transformed
+            CK(cudaStreamWaitEvent(g.cstream, g.ev_a, 0));
+            if (stage_b->mapped) CK(launch_copy_words(stage_b->dst, stage_b->src, (long long)stage_b->n, g.sms / 2, g.cstream));
+            else CK(cudaMemcpyAsync(stage_b->dst, stage_b->src, stage_b->n * 4, cudaMemcpyHostToDevice, g.cstream));
+            CK(cudaEventRecord(g.ev_b, g.cstream));
+            CK(cudaStreamWaitEvent(st, g.ev_b, 0));
+            if (aux) CK(cudaStreamWaitEvent(aux, g.ev_b, 0));
+        }
+        rc = radix3_stage(ps, specB, g.n_max, k, 1, false, d_b, nb, nullptr, nullptr, st, aux);
+        if (rc) return rc;
+        rc = forward(ps, specB, g.n_max, nullptr, 0, k, st, false, 3, nullptr, nullptr, aux, nullptr, true, nullptr,
+                     fused);
+        if (rc) return rc;
+    }
+    if (fused) {
+        rc = inner_fused(ps, specA, square ? specA : specB, g.n_max, k, st, square, 3, aux);
+        if (rc) return rc;
+    }
+    rc = inverse(ps, specA, square ? specA : specB, g.n_max, k, st, square, 3, aux, false, fused);
+    if (rc) return rc;
+    rc = radix3_stage(ps, specA, g.n_max, k, 1, true, nullptr, 0, nullptr, nullptr, st, aux);
+    if (rc) return rc;
+    return join_aux(st, aux);
+}
+
 // stage_a (optional): HBM copy of A made by its first pass (see forward).
 // stage_b (optional): copy of B into d_b, run on the copy stream while A is
 // transformed.
@@ -816,6 +998,8 @@ static int mul_dev(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint32_t
         set_err("product needs %zu coefficients but the engine was initialised for 2^%d", na + nb - 1, g.max_log);
         return GBNTT_ERR_SIZE;
     }
+    const int k3 = r3_log(na, nb);
+    if (k3 >= g.r3_min_log) return mul_dev_r3(d_c, d_a, na, d_b, nb, k3, st, stage_b, stage_a);
     const bool square = (d_a == d_b && na == nb);
     uint64_t *specA = g.d_spec;
     uint64_t *specB = g.d_spec + 3 * g.n_max;
@@ -935,13 +1119,14 @@ struct BatchItem {
 static inline size_t out_limbs(const BatchItem &it) { return it.nc ? it.nc : it.na + it.nb; }
 
 static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                         long long tiles, bool shared_b, bool pair_b = false);
+                         long long tiles, bool shared_b, bool pair_b = false, bool r3 = false);
 static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                      long long tiles, bool shared_b, bool pair_b = false);
+                      long long tiles, bool shared_b, bool pair_b = false, bool r3 = false);
 
-// One wave of W products, all of transform length 2^L, on stream st.
+// One wave of W products, all of transform length 2^L (r3: 3 2^L), on
+// stream st.
 static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, cudaStream_t st,
-                      cudaStream_t aux_stream = nullptr)
+                      cudaStream_t aux_stream = nullptr, bool r3 = false)
 {
     const int slot = *x.slot;
     CK(cudaEventSynchronize(x.btab_ev[slot]));
@@ -954,8 +1139,8 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
     // shared divisor or reciprocal): its transform is computed once; products
     // 2i and 2i + 1 multiplying by the same one (a product tree's B_L B_R and
     // P_L B_R): one transform per pair
-    bool shared_b = W > 1;
-    bool pair_b = W > 1 && W % 2 == 0;
+    bool shared_b = W > 1 && !r3;
+    bool pair_b = W > 1 && W % 2 == 0 && !r3;
     for (long long k = 0; k < W; k++) {
         const BatchItem &it = items[k];
         const BatchItem &mate = items[k ^ 1];
@@ -984,37 +1169,57 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
     CK(cudaMemcpyAsync(dtab, h, (7 * (size_t)W + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(x.btab_ev[slot], st));
     *x.slot = slot ^ 1;
-    if (g.graphs && !g_rec_on) return wave_graph(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b);
-    return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b);
+    if (g.graphs && !g_rec_on) return wave_graph(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b, r3);
+    return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b, r3);
 }
 
 // The launches of one wave after its table upload: both operands' forward
 // transforms, the fused pointwise product and inverse, the batched carry
 // kernel over `tiles` carry tiles.
 static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                         long long tiles, bool shared_b, bool pair_b)
+                         long long tiles, bool shared_b, bool pair_b, bool r3)
 {
     uint64_t *specA = x.spec, *specB = x.spec + 3 * x.cap;
     const PrimeSet &ps = coef32_set();
     cudaStream_t aux = fork_aux(ps, st, aux_stream);
-    // a shared right operand is transformed once and read by every product's
-    // pointwise pass, so it keeps the unfused innermost passes
-    const bool fused = !shared_b && fuse_inner(L);
-    int rc = forward(ps, specA, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab),
+    int rc = GBNTT_OK;
+    if (r3) {
+        // products of length 3 2^L: each operand's radix-3 stage, then its
+        // three sub-transforms as a batch of 3 W for the pass chain
+        const bool fused = fuse_inner(L);
+        for (int o = 0; o < 2; o++) {
+            uint64_t *spec = o ? specB : specA;
+            rc = radix3_stage(ps, spec, x.cap, L, W, false, nullptr, 0, (const uint32_t *const *)(dtab + 2 * o * W),
+                              (const long long *)(dtab + (2 * o + 1) * W), st, aux);
+            if (rc) return rc;
+            rc = forward(ps, spec, x.cap, nullptr, 0, L, st, false, 3 * W, nullptr, nullptr, aux, nullptr, true, nullptr,
+                         fused);
+            if (rc) return rc;
+        }
+        if (fused && (rc = inner_fused(ps, specA, specB, x.cap, L, st, false, 3 * W, aux)) != GBNTT_OK) return rc;
+        if ((rc = inverse(ps, specA, specB, x.cap, L, st, false, 3 * W, aux, false, fused)) != GBNTT_OK) return rc;
+        if ((rc = radix3_stage(ps, specA, x.cap, L, W, true, nullptr, 0, nullptr, nullptr, st, aux)) != GBNTT_OK)
+            return rc;
+    } else {
+        // a shared right operand is transformed once and read by every
+        // product's pointwise pass, so it keeps the unfused innermost passes
+        const bool fused = !shared_b && fuse_inner(L);
+        rc = forward(ps, specA, x.cap, nullptr, 0, L, st, false, W, (const uint32_t *const *)(dtab),
                      (const long long *)(dtab + W), aux, nullptr, false, nullptr, fused);
-    if (rc) return rc;
-    // shared right operand: one transform (table entry 0), read by every
-    // product's pointwise pass; pairs: W / 2 transforms (entries 0 .. W/2 - 1)
-    rc = forward(ps, specB, x.cap, nullptr, 0, L, st, false, shared_b ? 1 : pair_b ? W / 2 : W,
-                 (const uint32_t *const *)(dtab + 2 * W), (const long long *)(dtab + 3 * W), aux, nullptr, false,
-                 nullptr, fused);
-    if (rc) return rc;
-    if (fused) {
-        rc = inner_fused(ps, specA, specB, x.cap, L, st, false, W, aux, pair_b);
+        if (rc) return rc;
+        // shared right operand: one transform (table entry 0), read by every
+        // product's pointwise pass; pairs: W / 2 transforms (entries 0 .. W/2 - 1)
+        rc = forward(ps, specB, x.cap, nullptr, 0, L, st, false, shared_b ? 1 : pair_b ? W / 2 : W,
+                     (const uint32_t *const *)(dtab + 2 * W), (const long long *)(dtab + 3 * W), aux, nullptr, false,
+                     nullptr, fused);
+        if (rc) return rc;
+        if (fused) {
+            rc = inner_fused(ps, specA, specB, x.cap, L, st, false, W, aux, pair_b);
+            if (rc) return rc;
+        }
+        rc = inverse(ps, specA, specB, x.cap, L, st, false, W, aux, shared_b, fused, pair_b);
         if (rc) return rc;
     }
-    rc = inverse(ps, specA, specB, x.cap, L, st, false, W, aux, shared_b, fused, pair_b);
-    if (rc) return rc;
     rc = join_aux(st, aux);
     if (rc) return rc;
     CarryArgs c;
@@ -1028,11 +1233,13 @@ static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaSt
     c.nout_tab = (const long long *)(dtab + 5 * W);
     c.nprod = (int)W;
     c.log_n_prod = L;
+    c.radix3 = r3 ? 1 : 0;
     CK(cudaMemsetAsync(x.ctl, 0, sizeof(unsigned), st));
     CK(cudaMemsetAsync(x.ctl + 2, 0, (size_t)tiles * sizeof(unsigned), st));
     double rb = 0;
     for (int k = 0; k < ps.n; k++) rb += word_bytes(ps.pi[k]);
-    rec_begin(st, 4, 0, (rb * (double)((size_t)1 << L) + 4.0 * (double)(1 << L)) * (double)W);
+    const double npt = (double)((r3 ? 3LL : 1LL) << L);
+    rec_begin(st, 4, 0, (rb * npt + 4.0 * npt) * (double)W);
     CK(launch_garner_carry_batch(c, tiles, st));
     rec_end(st);
     return GBNTT_OK;
@@ -1079,15 +1286,15 @@ static void invalidate_wave_graphs()
 }
 
 static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStream_t st, cudaStream_t aux_stream,
-                      long long tiles, bool shared_b, bool pair_b)
+                      long long tiles, bool shared_b, bool pair_b, bool r3)
 {
     const PrimeSet &ps = coef32_set();
-    const long long ub = W * carry_tiles(((long long)1 << L) + 1);
-    if ((size_t)ub > x.n_status) return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b);
+    const long long ub = W * carry_tiles(((r3 ? 3LL : 1LL) << L) + 1);
+    if ((size_t)ub > x.n_status) return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b, r3);
     const bool aux = aux_used(ps, aux_stream);
     const WaveKey key{x.spec, dtab, x.ctl, x.cap, L, W,
                       ps.n * 16 + ps.pi[0] * 4 + ps.pi[1] + (aux ? 256 : 0) + (shared_b ? 512 : 0) +
-                          (pair_b ? 1024 : 0)};
+                          (pair_b ? 1024 : 0) + (r3 ? 2048 : 0)};
     cudaGraphExec_t exec = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_wave_graphs_mu);
@@ -1095,10 +1302,10 @@ static int wave_graph(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaStrea
         exec = wg.exec;
         if (!exec && wg.runs++ == 0) exec = (cudaGraphExec_t)-1;
     }
-    if (exec == (cudaGraphExec_t)-1) return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b);
+    if (exec == (cudaGraphExec_t)-1) return wave_launches(x, dtab, W, L, st, aux_stream, tiles, shared_b, pair_b, r3);
     if (!exec) {
         CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        const int rc = wave_launches(x, dtab, W, L, st, aux_stream, ub, shared_b, pair_b);
+        const int rc = wave_launches(x, dtab, W, L, st, aux_stream, ub, shared_b, pair_b, r3);
         cudaGraph_t graph = nullptr;
         const cudaError_t e = cudaStreamEndCapture(st, &graph);
         if (rc != GBNTT_OK || e != cudaSuccess) {
@@ -1155,6 +1362,8 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
         long long group;   // items of one split stay together (shared operand per wave)
         BatchItem item;
         int paired = 0;    // with its neighbour in the batch: the same right operand, one transform
+        int chunk = 0;     // a chunk product of a split
+        int r3 = 0;        // transform length 3 2^L
     };
     struct Split {
         uint32_t *E, *O, *c;
@@ -1216,7 +1425,7 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
             for (size_t j = 0, off = 0; off < nB; j++, off += chunk) {
                 const size_t len = std::min(chunk, nB - off);
                 uint32_t *dst = ((j & 1) ? (uint32_t *)O : (uint32_t *)E) + off;
-                all.push_back({choose_log(len, nS), (long long)i, {dst, Bp + off, S, len, nS}});
+                all.push_back({choose_log(len, nS), (long long)i, {dst, Bp + off, S, len, nS}, 0, 1});
             }
             continue;
         }
@@ -1239,8 +1448,33 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
                 i++;
             }
         }
+        // the other products (no right operand shared with a neighbour, not
+        // cyclic, not a split's chunk) take a transform of 3 2^k points where
+        // it is shorter than the power of two
+        // (enough of them: c products of 3 2^k points with c 2^k >= 2^r3_min_log)
+        std::vector<int> k3s(all.size(), -1);
+        long long count3[kMaxLog + 1] = {};
+        for (size_t i = 0; i < all.size(); i++) {
+            const Keyed &u = all[i];
+            if (u.paired || u.chunk || u.item.nc) continue;
+            if ((i > 0 && all[i - 1].item.b == u.item.b) || (i + 1 < all.size() && all[i + 1].item.b == u.item.b))
+                continue;
+            const int k3 = r3_log(u.item.na, u.item.nb);
+            if (k3 >= 0) {
+                k3s[i] = k3;
+                count3[k3]++;
+            }
+        }
+        for (size_t i = 0; i < all.size(); i++) {
+            const int k3 = k3s[i];
+            if (k3 >= 0 && (k3 >= g.r3_min_log || count3[k3] >= (1LL << (g.r3_min_log - k3)))) {
+                all[i].L = k3;
+                all[i].r3 = 1;
+            }
+        }
         std::stable_sort(all.begin(), all.end(), [](const Keyed &x, const Keyed &y) {
             if (x.L != y.L) return x.L < y.L;
+            if (x.r3 != y.r3) return x.r3 < y.r3;
             if (x.paired != y.paired) return x.paired < y.paired;
             return x.group < y.group;
         });
@@ -1248,16 +1482,16 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
         std::vector<BatchItem> items;
         size_t pos = 0;
         while (pos < all.size() && rc == GBNTT_OK) {
-            const int L = all[pos].L, paired = all[pos].paired;
+            const int L = all[pos].L, paired = all[pos].paired, r3 = all[pos].r3;
             size_t end = pos;
-            while (end < all.size() && all[end].L == L && all[end].paired == paired) end++;
-            long long wmax = std::min<long long>(kMaxBatch, (long long)(g.n_max >> L));
+            while (end < all.size() && all[end].L == L && all[end].paired == paired && all[end].r3 == r3) end++;
+            long long wmax = std::min<long long>(kMaxBatch, (long long)(g.n_max / ((r3 ? 3ull : 1ull) << L)));
             if (paired && wmax > 1) wmax &= ~1LL;   // waves split between pairs
             for (size_t w0 = pos; w0 < end && rc == GBNTT_OK; w0 += (size_t)wmax) {
                 const long long W = std::min<long long>(wmax, (long long)(end - w0));
                 items.clear();
                 for (long long k = 0; k < W; k++) items.push_back(all[w0 + k].item);
-                rc = batch_wave(x, items.data(), W, L, st, g.stream2);
+                rc = batch_wave(x, items.data(), W, L, st, g.stream2, r3 != 0);
             }
             pos = end;
         }
@@ -2308,6 +2542,28 @@ int gbntt_debug_lookback_timeout(unsigned int *flags, double *seconds)
     CK(cudaStreamSynchronize(g.stream));
     if (seconds) *seconds = (now_ms() - t0) * 1e-3;
     return read_errors(flags);
+}
+
+// Residues of a radix-3 product before Garner (mode 1) or of A after the
+// forward and inverse radix-3 stages alone (mode 0): q0 words to d_q0, p3
+// words to d_p3, 3 2^k of each (device pointers).
+int gbntt_debug_radix3(uint64_t *d_q0, uint32_t *d_p3, const uint32_t *d_a, size_t na, const uint32_t *d_b,
+                       size_t nb, int k, int mode)
+{
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    if (g.prime_set != 2 || k < kMinLog || (3ull << k) > g.n_max || na > (3ull << k) || nb > (3ull << k) ||
+        (mode == 1 && na + nb - 1 > (3ull << k)) || na == 0 || nb == 0) {
+        set_err("bad size");
+        return GBNTT_ERR_ARG;
+    }
+    const int rc = r3_residues(d_a, na, d_b, nb, k, g.stream, nullptr, nullptr, mode);
+    if (rc) return rc;
+    const size_t M3 = (size_t)3 << k;
+    CK(cudaMemcpyAsync(d_q0, g.d_spec, M3 * 8, cudaMemcpyDeviceToDevice, g.stream));
+    CK(cudaMemcpyAsync(d_p3, g.d_spec + g.n_max, M3 * 4, cudaMemcpyDeviceToDevice, g.stream));
+    CK(cudaStreamSynchronize(g.stream));
+    return GBNTT_OK;
 }
 
 int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log_n, void *stream)

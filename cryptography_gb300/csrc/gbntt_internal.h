@@ -102,6 +102,7 @@ struct CarryArgs {
     const long long *nout_tab;
     int nprod;
     int log_n_prod;
+    int radix3;                 // batched mode: products of 3 2^log_n_prod coefficients
     int mixed;                  // two-prime set: res[0] q0 (64-bit), res[1] p3 (32-bit words)
 };
 
@@ -172,6 +173,25 @@ void set_error_message(const char *msg);
 // device, cleared on read (gbntt_noalloc.cu); *set_up = 0 when that scratch
 // was never set up on this device.
 int noalloc_read_errors(unsigned *flags, int *set_up);
+
+// Outer radix-3 stage of length-3 M transforms (gbntt_radix3.cu): W
+// products, product w's three M-point sub-spectra at spec + w 3 M + m M.
+struct R3Args {
+    void *spec;                          // this prime's spectra
+    long long M;                         // sub-transform length 2^k
+    long long W;                         // products (<= 65535)
+    int shift;                           // 30 - k: w_N^j = rho^(j << shift)
+    const uint32_t *limbs;               // forward input of a single product ...
+    long long n_limbs;
+    const uint32_t *const *limb_tab;     // ... or of W products (device tables)
+    const long long *len_tab;
+    const void *hi, *lo;                 // rho^(i 2^15), i < 3 2^15, and rho^i, i < 2^15 (the field's multiply form)
+    uint64_t c, inv2, inv3, inv6, c3;    // (om - om^2) / 2, 1/2, 1/3, 1/6, c / 3 in the same form
+    uint64_t step;                       // w^G (forward) or w^-G (inverse), G = blocks x 256, same form
+    int blocks;                          // grid x (at most 65535)
+};
+constexpr int kR3Unroll = 4;             // j values a thread's loads cover per step of its loop
+cudaError_t launch_radix3(int pi, bool inverse, const R3Args &a, cudaStream_t st);
 
 // Engine state and operations behind the reference-compatible entry points
 // (gbntt_refabi.cu, built once for 64-bit and once for 112-bit BigInt

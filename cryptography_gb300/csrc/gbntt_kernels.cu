@@ -262,7 +262,8 @@ __global__ void __launch_bounds__(kCarryThreads, GBNTT_CARRY_MIN_BLOCKS) garner_
         // tickets beyond the batch's tiles (the grid is an upper bound) exit
         if (s_prod < 0) return;
         const long long b = s_prod;
-        const long long off = b << a.log_n_prod;
+        const long long n_prod = (a.radix3 ? 3LL : 1LL) << a.log_n_prod;
+        const long long off = b * n_prod;
         if (MIXED) {
             a.res[0] += off;
             a.res[1] = (const uint64_t *)((const uint32_t *)a.res[1] + off);
@@ -271,7 +272,7 @@ __global__ void __launch_bounds__(kCarryThreads, GBNTT_CARRY_MIN_BLOCKS) garner_
         }
         a.out = a.out_tab[b];
         a.n_out = a.nout_tab[b];
-        a.n_coef = 1LL << a.log_n_prod;
+        a.n_coef = n_prod;
         a.status += a.tile_start[b];
     }
     const long long tile = BATCH ? (long long)s_tile - a.tile_start[s_prod] : (long long)s_tile;

@@ -38,7 +38,7 @@ EXPORTS = (
     "ntt_gpu_emergency_reset", "bigint_alloc_managed", "hip_free_limbs", "ntt_bigint_sqr",
     "ntt_bigint_mul_checked", "gbntt_init", "gbntt_teardown", "gbntt_is_ready", "gbntt_max_log",
     "gbntt_workspace_bytes", "gbntt_transform_log", "gbntt_plan", "gbntt_mul_u32", "gbntt_sqr_u32",
-    "gbntt_mul_u32_host", "gbntt_device_errors", "gbntt_debug_forward", "gbntt_last_error", "gbntt_stream",
+    "gbntt_mul_u32_host", "gbntt_device_errors", "gbntt_debug_forward", "gbntt_debug_radix3", "gbntt_last_error", "gbntt_stream",
     "gbntt_launch_log", "gbntt_launch_records", "gbntt_set_plan", "gbntt_debug_modops",
     "gbntt_mul_u64", "gbntt_sqr_u64", "gbntt_mul_u64_host", "gbntt_set_coeff_bits", "gbntt_coeff_bits",
     "gbntt_mul_u32_noalloc", "gbntt_batch_mul_u32", "gbntt_fill_operand",
@@ -103,6 +103,8 @@ def lib():
     L.gbntt_device_errors.restype = ctypes.c_int
     L.gbntt_debug_forward.argtypes = [_vp, _vp, _sz, ctypes.c_int, _vp]
     L.gbntt_debug_forward.restype = ctypes.c_int
+    L.gbntt_debug_radix3.argtypes = [_vp, _vp, _vp, _sz, _vp, _sz, ctypes.c_int, ctypes.c_int]
+    L.gbntt_debug_radix3.restype = ctypes.c_int
     L.gbntt_debug_modops.argtypes = [ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _sz, _vp]
     L.gbntt_debug_modops.restype = ctypes.c_int
     L.gbntt_mul_u64.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp]
@@ -208,7 +210,8 @@ def plan(log_n):
     return [p[i] for i in range(n)]
 
 
-LAUNCH_KINDS = ("fwd_pass_first", "fwd_pass", "inv_pass_first", "inv_pass", "garner_carry", "fused_inner_pass")
+LAUNCH_KINDS = ("fwd_pass_first", "fwd_pass", "inv_pass_first", "inv_pass", "garner_carry", "fused_inner_pass",
+                "radix3_fwd", "radix3_inv")
 
 
 def launch_log(enable):

@@ -223,6 +223,14 @@ int gbntt_device_errors(unsigned int *flags);
  * tests. d_out needs 3 * 2^log_n entries. */
 int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log_n, void *stream);
 
+/* Residues of the 3 2^k-point transform path, two-prime set: mode 1, the
+ * cyclic convolution of a and b of length 3 2^k (n_a + n_b - 1 <= 3 2^k)
+ * before Garner; mode 0, a itself after the forward and inverse radix-3
+ * stages alone. d_q0 receives 3 2^k q0 residues (uint64), d_p3 3 2^k p3
+ * residues (uint32); device pointers. For known-answer tests. */
+int gbntt_debug_radix3(uint64_t *d_q0, uint32_t *d_p3, const uint32_t *d_a, size_t na, const uint32_t *d_b,
+                       size_t nb, int k, int mode);
+
 /* Self-test of the bounded waits (no reference counterpart): runs the
  * Garner+carry kernel over a few tiles with its tile ticket started past
  * tile 0, so one look-back waits on a status word that nothing writes; the

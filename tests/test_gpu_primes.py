@@ -113,10 +113,12 @@ def test_synth_2pow22_both_sets(engine):
 
 
 @pytest.mark.parametrize("knobs", [{"GBNTT_Q0_FORM": "lazy"}, {"GBNTT_OVERLAP": "0"},
-                                   {"GBNTT_Q0_FORM": "lazy", "GBNTT_OVERLAP": "0"}])
+                                   {"GBNTT_Q0_FORM": "lazy", "GBNTT_OVERLAP": "0"}, {"GBNTT_RADIX3": "0"},
+                                   {"GBNTT_Q0_FORM": "lazy", "GBNTT_RADIX3_MIN_LOG": "10"}])
 def test_engine_knobs_give_identical_products(knobs):
-    # the tuning switches (lazy normal-form q0, no second-prime stream) change
-    # how the product is computed, never its value
+    # the tuning switches (lazy normal-form q0, no second-prime stream, no
+    # transforms of length 3 2^k) change how the product is computed, never
+    # its value
     import json
     import os
     import subprocess
