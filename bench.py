@@ -68,6 +68,8 @@ def parse():
                     help="skip timing the same multiply with the reference's three 64-bit primes")
     ap.add_argument("--three-prime-steps", type=int, default=5)
     ap.add_argument("--no-square", action="store_true", help="skip the squaring and 2^20-limb legs")
+    ap.add_argument("--no-radix3", action="store_true",
+                    help="skip the leg timing products of 3 2^k points against the next power of two")
     ap.add_argument("--no-e", action="store_true", help="skip the e-digits leg")
     ap.add_argument("--e-digits", type=int, default=10 ** 8)
     ap.add_argument("--e-reps", type=int, default=3)
@@ -675,6 +677,10 @@ def run_gpu(args, dist):
             buf.free()
         flags |= g.device_errors()
 
+    radix3 = None if args.no_radix3 else run_radix3_leg(g, cudart, synth, lg, stream)
+    if radix3:
+        flags |= radix3["device_error_flags"]
+
     # packed mode (one 64-bit limb per coefficient, transform length 2^lg)
     packed = None
     if not args.no_packed:
@@ -846,6 +852,7 @@ def run_gpu(args, dist):
         "three_prime_64bit": three,
         "square": square,
         "multiply_2pow20": small,
+        "radix3": radix3,
         "packed_64bit_coefficients": packed,
         "negacyclic": negacyclic,
         "batched": batched,
@@ -864,6 +871,65 @@ def run_gpu(args, dist):
         buf.free()
     g.teardown()
     return 0 if flags == 0 else 3
+
+
+def run_radix3_leg(g, cudart, synth, lg, stream):
+    """Products whose coefficient count fits 3 2^k but not 2^(k+1): n x n
+    limbs with 2 n - 1 = 3 2^k - 1 run a transform of 3 2^k points, timed
+    against n + 1 x n + 1 limbs (3 2^k + 1 coefficients), which take the
+    power of two 2^(k+2): nearly the same product, a third more points."""
+    out = {"sizes": [], "rule": "a product alone takes 3 2^k points from k = 20 (GBNTT_RADIX3_MIN_LOG)"}
+    flags = 0
+    for k in (20, 22, 24):
+        if (3 << k) + 1 > (1 << (lg + 1)):
+            continue
+        n3 = 3 << (k - 1)
+        xa, xb = synth.operand(n3 + 1, 31), synth.operand(n3 + 1, 32)
+        ra, rb = cudart.DeviceBuffer(4 * (n3 + 1)), cudart.DeviceBuffer(4 * (n3 + 1))
+        rc = cudart.DeviceBuffer(8 * (n3 + 1))
+        ra.upload(xa)
+        rb.upload(xb)
+        reps = max(5, 40 >> (k - 20))
+
+        def timed(nn):
+            for _ in range(2):
+                g.mul_device(rc.ptr, ra.ptr, nn, rb.ptr, nn, None)
+            e0, e1 = cudart.Event(), cudart.Event()
+            e0.record(stream)
+            for _ in range(reps):
+                g.mul_device(rc.ptr, ra.ptr, nn, rb.ptr, nn, None)
+            e1.record(stream)
+            e1.synchronize()
+            return e0.elapsed_ms(e1) / reps
+
+        if not out["sizes"]:   # the clocks ramp on the first sizeable work of the leg
+            for _ in range(30):
+                g.mul_device(rc.ptr, ra.ptr, n3 + 1, rb.ptr, n3 + 1, None)
+        m3, m2 = timed(n3), timed(n3 + 1)
+        g.launch_log(True)
+        g.mul_device(rc.ptr, ra.ptr, n3, rb.ptr, n3, None)
+        cudart.stream_sync(stream)
+        recs = g.launch_records(256)
+        g.launch_log(False)
+        flags |= g.device_errors()
+        by = {}
+        for kind, _, nbytes, kms in recs:
+            e = by.setdefault(kind, {"launches": 0, "ms": 0.0, "bytes": 0.0})
+            e["launches"] += 1
+            e["ms"] += kms
+            e["bytes"] += nbytes
+        for e in by.values():
+            e["GBps"] = e["bytes"] / (e["ms"] * 1e-3) / 1e9 if e["ms"] > 0 else None
+        out["sizes"].append({"operand_limbs": n3, "points": 3 << k, "ms": m3, "pow2_operand_limbs": n3 + 1,
+                             "pow2_points": 1 << (k + 2), "pow2_ms": m2, "ratio": m3 / m2, "steps": reps,
+                             "radix3_launches": sum(by[x]["launches"] for x in by if x.startswith("radix3")),
+                             "launch_breakdown": by,
+                             "launch_breakdown_note": "one product with per-launch CUDA events (launches "
+                                                      "serialised, both primes on one stream)"})
+        for buf in (ra, rb, rc):
+            buf.free()
+    out["device_error_flags"] = flags
+    return out
 
 
 def run_negacyclic_leg(g, cudart, args, stream):

@@ -84,7 +84,7 @@ struct Engine {
     size_t ptw_budget = 0;          // ... up to this many bytes of tables in all
     bool radix3 = true;             // transforms of length 3 2^k where those are shorter than the next 2^L
     void *d_r3[5] = {};             // per prime: rho^(i 2^15) (3 2^15 words), then rho^i (2^15 words)
-    uint64_t r3c[5][5] = {};        // per prime: c, 1/2, 1/3, 1/6, c/3 in its multiply form
+    uint64_t r3c[5] = {};           // per prime: c = (om - om^2) / 2 in its multiply form
     uint64_t r3rho[5] = {};         // per prime: rho (order 3 2^30), plain
     int r3_min_log = 20;            // radix-3 for c products of 3 2^k points when c 2^k >= 2^r3_min_log
     bool batch_split = true;        // uneven batch products split into chunk products
@@ -221,10 +221,12 @@ static cudaError_t launch_build_ptw_any(int pi, uint64_t *t, const uint64_t *hi,
 // allocation failed, or a stream capture in progress: the pass then forms
 // its twiddles itself). A new table is built on st and st is synchronised
 // before the table is published, so any stream may use it afterwards.
-static const uint64_t *pass_table(int pi, int dir, int log_m, int log_s, bool scaled, uint64_t scale, cudaStream_t st)
+// scaled: 0 none, 1 the outermost inverse pass's 2^-log_m, 2 that times 1/3
+// (transforms of 3 2^k points); the value is `scale`, fixed by the key.
+static const uint64_t *pass_table(int pi, int dir, int log_m, int log_s, int scaled, uint64_t scale, cudaStream_t st)
 {
     if (!g.pass_tables || log_s <= 0) return nullptr;
-    const auto key = std::make_tuple(pi, dir, log_m, log_s, scaled ? 1 : 0);
+    const auto key = std::make_tuple(pi, dir, log_m, log_s, scaled);
     std::lock_guard<std::mutex> lk(g_ptw_mu);
     const auto it = g_ptw.find(key);
     if (it != g_ptw.end()) return it->second;
@@ -520,15 +522,11 @@ static int init_impl(int max_log)
                 free_all();
                 return GBNTT_ERR_CUDA;
             }
-            const uint64_t om = h_pow(rho, 1ull << kMaxLog, pp), inv2 = h_inv(2, pp), inv3 = h_inv(3, pp);
+            const uint64_t om = h_pow(rho, 1ull << kMaxLog, pp), inv2 = h_inv(2, pp);
             const uint64_t om2 = h_mul(om, om, pp);
             const uint64_t c = h_mul(om >= om2 ? om - om2 : om + (pp - om2), inv2, pp);   // no 64-bit overflow for q0
             g.r3rho[pi] = rho;
-            g.r3c[pi][0] = form(c);
-            g.r3c[pi][1] = form(inv2);
-            g.r3c[pi][2] = form(inv3);
-            g.r3c[pi][3] = form(h_mul(inv2, inv3, pp));
-            g.r3c[pi][4] = form(h_mul(c, inv3, pp));
+            g.r3c[pi] = form(c);
         }
         // two-prime Garner: q0^-1 mod p3 and 2^64 mod p3 as p3 Montgomery multipliers
         const uint64_t q0 = prime_value(0);
@@ -686,7 +684,7 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
             } else {
                 a.stage_out = staged ? stage : nullptr;
             }
-            a.ptw[k] = a.twiddle ? pass_table(ps.pi[k], 0, a.log_m, a.log_s, false, 0, sk) : nullptr;
+            a.ptw[k] = a.twiddle ? pass_table(ps.pi[k], 0, a.log_m, a.log_s, 0, 0, sk) : nullptr;
             rec_begin(sk, i == 0 ? 0 : 1, pl[i], i == 0 ? (packed ? 8.0 : 4.0) * (double)n + nbw : 2.0 * nbw);
             const int ld0 = preloaded ? LD_U64 : (packed ? LD_U64LIMB : LD_U32);
             CK(launch_pass_any(ps.pi[k], pl[i], 0, i == 0 ? ld0 : LD_U64, a, sk));
@@ -705,8 +703,10 @@ static int forward(const PrimeSet &ps, uint64_t *spec, size_t stride, const void
 // for products 2i and 2i + 1.
 static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, size_t stride, int L,
                    cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr, bool shared_b = false,
-                   bool skip_first = false, bool pair_b = false)
+                   bool skip_first = false, bool pair_b = false, bool third = false)
 {
+    // third: scale by (3 2^L)^-1 instead of 2^-L (the sub-transforms of a
+    // 3 2^L-point transform; the inverse radix-3 stage then has no 1/3)
     // skip_first: the pointwise product and the innermost inverse pass were
     // done by the fused kernel (inner_fused); start at the next pass
     int pl[kMaxPasses];
@@ -722,7 +722,7 @@ static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, s
         // N^-1 * R^2: with the R^-1 left by the Montgomery pointwise product
         // the inverse output is scaled by exactly N^-1.
         const uint64_t p = prime_value(pi);
-        const uint64_t ninv = h_inv(((uint64_t)1 << L) % p, p);
+        const uint64_t ninv = h_inv(h_mul(((uint64_t)1 << L) % p, third ? 3 : 1, p), p);
         // (normal-form q0: the pointwise product leaves no factor, so N^-1 itself)
         a.scale[k] = pi < 3 ? h_mont(h_mont(ninv, p), p) : pi == 3 ? (uint64_t)h_mont3(h_mont3(ninv)) : ninv;
     }
@@ -740,7 +740,8 @@ static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, s
         for (int k = 0; k < ps.n; k++) {
             const double nbw = word_bytes(ps.pi[k]) * (double)((size_t)1 << L) * (double)W;
             cudaStream_t sk = (aux && k == 1) ? aux : st;
-            a.ptw[k] = a.twiddle ? pass_table(ps.pi[k], 1, a.log_m, a.log_s, a.use_scale != 0, a.scale[k], sk)
+            a.ptw[k] = a.twiddle ? pass_table(ps.pi[k], 1, a.log_m, a.log_s, a.use_scale ? (third ? 2 : 1) : 0,
+                                              a.scale[k], sk)
                                  : nullptr;
             rec_begin(sk, first ? 2 : 3, pl[i], first ? (square ? 2.0 : 3.0) * nbw : 2.0 * nbw);
             CK(launch_pass_any(ps.pi[k], pl[i], 1, first ? LD_PW : LD_U64, a, sk));
@@ -889,15 +890,11 @@ static int radix3_stage(const PrimeSet &ps, uint64_t *spec, size_t stride, int k
         const size_t wb = pi == 3 ? 4 : 8;
         a.hi = g.d_r3[pi];
         a.lo = (const char *)g.d_r3[pi] + 3 * (size_t)kTwSize * wb;
-        a.c = g.r3c[pi][0];
-        a.inv2 = g.r3c[pi][1];
-        a.inv3 = g.r3c[pi][2];
-        a.inv6 = g.r3c[pi][3];
-        a.c3 = g.r3c[pi][4];
+        a.c = g.r3c[pi];
         // a thread steps through j, j + G, j + 2 G, ... (G = blocks x 256
         // threads): its twiddle is multiplied by w^(+-G) per step
         const long long per_block = 256LL * kR3Unroll;
-        a.blocks = (int)std::min<long long>((a.M + per_block - 1) / per_block, 8LL * g.sms);
+        a.blocks = (int)std::min<long long>((a.M + per_block - 1) / per_block, 65535LL);
         const uint64_t pp = prime_value(pi), order = 3ull << kMaxLog;
         uint64_t e = (uint64_t)(((unsigned __int128)(256ull * a.blocks) << a.shift) % order);
         if (inverse && e) e = order - e;
@@ -929,7 +926,8 @@ static int mul_dev_r3(uint32_t *d_c, const uint32_t *d_a, size_t na, const uint3
 
 // The residues of the product of length 3 2^k in the first slots of the
 // workspace (q0 at d_spec, p3 at d_spec + n_max). debug_mode 0: only the
-// forward and inverse radix-3 stages of A (the residues of A itself).
+// forward and inverse radix-3 stages of A (3 A: the 1/3 is the inverse
+// chain's).
 static int r3_residues(const uint32_t *d_a, size_t na, const uint32_t *d_b, size_t nb, int k, cudaStream_t st,
                        const StageJob *stage_b, uint32_t *stage_a, int debug_mode)
 {
@@ -973,7 +971,7 @@ static int r3_residues(const uint32_t *d_a, size_t na, const uint32_t *d_b, size
         rc = inner_fused(ps, specA, square ? specA : specB, g.n_max, k, st, square, 3, aux);
         if (rc) return rc;
     }
-    rc = inverse(ps, specA, square ? specA : specB, g.n_max, k, st, square, 3, aux, false, fused);
+    rc = inverse(ps, specA, square ? specA : specB, g.n_max, k, st, square, 3, aux, false, fused, false, true);
     if (rc) return rc;
     rc = radix3_stage(ps, specA, g.n_max, k, 1, true, nullptr, 0, nullptr, nullptr, st, aux);
     if (rc) return rc;
@@ -1197,7 +1195,8 @@ static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaSt
             if (rc) return rc;
         }
         if (fused && (rc = inner_fused(ps, specA, specB, x.cap, L, st, false, 3 * W, aux)) != GBNTT_OK) return rc;
-        if ((rc = inverse(ps, specA, specB, x.cap, L, st, false, 3 * W, aux, false, fused)) != GBNTT_OK) return rc;
+        if ((rc = inverse(ps, specA, specB, x.cap, L, st, false, 3 * W, aux, false, fused, false, true)) != GBNTT_OK)
+            return rc;
         if ((rc = radix3_stage(ps, specA, x.cap, L, W, true, nullptr, 0, nullptr, nullptr, st, aux)) != GBNTT_OK)
             return rc;
     } else {
@@ -2544,7 +2543,7 @@ int gbntt_debug_lookback_timeout(unsigned int *flags, double *seconds)
     return read_errors(flags);
 }
 
-// Residues of a radix-3 product before Garner (mode 1) or of A after the
+// Residues of a radix-3 product before Garner (mode 1) or of 3 A after the
 // forward and inverse radix-3 stages alone (mode 0): q0 words to d_q0, p3
 // words to d_p3, 3 2^k of each (device pointers).
 int gbntt_debug_radix3(uint64_t *d_q0, uint32_t *d_p3, const uint32_t *d_a, size_t na, const uint32_t *d_b,

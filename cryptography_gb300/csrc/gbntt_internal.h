@@ -186,7 +186,7 @@ struct R3Args {
     const uint32_t *const *limb_tab;     // ... or of W products (device tables)
     const long long *len_tab;
     const void *hi, *lo;                 // rho^(i 2^15), i < 3 2^15, and rho^i, i < 2^15 (the field's multiply form)
-    uint64_t c, inv2, inv3, inv6, c3;    // (om - om^2) / 2, 1/2, 1/3, 1/6, c / 3 in the same form
+    uint64_t c;                          // (om - om^2) / 2 in the same form
     uint64_t step;                       // w^G (forward) or w^-G (inverse), G = blocks x 256, same form
     int blocks;                          // grid x (at most 65535)
 };

@@ -16,10 +16,10 @@
 // give cyclic convolutions of length M), and the pointwise products pair
 // them up.
 // Inverse (decimation in time), in place, after the three M-point inverse
-// transforms (which scale by 1/M):
+// transforms (which scale by 1/(3 M): the 1/3 rides on their scale):
 //   t_0 = z_0[j], t_m = z_m[j] w^(-jm), s = t_1 + t_2, d = t_1 - t_2
-//   x[j] = (t_0 + s) / 3, x[j + M] = (t_0 - s / 2 - c d) / 3,
-//   x[j + 2M] = (t_0 - s / 2 + c d) / 3.
+//   x[j] = t_0 + s, x[j + M] = t_0 - s / 2 - c d, x[j + 2M] = t_0 - s / 2 + c d.
+// Halving is a shift and a conditional add of (p + 1) / 2, not a multiply.
 // A thread's first power of w comes from two-level tables of
 // rho = g^((p-1)/(3 2^30)): w^j = rho^(j 2^(30-k)) = hi[e >> 15]
 // lo[e & (2^15 - 1)], e < 3 2^30; its later ones by one multiply each.
@@ -37,6 +37,18 @@ namespace {
 
 constexpr long long kR3Order = 3LL << 30;   // order of rho
 
+// x / 2 mod p for a residue x of the field's range: x >> 1, plus (p + 1) / 2
+// when x is odd ((x - 1) / 2 + (p + 1) / 2 = (x + p) / 2, no overflow; a
+// canonical x gives a canonical result, and lazy q0 values below 2^64 stay
+// below 2^64).
+template <int PI>
+__device__ __forceinline__ typename Field<PI>::T r3_half(typename Field<PI>::T x)
+{
+    using V = typename Field<PI>::T;
+    constexpr V kHalfUp = PI == 3 ? (V)((kP3 + 1u) / 2u) : (V)(0xFFFFFFFF00000001ull / 2 + 1);
+    return (x >> 1) + ((x & 1) ? kHalfUp : (V)0);
+}
+
 template <int PI>
 __device__ __forceinline__ typename Field<PI>::T r3_pow(const R3Args &a, long long e)
 {
@@ -50,7 +62,7 @@ __device__ __forceinline__ typename Field<PI>::T r3_pow(const R3Args &a, long lo
 // of them per loop step with all their loads issued first. Its twiddle w^j
 // comes from the tables once and is then multiplied by w^G per j.
 template <int PI>
-__global__ void __launch_bounds__(256) radix3_fwd_kernel(const R3Args a)
+__global__ void __launch_bounds__(256, 4) radix3_fwd_kernel(const R3Args a)
 {
     using F = Field<PI>;
     using V = typename F::T;
@@ -60,7 +72,7 @@ __global__ void __launch_bounds__(256) radix3_fwd_kernel(const R3Args a)
     const uint32_t *x = a.limb_tab ? a.limb_tab[w] : a.limbs;
     const long long n = a.len_tab ? a.len_tab[w] : a.n_limbs;
     V *out = (V *)a.spec + w * 3 * M;
-    const V c = (V)a.c, inv2 = (V)a.inv2, step = (V)a.step;
+    const V c = (V)a.c, step = (V)a.step;
     long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (j >= M) return;
     V w1 = r3_pow<PI>(a, j << a.shift);
@@ -81,7 +93,7 @@ __global__ void __launch_bounds__(256) radix3_fwd_kernel(const R3Args a)
             if (jj < M) {
                 const V x0 = F::from_u32(v[u][0]), x1 = F::from_u32(v[u][1]), x2 = F::from_u32(v[u][2]);
                 const V s = F::add(x1, x2), d = F::sub(x1, x2);
-                const V t = F::sub(x0, F::mul(s, inv2)), e = F::mul(d, c);
+                const V t = F::sub(x0, r3_half<PI>(s)), e = F::mul(d, c);
                 const V w2 = F::mul(w1, w1);
                 out[jj] = F::add(x0, s);
                 out[M + jj] = F::mul(F::add(t, e), w1);
@@ -93,7 +105,7 @@ __global__ void __launch_bounds__(256) radix3_fwd_kernel(const R3Args a)
 }
 
 template <int PI>
-__global__ void __launch_bounds__(256) radix3_inv_kernel(const R3Args a)
+__global__ void __launch_bounds__(256, 4) radix3_inv_kernel(const R3Args a)
 {
     using F = Field<PI>;
     using V = typename F::T;
@@ -101,7 +113,7 @@ __global__ void __launch_bounds__(256) radix3_inv_kernel(const R3Args a)
     const long long M = a.M, w = blockIdx.y;
     const long long G = (long long)gridDim.x * blockDim.x;
     V *z = (V *)a.spec + w * 3 * M;
-    const V c3 = (V)a.c3, inv3 = (V)a.inv3, inv6 = (V)a.inv6, step = (V)a.step;
+    const V c = (V)a.c, step = (V)a.step;
     long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (j >= M) return;
     const long long ex = j << a.shift;
@@ -121,8 +133,8 @@ __global__ void __launch_bounds__(256) radix3_inv_kernel(const R3Args a)
                 const V w2 = F::mul(w1, w1);
                 const V t1 = F::mul(v[u][1], w1), t2 = F::mul(v[u][2], w2);
                 const V s = F::add(t1, t2), d = F::sub(t1, t2);
-                const V a0 = F::mul(v[u][0], inv3), q = F::sub(a0, F::mul(s, inv6)), e = F::mul(d, c3);
-                z[jj] = F::add(a0, F::mul(s, inv3));
+                const V t0 = v[u][0], q = F::sub(t0, r3_half<PI>(s)), e = F::mul(d, c);
+                z[jj] = F::add(t0, s);
                 z[M + jj] = F::sub(q, e);
                 z[2 * M + jj] = F::add(q, e);
             }

@@ -225,8 +225,8 @@ int gbntt_debug_forward(uint64_t *d_out, const uint32_t *d_in, size_t n, int log
 
 /* Residues of the 3 2^k-point transform path, two-prime set: mode 1, the
  * cyclic convolution of a and b of length 3 2^k (n_a + n_b - 1 <= 3 2^k)
- * before Garner; mode 0, a itself after the forward and inverse radix-3
- * stages alone. d_q0 receives 3 2^k q0 residues (uint64), d_p3 3 2^k p3
+ * before Garner; mode 0, 3 a after the forward and inverse radix-3 stages
+ * alone (the 1/3 belongs to the inverse sub-transforms' scale). d_q0 receives 3 2^k q0 residues (uint64), d_p3 3 2^k p3
  * residues (uint32); device pointers. For known-answer tests. */
 int gbntt_debug_radix3(uint64_t *d_q0, uint32_t *d_p3, const uint32_t *d_a, size_t na, const uint32_t *d_b,
                        size_t nb, int k, int mode);

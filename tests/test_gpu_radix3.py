@@ -110,7 +110,8 @@ def _cyclic(a, b, n):
 
 @pytest.mark.parametrize("k", [10, 11, 13])
 def test_radix3_stage_residues(r3engine, k):
-    # the radix-3 stages alone invert each other (mode 0), and the whole
+    # the radix-3 stages alone give 3 a (mode 0: the 1/3 is applied by the
+    # inverse sub-transforms' scale), and the whole
     # transform path gives the cyclic convolution mod q0 and p3 (mode 1),
     # for operands that fill all three thirds and for short ones
     rng = np.random.default_rng(900 + k)
@@ -121,7 +122,7 @@ def test_radix3_stage_residues(r3engine, k):
         dq, dp = cudart.DeviceBuffer(8 * M3), cudart.DeviceBuffer(4 * M3)
         assert r3engine.lib().gbntt_debug_radix3(dq.ptr, dp.ptr, da.ptr, na, db.ptr, nb, k, mode) == 0
         q, p = dq.download(np.uint64, M3), dp.download(np.uint32, M3)
-        want = [int(x) for x in a] + [0] * (M3 - na) if mode == 0 else _cyclic(a, b, M3)
+        want = [3 * int(x) for x in a] + [0] * (M3 - na) if mode == 0 else _cyclic(a, b, M3)
         assert [int(x) % Q0 for x in q] == [v % Q0 for v in want], (k, na, nb, mode)
         assert [int(x) % P3 for x in p] == [v % P3 for v in want], (k, na, nb, mode)
         for x in (da, db, dq, dp):
