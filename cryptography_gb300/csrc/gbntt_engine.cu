@@ -1544,6 +1544,7 @@ namespace {
 struct SrvRequest {
     BatchItem item;
     int L = 0;
+    int r3 = 0;      // transform of 3 2^L points (a product alone over the radix-3 threshold)
     int state = 0;   // 0 pending, 1 running, 2 done
     std::chrono::steady_clock::time_point t_submit, t_done;
 };
@@ -1607,7 +1608,7 @@ void CUDART_CB srv_done_cb(void *p)
 // slot workspace: they run one after the other). The tables of all
 // sub-waves are filled into one host table slot and go up in one copy.
 // Launches directly (no wave graphs: group layouts rarely repeat).
-int srv_activation(Server *S, SrvSlot &sl, const std::vector<int> &gL,
+int srv_activation(Server *S, SrvSlot &sl, const std::vector<int> &gL, const std::vector<int> &g3,
                    const std::vector<std::vector<BatchItem>> &gitems, std::vector<std::vector<uint64_t>> &gids)
 {
     BatchCtx &x = sl.ctx;
@@ -1628,7 +1629,7 @@ int srv_activation(Server *S, SrvSlot &sl, const std::vector<int> &gL,
         uint64_t *hA = hg, *hLA = hg + W, *hB = hg + 2 * W, *hLB = hg + 3 * W, *hC = hg + 4 * W, *hNC = hg + 5 * W,
                  *hTS = hg + 6 * W;
         long long t = 0;
-        bool sb = W > 1;
+        bool sb = W > 1 && !g3[gi];
         for (long long k = 0; k < W; k++) {
             const BatchItem &it = items[k];
             if (it.b != items[0].b || it.nb != items[0].nb || it.a == it.b) sb = false;
@@ -1653,7 +1654,7 @@ int srv_activation(Server *S, SrvSlot &sl, const std::vector<int> &gL,
     *x.slot = slot ^ 1;
     for (size_t gi = 0; gi < ng; gi++) {
         const int rc = wave_launches(x, dtab + off[gi], (long long)gitems[gi].size(), gL[gi], sl.stream, nullptr,
-                                     tiles[gi], shared[gi] != 0);
+                                     tiles[gi], shared[gi] != 0, false, g3[gi] != 0);
         if (rc) return rc;
         SrvDone *d = new SrvDone{S, &sl, std::move(gids[gi]), gi + 1 == ng};
         const cudaError_t e = cudaLaunchHostFunc(sl.stream, srv_done_cb, d);
@@ -1671,7 +1672,7 @@ int srv_activation(Server *S, SrvSlot &sl, const std::vector<int> &gL,
 // kMaxBatch requests) and starts them as one activation of that slot.
 void server_loop(Server *S)
 {
-    std::vector<int> gL;
+    std::vector<int> gL, g3;
     std::vector<std::vector<BatchItem>> gitems;
     std::vector<std::vector<uint64_t>> gids;
     for (;;) {
@@ -1697,23 +1698,26 @@ void server_loop(Server *S)
             sl = free_slot();
             std::map<int, size_t> group_of;
             gL.clear();
+            g3.clear();
             gitems.clear();
             gids.clear();
             size_t used = 0;
             while (!S->pending.empty() && count < (size_t)kMaxBatch) {
                 const uint64_t id = S->pending.front();
                 SrvRequest &r = S->reqs[id];
-                const size_t need = (size_t)1 << r.L;
+                const size_t need = (size_t)(r.r3 ? 3 : 1) << r.L;
                 if (count > 0 && used + need > S->cap) break;
                 used += need;
                 count++;
                 r.state = 1;
-                auto it = group_of.find(r.L);
+                const int key = 2 * r.L + r.r3;
+                auto it = group_of.find(key);
                 size_t gi;
                 if (it == group_of.end()) {
                     gi = gL.size();
-                    group_of[r.L] = gi;
+                    group_of[key] = gi;
                     gL.push_back(r.L);
+                    g3.push_back(r.r3);
                     gitems.emplace_back();
                     gids.emplace_back();
                 } else {
@@ -1728,16 +1732,19 @@ void server_loop(Server *S)
         // shortest transforms first: their requests complete earliest
         std::vector<size_t> order(gL.size());
         for (size_t i = 0; i < order.size(); i++) order[i] = i;
-        std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return gL[a] < gL[b]; });
-        std::vector<int> sL;
+        std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+            return ((g3[a] ? 3ull : 1ull) << gL[a]) < ((g3[b] ? 3ull : 1ull) << gL[b]);
+        });
+        std::vector<int> sL, s3;
         std::vector<std::vector<BatchItem>> sitems;
         std::vector<std::vector<uint64_t>> sids;
         for (size_t i : order) {
             sL.push_back(gL[i]);
+            s3.push_back(g3[i]);
             sitems.push_back(std::move(gitems[i]));
             sids.push_back(std::move(gids[i]));
         }
-        const int rc = srv_activation(S, *sl, sL, sitems, sids);
+        const int rc = srv_activation(S, *sl, sL, s3, sitems, sids);
         S->activations++;
         S->wave_products += count;
         if (rc) {
@@ -2407,6 +2414,11 @@ int gbntt_server_submit(uint32_t *d_c, const uint32_t *d_a, size_t na, const uin
     SrvRequest &r = S->reqs.back();
     r.item = BatchItem{d_c, d_a, d_b, na, nb};
     r.L = L;
+    const int k3 = r3_log(na, nb);   // the single-product rule: the server cannot count future requests
+    if (k3 >= g.r3_min_log) {
+        r.L = k3;
+        r.r3 = 1;
+    }
     r.t_submit = std::chrono::steady_clock::now();
     S->pending.push_back(id);
     *ticket = id;

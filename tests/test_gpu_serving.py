@@ -51,3 +51,35 @@ def test_serving_mix_equals_alone(engine):
         for buf in (da, db, dc):
             buf.free()
     assert engine.device_errors() == 0
+
+
+def test_serving_radix3_requests(engine):
+    # requests large enough for transforms of 3 2^k points on their own
+    # (k >= 20), power-of-two ones of the same sizes and small ones, in one
+    # stream of submissions: every product equals GMP's
+    rng = np.random.default_rng(77)
+    srv = engine.Server(slots=2, slot_log=24)
+    sizes = [(3 << 19, 3 << 19), ((3 << 20) - 7, 3 << 20), ((1 << 21) + 1, 1 << 21), (1 << 21, (1 << 21) - 1),
+             (3 << 19, 1000), (500, 700), (3 << 18, 3 << 18), (40000, 3 << 20)]
+    reqs = []
+    try:
+        for na, nb in sizes:
+            a = rng.integers(0, 1 << 32, na, dtype=np.uint64).astype(np.uint32)
+            b = rng.integers(0, 1 << 32, nb, dtype=np.uint64).astype(np.uint32)
+            da, db, dc = cudart.DeviceBuffer(4 * na), cudart.DeviceBuffer(4 * nb), cudart.DeviceBuffer(4 * (na + nb))
+            da.upload(a)
+            db.upload(b)
+            reqs.append((srv.submit(dc.ptr, da.ptr, na, db.ptr, nb), a, b, da, db, dc))
+        for t, *_ in reqs:
+            srv.wait(t, 120.0)
+        assert srv.stats()["device_errors"] == 0
+        for t, a, b, da, db, dc in reqs:
+            got = dc.download(np.uint32, len(a) + len(b))
+            want = oracle.gmp_mul(a, b) if oracle.gmp_available() else oracle.mul(a, b)
+            assert np.array_equal(got[:len(want)], want) and not got[len(want):].any(), (len(a), len(b))
+    finally:
+        srv.stop()
+    for _, _, _, da, db, dc in reqs:
+        for buf in (da, db, dc):
+            buf.free()
+    assert engine.device_errors() == 0
