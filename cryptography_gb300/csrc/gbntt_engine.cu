@@ -326,7 +326,8 @@ static size_t workspace_bytes(int max_log)
     const size_t n = (size_t)1 << max_log;
     const size_t spec = 6 * n * sizeof(uint64_t);
     const size_t tw = 4 * 2 * 2 * (size_t)kTwSize * sizeof(uint64_t) + 2 * 2 * (size_t)kTwSize * sizeof(uint32_t) +
-                      4 * 2 * (size_t)kStep1Words * sizeof(uint64_t) + 2 * (size_t)kStep1Words * sizeof(uint32_t);
+                      4 * 2 * (size_t)kStep1Words * sizeof(uint64_t) + 2 * (size_t)kStep1Words * sizeof(uint32_t) +
+                      4 * (size_t)kTwSize * (2 * sizeof(uint64_t) + sizeof(uint32_t));   // radix-3 rho tables
     const size_t ctl = (2 + status_words(n)) * sizeof(unsigned);
     const size_t io = (4 * n + 64) * sizeof(uint32_t);
     return spec + tw + ctl + io;
