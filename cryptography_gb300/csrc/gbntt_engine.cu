@@ -878,6 +878,10 @@ static int radix3_stage(const PrimeSet &ps, uint64_t *spec, size_t stride, int k
 {
     for (int q = 0; q < ps.n; q++) {
         const int pi = ps.pi[q];
+        if (!g.d_r3[pi]) {   // only q0 (both forms) and p3 have radix-3 tables
+            set_err("radix-3 transform on prime %d (two-prime set only)", pi);
+            return GBNTT_ERR_ARG;
+        }
         R3Args a;
         memset(&a, 0, sizeof a);
         a.spec = spec + q * stride;
@@ -2324,6 +2328,10 @@ int gbntt_set_prime_set(int nprimes)
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     if (nprimes != 2 && nprimes != 3) { set_err("gbntt_set_prime_set: 2 or 3 primes"); return GBNTT_ERR_ARG; }
     if (!g.ready) { set_err("engine not initialised"); return GBNTT_ERR_NOT_INIT; }
+    if (g_srv) {   // its thread reads the prime set per sub-wave, and its requests were sized for it
+        set_err("gbntt_set_prime_set: stop the server first");
+        return GBNTT_ERR_ARG;
+    }
     cudaStreamSynchronize(g.stream);
     g.prime_set = nprimes;
     invalidate_wave_graphs();

@@ -352,7 +352,8 @@ int gbntt_compute_e(long digits, char *out, size_t cap, double *phase_seconds);
  * the default; 3 = the reference's three 64-bit primes. Products are
  * identical either way. Packed (64-bit coefficient) products always use
  * three 64-bit primes. The default comes from GBNTT_PRIMES (2 or 3) at
- * init. gbntt_prime_set returns 0 when no engine is initialised. */
+ * init. gbntt_prime_set returns 0 when no engine is initialised. Refused
+ * (GBNTT_ERR_ARG) while the serving loop runs. */
 int gbntt_set_prime_set(int nprimes);
 int gbntt_prime_set(void);
 

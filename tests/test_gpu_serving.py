@@ -59,6 +59,9 @@ def test_serving_radix3_requests(engine):
     # stream of submissions: every product equals GMP's
     rng = np.random.default_rng(77)
     srv = engine.Server(slots=2, slot_log=24)
+    with pytest.raises(engine.EngineError):   # the server's requests are sized for the prime set
+        engine.set_prime_set(3)
+    assert engine.prime_set() == 2
     sizes = [(3 << 19, 3 << 19), ((3 << 20) - 7, 3 << 20), ((1 << 21) + 1, 1 << 21), (1 << 21, (1 << 21) - 1),
              (3 << 19, 1000), (500, 700), (3 << 18, 3 << 18), (40000, 3 << 20)]
     reqs = []
