@@ -1098,7 +1098,8 @@ static int mul_dev64(uint64_t *d_c, const uint64_t *d_a, size_t na, const uint64
 
 // Batched products: bucket by transform length, then run waves of up to
 // W = min(kMaxBatch, cap / N) products through the same pass kernels (a
-// wave of W transforms of N points is, for a pass, W N / 2^l columns) and the
+// wave of W transforms of N points is, for a pass, W N / 2^l columns; a wave
+// of W transforms of 3 2^k points is 3 W sub-transforms of 2^k) and the
 // batched carry kernel. Per-product pointers and lengths travel in device
 // tables, so every launch of a wave has fixed arguments. A context is one
 // workspace (the engine's, or a slice of it owned by a serving slot).
@@ -1256,8 +1257,9 @@ static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaSt
 // cudaGraphLaunch from then on. Every argument of the captured launches is
 // fixed for the key: the tables live at the slot's device address and are
 // refreshed by the upload that precedes each replay, and the carry grid is
-// the key's upper bound on carry tiles, W ceil((2^L + 1) / 2048), whose
-// surplus CTAs take the highest tickets and exit at once. Anything that
+// the key's upper bound on carry tiles, W ceil((2^L + 1) / 2048) (3 2^L for
+// a radix-3 wave), whose surplus CTAs take the highest tickets and exit at
+// once. Anything that
 // changes the captured launches (plans, prime set, freed contexts) drops the
 // cache through invalidate_wave_graphs().
 struct WaveKey {
@@ -1536,8 +1538,9 @@ int batch_mul_wrap(uint32_t *const *d_c, const uint32_t *const *d_a, const size_
 // free, the server admits pending requests in arrival order, of any
 // transform length, while the sum of their transform lengths fits the slot
 // (the HBM-footprint admission: 48 N bytes per product against the slot's
-// 48 cap bytes; at most kMaxBatch), and runs them as one sub-wave per
-// length, shortest first, back to back on the slot's stream
+// 48 cap bytes, N = 2^L or, for a product over the radix-3 threshold,
+// 3 2^k; at most kMaxBatch), and runs them as one sub-wave per length,
+// shortest first, back to back on the slot's stream
 // (srv_activation). Waves in different slots overlap on the device. The
 // server thread sleeps on a condition variable: a host callback enqueued
 // after each sub-wave (srv_done_cb) marks its requests done, the one after
@@ -1672,9 +1675,10 @@ int srv_activation(Server *S, SrvSlot &sl, const std::vector<int> &gL, const std
 // The server thread: sleeps on the condition variable until a request is
 // pending and a slot is free (submissions and sub-wave completions notify
 // it), then admits pending requests in arrival order while their transform
-// lengths fit one slot workspace (the sum of 2^L over the admitted
-// requests, HBM-footprint admission; at least the oldest request; at most
-// kMaxBatch requests) and starts them as one activation of that slot.
+// lengths fit one slot workspace (the sum of 2^L, or 3 2^L, over the
+// admitted requests, HBM-footprint admission; at least the oldest request;
+// at most kMaxBatch requests) and starts them as one activation of that
+// slot, one sub-wave per transform length.
 void server_loop(Server *S)
 {
     std::vector<int> gL, g3;
