@@ -70,6 +70,7 @@ def parse():
     ap.add_argument("--no-square", action="store_true", help="skip the squaring and 2^20-limb legs")
     ap.add_argument("--no-radix3", action="store_true",
                     help="skip the leg timing products of 3 2^k points against the next power of two")
+    ap.add_argument("--radix3-logs", default="20,22,24", help="radix-3 leg: the k of its 3 2^k-point products")
     ap.add_argument("--no-e", action="store_true", help="skip the e-digits leg")
     ap.add_argument("--e-digits", type=int, default=10 ** 8)
     ap.add_argument("--e-reps", type=int, default=3)
@@ -677,7 +678,8 @@ def run_gpu(args, dist):
             buf.free()
         flags |= g.device_errors()
 
-    radix3 = None if args.no_radix3 else run_radix3_leg(g, cudart, synth, lg, stream)
+    radix3 = None if args.no_radix3 else run_radix3_leg(g, cudart, synth, lg, stream,
+                                                        [int(x) for x in args.radix3_logs.split(",") if x])
     if radix3:
         flags |= radix3["device_error_flags"]
 
@@ -873,15 +875,16 @@ def run_gpu(args, dist):
     return 0 if flags == 0 else 3
 
 
-def run_radix3_leg(g, cudart, synth, lg, stream):
+def run_radix3_leg(g, cudart, synth, lg, stream, logs):
     """Products whose coefficient count fits 3 2^k but not 2^(k+1): n x n
     limbs with 2 n - 1 = 3 2^k - 1 run a transform of 3 2^k points, timed
     against n + 1 x n + 1 limbs (3 2^k + 1 coefficients), which take the
     power of two 2^(k+2): nearly the same product, a third more points."""
-    out = {"sizes": [], "rule": "a product alone takes 3 2^k points from k = 20 (GBNTT_RADIX3_MIN_LOG)"}
+    out = {"sizes": [], "rule": "a product alone takes 3 2^k points from k = %s (GBNTT_RADIX3_MIN_LOG)"
+                                % os.environ.get("GBNTT_RADIX3_MIN_LOG", "20")}
     flags = 0
-    for k in (20, 22, 24):
-        if (3 << k) + 1 > (1 << (lg + 1)):
+    for k in logs:
+        if k < 10 or (3 << k) + 1 > (1 << (lg + 1)):
             continue
         n3 = 3 << (k - 1)
         xa, xb = synth.operand(n3 + 1, 31), synth.operand(n3 + 1, 32)
@@ -889,7 +892,7 @@ def run_radix3_leg(g, cudart, synth, lg, stream):
         rc = cudart.DeviceBuffer(8 * (n3 + 1))
         ra.upload(xa)
         rb.upload(xb)
-        reps = max(5, 40 >> (k - 20))
+        reps = min(200, 40 << (20 - k)) if k < 20 else max(5, 40 >> (k - 20))
 
         def timed(nn):
             for _ in range(2):
