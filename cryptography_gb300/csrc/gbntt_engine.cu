@@ -716,6 +716,7 @@ static int inverse(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, s
     memset(&a, 0, sizeof a);
     a.other_log = shared_b ? L : 0;
     a.other_pair_log = !shared_b && pair_b ? L : 0;
+    a.other_r3 = third && (shared_b || pair_b) ? 1 : 0;   // the shared spectra are per sub-transform
     for (int k = 0; k < ps.n; k++) {
         const int pi = ps.pi[k];
         a.data[k] = specA + k * stride;
@@ -765,8 +766,11 @@ static bool fuse_inner(int L)
 // prime, in place in specA (see ntt_inner_fused_kernel). Runs between
 // forward(..., skip_last) of both operands and inverse(..., skip_first).
 static int inner_fused(const PrimeSet &ps, uint64_t *specA, const uint64_t *specB, size_t stride, int L,
-                       cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr, bool pair_b = false)
+                       cudaStream_t st, bool square, long long W = 1, cudaStream_t aux = nullptr, bool pair_b = false,
+                       bool r3 = false)
 {
+    // r3: W counts sub-transforms of 2^L points of products of 3 2^L (pairs
+    // then share per sub-transform)
     int pl[kMaxPasses];
     const int np = plan_passes(L, pl);
     const int l = pl[np - 1];
@@ -783,6 +787,7 @@ static int inner_fused(const PrimeSet &ps, uint64_t *specA, const uint64_t *spec
     a.log_s = 0;
     a.ncols = W << (L - l);
     a.other_pair_log = pair_b ? L : 0;   // products 2i and 2i + 1 read specB's spectrum i
+    a.other_r3 = pair_b && r3 ? 1 : 0;
     for (int k = 0; k < ps.n; k++) {
         const int pi = ps.pi[k];
         const double nbw = word_bytes(pi) * (double)((size_t)1 << L) * (double)W;
@@ -1143,8 +1148,8 @@ static int batch_wave(BatchCtx &x, const BatchItem *items, long long W, int L, c
     // shared divisor or reciprocal): its transform is computed once; products
     // 2i and 2i + 1 multiplying by the same one (a product tree's B_L B_R and
     // P_L B_R): one transform per pair
-    bool shared_b = W > 1 && !r3;
-    bool pair_b = W > 1 && W % 2 == 0 && !r3;
+    bool shared_b = W > 1;
+    bool pair_b = W > 1 && W % 2 == 0;
     for (long long k = 0; k < W; k++) {
         const BatchItem &it = items[k];
         const BatchItem &mate = items[k ^ 1];
@@ -1189,19 +1194,23 @@ static int wave_launches(BatchCtx &x, uint64_t *dtab, long long W, int L, cudaSt
     int rc = GBNTT_OK;
     if (r3) {
         // products of length 3 2^L: each operand's radix-3 stage, then its
-        // three sub-transforms as a batch of 3 W for the pass chain
-        const bool fused = fuse_inner(L);
+        // three sub-transforms as a batch of 3 W for the pass chain (a
+        // shared right operand: one product's three; pairs: W / 2 products')
+        const bool fused = !shared_b && fuse_inner(L);
         for (int o = 0; o < 2; o++) {
             uint64_t *spec = o ? specB : specA;
-            rc = radix3_stage(ps, spec, x.cap, L, W, false, nullptr, 0, (const uint32_t *const *)(dtab + 2 * o * W),
+            const long long Wo = o == 0 ? W : shared_b ? 1 : pair_b ? W / 2 : W;
+            rc = radix3_stage(ps, spec, x.cap, L, Wo, false, nullptr, 0, (const uint32_t *const *)(dtab + 2 * o * W),
                               (const long long *)(dtab + (2 * o + 1) * W), st, aux);
             if (rc) return rc;
-            rc = forward(ps, spec, x.cap, nullptr, 0, L, st, false, 3 * W, nullptr, nullptr, aux, nullptr, true, nullptr,
-                         fused);
+            rc = forward(ps, spec, x.cap, nullptr, 0, L, st, false, 3 * Wo, nullptr, nullptr, aux, nullptr, true,
+                         nullptr, fused);
             if (rc) return rc;
         }
-        if (fused && (rc = inner_fused(ps, specA, specB, x.cap, L, st, false, 3 * W, aux)) != GBNTT_OK) return rc;
-        if ((rc = inverse(ps, specA, specB, x.cap, L, st, false, 3 * W, aux, false, fused, false, true)) != GBNTT_OK)
+        if (fused && (rc = inner_fused(ps, specA, specB, x.cap, L, st, false, 3 * W, aux, pair_b, true)) != GBNTT_OK)
+            return rc;
+        if ((rc = inverse(ps, specA, specB, x.cap, L, st, false, 3 * W, aux, shared_b, fused, pair_b, true)) !=
+            GBNTT_OK)
             return rc;
         if ((rc = radix3_stage(ps, specA, x.cap, L, W, true, nullptr, 0, nullptr, nullptr, st, aux)) != GBNTT_OK)
             return rc;
@@ -1454,18 +1463,26 @@ static int batch_mul(uint32_t *const *d_c, const uint32_t *const *d_a, const siz
                 i++;
             }
         }
-        // the other products (no right operand shared with a neighbour, not
-        // cyclic, not a split's chunk) take a transform of 3 2^k points where
-        // it is shorter than the power of two
-        // (enough of them: c products of 3 2^k points with c 2^k >= 2^r3_min_log)
+        // products (not cyclic, not a split's chunk) take a transform of
+        // 3 2^k points where it is shorter than the power of two and there
+        // is enough of them: c products of 3 2^k points with
+        // c 2^k >= 2^r3_min_log. A pair takes it for both or neither (its
+        // right operand's transform is shared); a run sharing one right
+        // operand is split by length as before, each length's wave sharing it.
         std::vector<int> k3s(all.size(), -1);
         long long count3[kMaxLog + 1] = {};
+        auto eligible = [](const Keyed &u) { return u.chunk || u.item.nc ? -1 : r3_log(u.item.na, u.item.nb); };
         for (size_t i = 0; i < all.size(); i++) {
-            const Keyed &u = all[i];
-            if (u.paired || u.chunk || u.item.nc) continue;
-            if ((i > 0 && all[i - 1].item.b == u.item.b) || (i + 1 < all.size() && all[i + 1].item.b == u.item.b))
+            const int k3 = eligible(all[i]);
+            if (all[i].paired) {   // pairs were marked as neighbours (i, i + 1), first to last
+                const int k3v = i + 1 < all.size() ? eligible(all[i + 1]) : -1;
+                if (k3 >= 0 && k3 == k3v) {
+                    k3s[i] = k3s[i + 1] = k3;
+                    count3[k3] += 2;
+                }
+                i++;
                 continue;
-            const int k3 = r3_log(u.item.na, u.item.nb);
+            }
             if (k3 >= 0) {
                 k3s[i] = k3;
                 count3[k3]++;

@@ -54,6 +54,9 @@ struct PassArgs {
     const uint64_t *other[3];   // second spectrum for the fused pointwise product
     int other_log;              // nonzero: one shared second spectrum of 2^other_log points for every product
     int other_pair_log;         // nonzero: products 2i and 2i + 1 (of 2^other_pair_log points) share second spectrum i
+    int other_r3;               // with either: products of 3 2^k points, k = that log, run as sub-transforms
+                                // s = 3 p + m of 2^k points; product p's part m reads the second spectrum's
+                                // sub-transform m (shared) or 3 (p >> 1) + m (pairs)
     const uint32_t *limbs;      // 32-bit limbs for the fused decomposition
     const uint64_t *limbs64;    // 64-bit limbs (one per coefficient) for the packed mode
     // batched first pass: product b's limbs are limb_tab[b][0 .. len_tab[b]),

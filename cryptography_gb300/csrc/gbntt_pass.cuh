@@ -189,9 +189,16 @@ __device__ __forceinline__ typename Field<PI>::T tile_in(const typename Field<PI
 
 // Position in the second spectra of element addr of the product spectra: the
 // same, within the one shared spectrum (other_log), or within the spectrum
-// a pair of products shares (other_pair_log).
+// a pair of products shares (other_pair_log); for transforms of 3 2^k
+// points (other_r3) the same per sub-transform of 2^k points.
 __device__ __forceinline__ long long other_index(const PassArgs &a, long long addr)
 {
+    const int k = a.other_log ? a.other_log : a.other_pair_log;
+    if (a.other_r3 && k) {   // sub-transform s = 3 p + m of product p (2^k points each)
+        const long long s = addr >> k, p = s / 3, m = s - 3 * p;
+        const long long bs = a.other_log ? m : 3 * (p >> 1) + m;
+        return (bs << k) | (addr & ((1LL << k) - 1));
+    }
     if (a.other_log) return addr & ((1LL << a.other_log) - 1);
     if (a.other_pair_log) {
         const int L = a.other_pair_log;
@@ -201,9 +208,10 @@ __device__ __forceinline__ long long other_index(const PassArgs &a, long long ad
 }
 
 // The second spectra for a contiguous tile [base, base + span) of the
-// product spectra: when the tile lies within one product, other_index is a
-// constant offset off over it (returns true; off = 0 without a shared
-// spectrum), else it must be applied per element (returns false).
+// product spectra: when the tile lies within one product (one sub-transform
+// for other_r3), other_index is a constant offset off over it (returns true;
+// off = 0 without a shared spectrum), else it must be applied per element
+// (returns false).
 __device__ __forceinline__ bool other_tile_offset(const PassArgs &a, long long base, long long span, long long &off)
 {
     off = 0;

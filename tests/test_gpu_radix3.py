@@ -220,22 +220,26 @@ def test_radix3_pinned_host_operands(r3engine):
 def test_radix3_batches(r3engine):
     engine = r3engine
     # a batch mixing radix-3 products with power-of-two ones, pairs sharing
-    # a right operand and a run sharing one right operand (those keep the
-    # power-of-two transforms and their shared spectra); two rounds so the
-    # second replays the wave graphs
+    # a right operand (one transform per pair, per sub-transform for 3 2^k
+    # points) and a run sharing one right operand, whose radix-3 and
+    # power-of-two lengths become two waves each transforming it once; two
+    # rounds so the second replays the wave graphs
     rng = np.random.default_rng(29)
-    shared = _rand(rng, 2500)
+    shared = _rand(rng, 2000)
     pair_b = _rand(rng, 5000)
+    pair_c = _rand(rng, 3000)
     for rnd in range(2):
         A, B = [], []
         for n in rng.integers(1100, 30000, 24):
             A.append(_rand(rng, int(n)))
             B.append(_rand(rng, int(rng.integers(1100, 30000))))
-        for _ in range(4):
-            A.append(_rand(rng, 4000))
+        for n in (4000, 4000, 4300, 4100, 4300, 3900):   # 5999 / 6099 <= 3 2^11; 6299 > 3 2^11
+            A.append(_rand(rng, n))
             B.append(shared)
-        A += [_rand(rng, 5000), _rand(rng, 4500)]
+        A += [_rand(rng, 5000), _rand(rng, 4500)]        # a pair at 3 2^12 points
         B += [pair_b, pair_b]
+        A += [_rand(rng, 3000), _rand(rng, 3200)]        # a pair split by length: 5999 and 6199
+        B += [pair_c, pair_c]
         da, db = _upload(A), _upload(B)
         dc = [cudart.DeviceBuffer(4 * (len(a) + len(b))) for a, b in zip(A, B)]
         call = lambda: engine.batch_mul_device([c.ptr for c in dc], [x.ptr for x in da], [len(a) for a in A],
@@ -274,3 +278,32 @@ def test_radix3_batch_one_size(r3engine):
         x.free()
     assert engine.device_errors() == 0
 
+
+
+def test_radix3_shared_and_paired_waves_alone(r3engine):
+    # batches made only of products sharing one right operand (radix-3 and
+    # power-of-two lengths: two shared waves) and only of pairs (radix-3
+    # pairs: the right operands' sub-transforms shared per pair)
+    engine = r3engine
+    rng = np.random.default_rng(41)
+    b = _rand(rng, 2000)
+    A = [_rand(rng, n) for n in (4000, 4100, 4300, 3900, 4000, 4300, 2500)]
+    B = [b] * len(A)
+    bs = [_rand(rng, 7000 + 50 * i) for i in range(4)]
+    A2, B2 = [], []
+    for i, bb in enumerate(bs):                        # pairs: n + 7000.. - 1 <= 3 2^12
+        A2 += [_rand(rng, 5000 - 100 * i), _rand(rng, 4800 - 100 * i)]
+        B2 += [bb, bb]
+    for AA, BB in ((A, B), (A2, B2)):
+        da, db = _upload(AA), _upload(BB)
+        dc = [cudart.DeviceBuffer(4 * (len(x) + len(y))) for x, y in zip(AA, BB)]
+        call = lambda: (engine.batch_mul_device([c.ptr for c in dc], [x.ptr for x in da], [len(x) for x in AA],
+                                                [x.ptr for x in db], [len(y) for y in BB]), cudart.synchronize())
+        kinds = _kinds(engine, call)
+        assert {"radix3_fwd", "radix3_inv"} <= kinds, kinds
+        call()                                         # again without the launch log (second stream)
+        for i, (x, y, c) in enumerate(zip(AA, BB, dc)):
+            assert np.array_equal(c.download(np.uint32, len(x) + len(y)), _want(x, y)), (i, len(x), len(y))
+        for buf in da + db + dc:
+            buf.free()
+    assert engine.device_errors() == 0
