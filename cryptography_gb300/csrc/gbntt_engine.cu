@@ -862,10 +862,10 @@ struct StageJob {
 // 3/4 of 2^L coefficients), else -1. Two-prime set, 2^k of at least 2^10.
 // The radix-3 stage adds six launches and a sweep over the spectrum, which
 // the quarter fewer points repay from about 2^20-point sub-transforms on
-// (measured per product: 3 2^18 points 1.11 x the time of 2^20, 3 2^20
-// points 0.875 x that of 2^22, 3 2^22 0.816 x): a product alone takes it
-// from k = r3_min_log, a batch for c products of one length when
-// c 2^k >= 2^r3_min_log (batch_mul).
+// (measured per product against the next power of two: 3 2^18 points
+// 1.02 x, 3 2^19 0.99 x, 3 2^20 0.84 x, 3 2^22 0.81 x, 3 2^24 0.79 x): a
+// product alone takes it from k = r3_min_log, a batch for c products of one
+// length when c 2^k >= 2^r3_min_log (batch_mul).
 static int r3_log(size_t na, size_t nb)
 {
     if (!g.radix3 || g.prime_set != 2 || na == 0 || nb == 0) return -1;
@@ -906,7 +906,7 @@ static int radix3_stage(const PrimeSet &ps, uint64_t *spec, size_t stride, int k
         const long long per_block = 256LL * kR3Unroll;
         a.blocks = (int)std::min<long long>((a.M + per_block - 1) / per_block, 65535LL);
         const uint64_t pp = prime_value(pi), order = 3ull << kMaxLog;
-        uint64_t e = (uint64_t)(((unsigned __int128)(256ull * a.blocks) << a.shift) % order);
+        uint64_t e = (uint64_t)(((u128)(256ull * a.blocks) << a.shift) % order);
         if (inverse && e) e = order - e;
         const uint64_t step = h_pow(g.r3rho[pi], e, pp);
         a.step = pi == 3 ? h_mont3(step) : pi == 4 ? step : h_mont(step, pp);
